@@ -1,0 +1,214 @@
+/*
+ * opendust_gb300.h — C ABI of the GB300 superion step engine.
+ *
+ * This is the drop-in boundary for OpenDust's per-timestep superion update.
+ * In the reference (OpenDust, src/opendust/opendust.py) that update is an
+ * OpenMM program: a CustomNonbondedForce for ion–ion forces (opendust.py:471-485),
+ * one CustomExternalForce per grain (opendust.py:350-360, :487-495), a trap
+ * CustomExternalForce (opendust.py:552-577), a field force (opendust.py:579-585),
+ * a CustomIntegrator program (opendust.py:839-1037) driven by
+ * integrator.step(1) (opendust.py:1061), and a per-step host tail
+ * (opendust.py:1117-1383) that reads integrator globals back with
+ * getGlobalVariableByName and writes grain charges with context.setParameter.
+ * Every entry point below replaces one of those call sites; the citation on
+ * each declaration names the one it replaces.
+ *
+ * Conventions
+ *  - Plain C types only; the caller owns every host array, the library owns all
+ *    device memory it allocates.
+ *  - No exceptions cross the ABI: every call returns od_status; a message for the
+ *    last failure on a handle is returned by od_last_error(handle) (or by
+ *    od_last_error(NULL) for failures without a handle).
+ *  - One host thread per handle. Each handle owns one CUDA stream.
+ *  - All device-side waits inside the library are bounded; a wait that runs out
+ *    sets a device error word that the next host call reports as OD_ERR_TIMEOUT.
+ *  - Units at the boundary are SI (m, s, m/s, C, kg, N), as in the reference API.
+ *
+ * Random numbers (identical definition in the CUDA library and the CPU oracle)
+ *  Philox4x32-10 (Salmon et al., SC'11), key = (seed & 0xffffffff, seed >> 32),
+ *  counter = (ion index, step index, stream id, simulation id).
+ *  uniform  u = (w >> 8) * 2^-24            in [0,1)
+ *  uniform' u = ((w >> 8) + 1) * 2^-24      in (0,1]
+ *  gaussian pair from words (a,b): sqrt(-2 ln u'(a)) * (cos, sin)(2 pi u(b))
+ *  Stream ids are the OD_RNG_* constants below; the word use of each stream is
+ *  documented beside it.
+ */
+#ifndef OPENDUST_GB300_H
+#define OPENDUST_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OD_ABI_VERSION 1
+
+typedef enum od_status {
+  OD_OK = 0,
+  OD_ERR_INVALID = 1,      /* bad argument or configuration */
+  OD_ERR_CUDA = 2,         /* CUDA runtime failure (message has the CUDA error) */
+  OD_ERR_OOM = 3,          /* device allocation failed or HBM budget exceeded */
+  OD_ERR_STATE = 4,        /* call not valid in the handle's current state */
+  OD_ERR_TIMEOUT = 5,      /* a bounded device wait ran out */
+  OD_ERR_UNSUPPORTED = 6,  /* feature not compiled in / no suitable GPU */
+  OD_ERR_CAPACITY = 7      /* an output buffer given by the caller is too small */
+} od_status;
+
+/* distributionType (opendust.py:261, :302): "Maxwellian" / "fieldDriven" */
+enum { OD_DIST_MAXWELLIAN = 0, OD_DIST_FIELD_DRIVEN = 1 };
+/* chargeCalculationMethod (opendust.py:1120, :1153): "given" / "consistent" / "oml" */
+enum { OD_CHARGE_GIVEN = 0, OD_CHARGE_CONSISTENT = 1, OD_CHARGE_OML = 2 };
+/* ion–neutral collisions.
+ *  PER_DOF: the reference's field-driven model (opendust.py:869-873): each velocity
+ *           component independently replaced by v_T*gaussian with probability d_t*w_c.
+ *  MFP:     charge exchange with a constant mean free path (rate |v|/mfp), sampled by the
+ *           null-collision method; the whole velocity is replaced by a neutral draw. */
+enum { OD_COLL_NONE = 0, OD_COLL_PER_DOF = 1, OD_COLL_MFP = 2 };
+/* ion–ion force: all pairs (NoCutoff, opendust.py:472) or cutoff with the OpenMM
+ * switching polynomial (CutoffNonPeriodic + switching, opendust.py:481-485) */
+enum { OD_FORCE_ALLPAIRS = 0, OD_FORCE_CUTOFF = 1 };
+/* injection tables: index into od_config.tab_* */
+enum { OD_TAB_TOP = 0, OD_TAB_BOTTOM = 1, OD_TAB_SIDE = 2, OD_TAB_VZ = 3, OD_NTAB = 4 };
+
+/* Philox stream ids (counter word 2) and the words each one uses. */
+enum {
+  OD_RNG_COLL_TEST = 1,  /* PER_DOF: w0..w2 = per-axis collision test u <= d_t*w_c */
+  OD_RNG_COLL_GAUSS = 2, /* PER_DOF: gauss(w0,w1) -> (gx,gy), gauss(w2,w3).cos -> gz */
+  OD_RNG_MFP_TEST = 3,   /* MFP: w0 = null-collision screen, w1 = real/null acceptance */
+  OD_RNG_MFP_GAUSS = 4,  /* MFP: new velocity v_T*(gx,gy,gz) as for COLL_GAUSS */
+  OD_RNG_FACE = 5,       /* w0: face choice (opendust.py:923-926) */
+  OD_RNG_TOP_V = 6,      /* gauss(w0,w1) -> (gx,gy), w2 -> u for the top inverse CDF */
+  OD_RNG_TOP_X = 7,      /* w0 -> radius^2 fraction, w1 -> angle fraction */
+  OD_RNG_BOT_V = 8,      /* as TOP_V with the bottom table */
+  OD_RNG_BOT_X = 9,      /* as TOP_X */
+  OD_RNG_SIDE_X = 10,    /* w0 -> angle fraction, w1 -> axial fraction */
+  OD_RNG_SIDE_V = 11,    /* gauss(w0,w1) -> (gy,gz), w2 -> u for side (and v_z) tables */
+  OD_RNG_TRAP = 13       /* trap-fit sample point p: counter (p,0,13,0); w0 radius^2, w1 angle, w2 axial */
+};
+
+#define OD_MAX_GRAINS 16
+#define OD_MAX_TABLE 256
+
+/* Everything one simulation needs; SI units. Mirrors the state that the reference
+ * builds in OpenDust.__init__ (opendust.py:255-360) and simulate() setup
+ * (opendust.py:370-1044). Array pointers are read during od_create only. */
+typedef struct od_config {
+  int32_t abi_version;      /* must be OD_ABI_VERSION */
+  int32_t distribution;     /* OD_DIST_* */
+  int32_t collision_model;  /* OD_COLL_* */
+  int32_t force_method;     /* OD_FORCE_* */
+  int64_t n_ions;           /* N superions (opendust.py:280) */
+  int64_t n_steps;          /* n: length of the per-step result series (opendust.py:282) */
+  int64_t avg_start;        /* first step of the steady-state time average */
+  int32_t n_grains;         /* P <= OD_MAX_GRAINS */
+  int32_t sim_id;           /* Philox counter word 3 */
+  uint64_t seed;            /* Philox key */
+
+  /* constants as written in the reference (opendust.py:64-67) */
+  double k_B, e, eps_0, m_e;
+  /* plasma (opendust.py:49-77, :112-143) */
+  double T_e, T_n, n_inf, m_i;
+  double r_D_e;             /* electron Debye length = length unit lambda */
+  double v_T, v_fl;         /* thermal and flow speed [m/s] */
+  double E;                 /* external field along z [V/m] (fieldDriven) */
+  double w_c;               /* ion–neutral collision frequency [1/s] (PER_DOF) */
+  double mfp;               /* mean free path [m] (MFP) */
+  /* simulation (opendust.py:181-200) */
+  double R, H, d_t, r_0, N_s;
+  /* cutoff (opendust.py:481-485): cutoff and switching distance [m]; switch_dist <= 0: none */
+  double cutoff, switch_dist;
+  /* trap polynomial coefficients alpha[0..14] (opendust.py:525-550); alpha[0] unused */
+  double alpha[15];
+  /* face probabilities (opendust.py:806-837) */
+  double p_top, p_side, p_bottom;
+  /* piecewise-linear inverse CDFs (opendust.py:608-787): for node i in 1..n-1 the
+   * reference term is v[i-1] + (u - xi[i-1]) * slope[i] on xi[i-1] <= u <= xi[i].
+   * v and slope in m/s (bottom table already negated, as opendust.py:716-717). */
+  int32_t tab_n[OD_NTAB];
+  const double* tab_v[OD_NTAB];
+  const double* tab_xi[OD_NTAB];
+  const double* tab_slope[OD_NTAB];
+  /* grains (opendust.py:25-40, :314-338) */
+  const double* grain_x;
+  const double* grain_y;
+  const double* grain_z;
+  const double* grain_r;
+  const double* grain_q0;
+  const int32_t* grain_method; /* OD_CHARGE_* */
+} od_config;
+
+typedef struct od_handle od_handle;
+
+/* Library identification. */
+int32_t od_abi_version(void);
+const char* od_version(void);
+/* Number of CUDA devices visible (0 on a host without a GPU); never allocates. */
+int32_t od_device_count(void);
+
+/* Replaces mm.Context(system, integrator, Platform "CUDA", {DeviceIndex, Precision})
+ * and the System/force/integrator build (opendust.py:469-604, :839-1044).
+ * Allocates device state for cfg->n_ions ions and the n_steps result series. */
+od_status od_create(const od_config* cfg, int32_t device, od_handle** out);
+
+/* Replaces Context destruction. Safe on NULL. */
+od_status od_destroy(od_handle* h);
+
+/* Message for the last failure on h (or the last failure without a handle if h is NULL). */
+const char* od_last_error(const od_handle* h);
+
+/* Replaces context.setPositions / setVelocities (opendust.py:1043-1044) and the
+ * restart-file read (opendust.py:452-466). pos [m], vel [m/s], both n x 3 row-major. */
+od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n);
+
+/* Replaces context.getState(...).getPositions/getVelocities (opendust.py:1074-1078, :1102-1105). */
+od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n);
+
+/* Replaces `integrator.step(1)` plus the host tail, nsteps times (opendust.py:1059-1383).
+ * Each step appends one entry to the result series. Fails with OD_ERR_STATE when the
+ * series (cfg->n_steps entries) is full. */
+od_status od_step(od_handle* h, int64_t nsteps);
+
+/* Index of the next step (number of steps taken so far). */
+int64_t od_step_index(const od_handle* h);
+
+/* Replaces the per-step reads of dustParticles[p].q / forceIonsOrbit / forceIonsCollect /
+ * forceDust / forceExternalField (opendust.py:1117-1383). Copies steps [first, first+count)
+ * into row-major host arrays: q [count x P] (C), forces [count x P x 3] (N). Any output
+ * pointer may be NULL. f_field is zero for Maxwellian runs. */
+od_status od_get_series(od_handle* h, int64_t first, int64_t count, double* q,
+                        double* f_orbit, double* f_collect, double* f_dust, double* f_field);
+
+/* FP64 time averages over steps [avg_start, steps taken): out has P x 13 doubles per grain:
+ * q, f_orbit[3], f_collect[3], f_dust[3], f_field[3]. *n_avg receives the number of steps. */
+od_status od_get_averages(od_handle* h, double* out, int64_t* n_avg);
+
+/* Ion–ion force on a given snapshot (the CustomNonbondedForce of opendust.py:471-485 evaluated
+ * alone): pos [m] n x 3 -> force [N] n x 3 on each ion, with the handle's force method.
+ * The positions are rounded to the device representation first; od_snapshot_positions
+ * returns exactly the values the kernel consumed. */
+od_status od_force_snapshot(od_handle* h, const double* pos, int64_t n, double* force);
+
+/* The device representation of a snapshot, as doubles [m] (what od_force_snapshot and
+ * od_collect_flags consume for the same input). */
+od_status od_snapshot_positions(od_handle* h, const double* pos, int64_t n, double* pos_dev);
+
+/* Collection / removal flags of opendust.py:894-910 on a given snapshot: idx_out receives, in
+ * increasing order, every ion index with inside_dust_p or outside_domain set (cap entries max);
+ * *count the number of such ions; grain_counts[P] the number inside each grain (delta_q_p of
+ * opendust.py:911-912). Returns OD_ERR_CAPACITY if count > cap (count is still set). */
+od_status od_collect_flags(od_handle* h, const double* pos, int64_t n, int64_t* idx_out,
+                           int64_t cap, int64_t* count, int64_t* grain_counts);
+
+/* Monte-Carlo background potential of the trap fit (the CuPy loop of opendust.py:499-523):
+ * for an n_r x n_h grid (rows: radius linspace(0,R/lambda,n_r); columns: height
+ * linspace(0,H/(2 lambda),n_h)) writes the mean of exp(-r)/(r+0.001) over n_points
+ * uniform points of the cylinder (lambda units), row-major into pot[n_r*n_h].
+ * Points come from Philox stream OD_RNG_TRAP with the given seed. */
+od_status od_trap_potential(double R_over_lambda, double H_over_lambda, int32_t n_r, int32_t n_h,
+                            int64_t n_points, uint64_t seed, int32_t device, double* pot);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPENDUST_GB300_H */

@@ -1,0 +1,349 @@
+"""ctypes binding of libopendust_gb300.so (the C ABI of include/opendust_gb300.h).
+
+The library is built in-tree by ``opendust_gb300._build.build()``. There is no CPU
+fallback: if the shared library is missing or no CUDA device is visible, the calls
+below raise ``OpenDustError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint64, c_void_p
+
+import numpy as np
+
+OD_ABI_VERSION = 1
+OD_MAX_GRAINS = 16
+OD_MAX_TABLE = 256
+OD_NTAB = 4
+OD_TAB_TOP, OD_TAB_BOTTOM, OD_TAB_SIDE, OD_TAB_VZ = 0, 1, 2, 3
+OD_DIST_MAXWELLIAN, OD_DIST_FIELD_DRIVEN = 0, 1
+OD_CHARGE = {"given": 0, "consistent": 1, "oml": 2}
+OD_COLL_NONE, OD_COLL_PER_DOF, OD_COLL_MFP = 0, 1, 2
+OD_FORCE_ALLPAIRS, OD_FORCE_CUTOFF = 0, 1
+
+STATUS = {
+    0: "OD_OK",
+    1: "OD_ERR_INVALID",
+    2: "OD_ERR_CUDA",
+    3: "OD_ERR_OOM",
+    4: "OD_ERR_STATE",
+    5: "OD_ERR_TIMEOUT",
+    6: "OD_ERR_UNSUPPORTED",
+    7: "OD_ERR_CAPACITY",
+}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libopendust_gb300.so")
+
+_DP = POINTER(c_double)
+
+
+class od_config(ctypes.Structure):
+    """Mirror of ``od_config`` in include/opendust_gb300.h (field order matters)."""
+
+    _fields_ = [
+        ("abi_version", c_int32),
+        ("distribution", c_int32),
+        ("collision_model", c_int32),
+        ("force_method", c_int32),
+        ("n_ions", c_int64),
+        ("n_steps", c_int64),
+        ("avg_start", c_int64),
+        ("n_grains", c_int32),
+        ("sim_id", c_int32),
+        ("seed", c_uint64),
+        ("k_B", c_double),
+        ("e", c_double),
+        ("eps_0", c_double),
+        ("m_e", c_double),
+        ("T_e", c_double),
+        ("T_n", c_double),
+        ("n_inf", c_double),
+        ("m_i", c_double),
+        ("r_D_e", c_double),
+        ("v_T", c_double),
+        ("v_fl", c_double),
+        ("E", c_double),
+        ("w_c", c_double),
+        ("mfp", c_double),
+        ("R", c_double),
+        ("H", c_double),
+        ("d_t", c_double),
+        ("r_0", c_double),
+        ("N_s", c_double),
+        ("cutoff", c_double),
+        ("switch_dist", c_double),
+        ("alpha", c_double * 15),
+        ("p_top", c_double),
+        ("p_side", c_double),
+        ("p_bottom", c_double),
+        ("tab_n", c_int32 * OD_NTAB),
+        ("tab_v", _DP * OD_NTAB),
+        ("tab_xi", _DP * OD_NTAB),
+        ("tab_slope", _DP * OD_NTAB),
+        ("grain_x", _DP),
+        ("grain_y", _DP),
+        ("grain_z", _DP),
+        ("grain_r", _DP),
+        ("grain_q0", _DP),
+        ("grain_method", POINTER(c_int32)),
+    ]
+
+
+class OpenDustError(RuntimeError):
+    """Raised when a C-ABI call returns a non-OK status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OpenDustError(
+            6, f"{p} not found: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+        )
+    lib = ctypes.CDLL(p)
+    H = c_void_p
+    sig = {
+        "od_abi_version": (c_int32, []),
+        "od_version": (c_char_p, []),
+        "od_device_count": (c_int32, []),
+        "od_create": (c_int32, [POINTER(od_config), c_int32, POINTER(H)]),
+        "od_destroy": (c_int32, [H]),
+        "od_last_error": (c_char_p, [H]),
+        "od_set_state": (c_int32, [H, _DP, _DP, c_int64]),
+        "od_get_state": (c_int32, [H, _DP, _DP, c_int64]),
+        "od_step": (c_int32, [H, c_int64]),
+        "od_step_index": (c_int64, [H]),
+        "od_get_series": (c_int32, [H, c_int64, c_int64, _DP, _DP, _DP, _DP, _DP]),
+        "od_get_averages": (c_int32, [H, _DP, POINTER(c_int64)]),
+        "od_force_snapshot": (c_int32, [H, _DP, c_int64, _DP]),
+        "od_snapshot_positions": (c_int32, [H, _DP, c_int64, _DP]),
+        "od_collect_flags": (
+            c_int32,
+            [H, _DP, c_int64, POINTER(c_int64), c_int64, POINTER(c_int64), POINTER(c_int64)],
+        ),
+        "od_trap_potential": (
+            c_int32,
+            [c_double, c_double, c_int32, c_int32, c_int64, c_uint64, c_int32, _DP],
+        ),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if lib.od_abi_version() != OD_ABI_VERSION:
+        raise OpenDustError(1, "library ABI version does not match the Python binding")
+    _lib = lib
+    return lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def check(status: int, handle=None):
+    if status != 0:
+        lib = load()
+        msg = lib.od_last_error(handle)
+        raise OpenDustError(status, msg.decode() if msg else "")
+
+
+def device_count() -> int:
+    return int(load().od_device_count())
+
+
+class ConfigHolder:
+    """An ``od_config`` plus the numpy arrays its pointers refer to (kept alive together)."""
+
+    def __init__(self, cfg: od_config, keep: list):
+        self.cfg = cfg
+        self._keep = keep
+
+    def ptr(self):
+        return ctypes.byref(self.cfg)
+
+
+def make_config(
+    *,
+    distribution: int,
+    collision_model: int,
+    force_method: int,
+    n_ions: int,
+    n_steps: int,
+    avg_start: int,
+    seed: int,
+    sim_id: int,
+    consts: dict,
+    plasma: dict,
+    sim: dict,
+    alpha: np.ndarray,
+    probs: tuple,
+    tables: list,
+    grains: dict,
+) -> ConfigHolder:
+    """Fill an od_config from plain Python/numpy values (SI units)."""
+    c = od_config()
+    c.abi_version = OD_ABI_VERSION
+    c.distribution = distribution
+    c.collision_model = collision_model
+    c.force_method = force_method
+    c.n_ions = int(n_ions)
+    c.n_steps = int(n_steps)
+    c.avg_start = int(avg_start)
+    c.n_grains = len(grains["x"])
+    c.sim_id = int(sim_id)
+    c.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    for k in ("k_B", "e", "eps_0", "m_e"):
+        setattr(c, k, float(consts[k]))
+    for k in ("T_e", "T_n", "n_inf", "m_i", "r_D_e", "v_T", "v_fl", "E", "w_c", "mfp"):
+        setattr(c, k, float(plasma.get(k, 0.0)))
+    for k in ("R", "H", "d_t", "r_0", "N_s", "cutoff", "switch_dist"):
+        setattr(c, k, float(sim.get(k, 0.0)))
+    for i in range(15):
+        c.alpha[i] = float(alpha[i])
+    c.p_top, c.p_side, c.p_bottom = (float(x) for x in probs)
+    keep = []
+    for t in range(OD_NTAB):
+        v, xi, sl = tables[t]
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        xi = np.ascontiguousarray(xi, dtype=np.float64)
+        sl = np.ascontiguousarray(sl, dtype=np.float64)
+        if len(v) > OD_MAX_TABLE:
+            raise ValueError("injection table longer than OD_MAX_TABLE")
+        keep += [v, xi, sl]
+        c.tab_n[t] = len(v)
+        c.tab_v[t] = _dptr(v)
+        c.tab_xi[t] = _dptr(xi)
+        c.tab_slope[t] = _dptr(sl)
+    garr = {}
+    for k in ("x", "y", "z", "r", "q0"):
+        garr[k] = np.ascontiguousarray(grains[k], dtype=np.float64)
+        keep.append(garr[k])
+    gm = np.ascontiguousarray(grains["method"], dtype=np.int32)
+    keep.append(gm)
+    c.grain_x, c.grain_y, c.grain_z = _dptr(garr["x"]), _dptr(garr["y"]), _dptr(garr["z"])
+    c.grain_r, c.grain_q0 = _dptr(garr["r"]), _dptr(garr["q0"])
+    c.grain_method = gm.ctypes.data_as(POINTER(c_int32))
+    return ConfigHolder(c, keep)
+
+
+class Engine:
+    """One simulation resident on one GPU (an ``od_handle``)."""
+
+    def __init__(self, holder: ConfigHolder, device: int = 0):
+        lib = load()
+        self._lib = lib
+        self.holder = holder
+        self.n = int(holder.cfg.n_ions)
+        self.P = int(holder.cfg.n_grains)
+        self.n_steps = int(holder.cfg.n_steps)
+        h = c_void_p()
+        check(lib.od_create(holder.ptr(), int(device), ctypes.byref(h)), None)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.od_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, pos: np.ndarray, vel: np.ndarray):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        check(self._lib.od_set_state(self.h, _dptr(pos), _dptr(vel), pos.shape[0]), self.h)
+
+    def get_state(self):
+        pos = np.empty((self.n, 3))
+        vel = np.empty((self.n, 3))
+        check(self._lib.od_get_state(self.h, _dptr(pos), _dptr(vel), self.n), self.h)
+        return pos, vel
+
+    def step(self, nsteps: int):
+        check(self._lib.od_step(self.h, int(nsteps)), self.h)
+
+    @property
+    def step_index(self) -> int:
+        return int(self._lib.od_step_index(self.h))
+
+    def series(self, first: int = 0, count: int | None = None):
+        if count is None:
+            count = self.step_index - first
+        P = self.P
+        q = np.empty((count, P))
+        fo, fc, fd, ff = (np.empty((count, P, 3)) for _ in range(4))
+        check(
+            self._lib.od_get_series(
+                self.h, first, count, _dptr(q), _dptr(fo), _dptr(fc), _dptr(fd), _dptr(ff)
+            ),
+            self.h,
+        )
+        return {"q": q, "orbit": fo, "collect": fc, "dust": fd, "field": ff}
+
+    def averages(self):
+        out = np.empty((self.P, 13))
+        n = c_int64()
+        check(self._lib.od_get_averages(self.h, _dptr(out), ctypes.byref(n)), self.h)
+        return out, int(n.value)
+
+    def force_snapshot(self, pos: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        f = np.empty_like(pos)
+        check(self._lib.od_force_snapshot(self.h, _dptr(pos), pos.shape[0], _dptr(f)), self.h)
+        return f
+
+    def snapshot_positions(self, pos: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        out = np.empty_like(pos)
+        check(self._lib.od_snapshot_positions(self.h, _dptr(pos), pos.shape[0], _dptr(out)), self.h)
+        return out
+
+    def collect_flags(self, pos: np.ndarray, cap: int | None = None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        cap = pos.shape[0] if cap is None else cap
+        idx = np.empty(max(cap, 1), dtype=np.int64)
+        cnt = c_int64()
+        gc = np.zeros(max(self.P, 1), dtype=np.int64)
+        st = self._lib.od_collect_flags(
+            self.h,
+            _dptr(pos),
+            pos.shape[0],
+            idx.ctypes.data_as(POINTER(c_int64)),
+            cap,
+            ctypes.byref(cnt),
+            gc.ctypes.data_as(POINTER(c_int64)),
+        )
+        check(st, self.h)
+        return idx[: cnt.value].copy(), int(cnt.value), gc[: self.P].copy()
+
+
+def trap_potential(Rh: float, Hh: float, n_r: int, n_h: int, n_points: int, seed: int, device: int = 0):
+    pot = np.empty(n_r * n_h)
+    check(
+        load().od_trap_potential(
+            float(Rh), float(Hh), int(n_r), int(n_h), int(n_points), int(seed), int(device), _dptr(pot)
+        ),
+        None,
+    )
+    return pot.reshape(n_r, n_h)

@@ -1,0 +1,535 @@
+// od_api.cu — the C ABI declared in include/opendust_gb300.h (host side).
+//
+// A handle owns one simulation's device state and one CUDA stream. Host arrays belong to
+// the caller; every device buffer belongs to the handle. No C++ exception crosses the ABI.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include <string>
+#include <vector>
+#include "od_internal.h"
+
+#define OD_VERSION_STRING "opendust-gb300 0.1.0 (sm_103a)"
+
+struct od_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  od_config cfg{};
+  od_dparams hp{};
+  od_dparams* dp = nullptr;
+  od_dstate* ds = nullptr;
+  od_dbufs b{};
+  int N = 0, Npad = 0, P = 0, nb = 0, nrec = 32;
+  int64_t step = 0;
+  bool state_set = false;
+  od_pair_plan plan{};
+  // snapshot scratch (allocated on first use)
+  float4 *snap_pos = nullptr, *snap_hi = nullptr, *snap_lo = nullptr;
+  double* snap_counts = nullptr;
+  std::string err;
+};
+
+static thread_local std::string g_err;
+
+static od_status fail(od_handle* h, od_status st, const std::string& msg) {
+  if (h) h->err = msg; else g_err = msg;
+  return st;
+}
+static od_status cuda_fail(od_handle* h, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return fail(h, e == cudaErrorMemoryAllocation ? OD_ERR_OOM : OD_ERR_CUDA, m);
+}
+#define OD_CK(h, call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+extern "C" int32_t od_abi_version(void) { return OD_ABI_VERSION; }
+extern "C" const char* od_version(void) { return OD_VERSION_STRING; }
+extern "C" int32_t od_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+  return n;
+}
+extern "C" const char* od_last_error(const od_handle* h) {
+  return h ? h->err.c_str() : g_err.c_str();
+}
+
+// smallest float not below d
+static float float_ceil(double d) {
+  float f = (float)d;
+  if ((double)f < d) f = nextafterf(f, INFINITY);
+  return f;
+}
+static void split2(double d, float& hi, float& lo) {
+  hi = (float)d;
+  lo = (float)(d - (double)hi);
+}
+
+static od_status validate(const od_config* c) {
+  if (!c) return fail(nullptr, OD_ERR_INVALID, "config is NULL");
+  if (c->abi_version != OD_ABI_VERSION)
+    return fail(nullptr, OD_ERR_INVALID, "config abi_version mismatch");
+  if (c->n_ions < 2 || c->n_ions > (int64_t)1 << 30)
+    return fail(nullptr, OD_ERR_INVALID, "n_ions must be in [2, 2^30]");
+  if (c->n_grains < 0 || c->n_grains > OD_MAX_GRAINS)
+    return fail(nullptr, OD_ERR_INVALID, "n_grains must be in [0, 16]");
+  if (c->n_steps < 1) return fail(nullptr, OD_ERR_INVALID, "n_steps must be >= 1");
+  if (c->distribution != OD_DIST_MAXWELLIAN && c->distribution != OD_DIST_FIELD_DRIVEN)
+    return fail(nullptr, OD_ERR_INVALID, "distribution must be Maxwellian or fieldDriven");
+  if (c->collision_model < OD_COLL_NONE || c->collision_model > OD_COLL_MFP)
+    return fail(nullptr, OD_ERR_INVALID, "unknown collision model");
+  if (c->collision_model == OD_COLL_MFP && !(c->mfp > 0))
+    return fail(nullptr, OD_ERR_INVALID, "MFP collisions need mfp > 0");
+  if (c->force_method != OD_FORCE_ALLPAIRS && c->force_method != OD_FORCE_CUTOFF)
+    return fail(nullptr, OD_ERR_INVALID, "unknown force method");
+  if (c->force_method == OD_FORCE_CUTOFF && !(c->cutoff > 0))
+    return fail(nullptr, OD_ERR_INVALID, "cutoff method needs cutoff > 0");
+  if (!(c->r_D_e > 0) || !(c->d_t > 0) || !(c->R > 0) || !(c->H > 0) || !(c->N_s > 0))
+    return fail(nullptr, OD_ERR_INVALID, "r_D_e, d_t, R, H and N_s must be positive");
+  for (int t = 0; t < OD_NTAB; t++) {
+    if (c->tab_n[t] < 0 || c->tab_n[t] > OD_MAX_TABLE)
+      return fail(nullptr, OD_ERR_INVALID, "injection table longer than OD_MAX_TABLE");
+    if (c->tab_n[t] > 0 && (!c->tab_v[t] || !c->tab_xi[t] || !c->tab_slope[t]))
+      return fail(nullptr, OD_ERR_INVALID, "injection table pointer is NULL");
+  }
+  if (c->tab_n[OD_TAB_TOP] < 2 && c->p_top > 0)
+    return fail(nullptr, OD_ERR_INVALID, "top table needs at least 2 nodes");
+  if (c->tab_n[OD_TAB_SIDE] < 2 && c->p_side > 0)
+    return fail(nullptr, OD_ERR_INVALID, "side table needs at least 2 nodes");
+  if (c->distribution == OD_DIST_FIELD_DRIVEN && c->tab_n[OD_TAB_VZ] < 2)
+    return fail(nullptr, OD_ERR_INVALID, "fieldDriven needs the side v_z table");
+  if (c->n_grains > 0 &&
+      (!c->grain_x || !c->grain_y || !c->grain_z || !c->grain_r || !c->grain_q0 || !c->grain_method))
+    return fail(nullptr, OD_ERR_INVALID, "grain array pointer is NULL");
+  for (int g = 0; g < c->n_grains; g++)
+    if (c->grain_method[g] < OD_CHARGE_GIVEN || c->grain_method[g] > OD_CHARGE_OML)
+      return fail(nullptr, OD_ERR_INVALID, "unknown charge method");
+  return OD_OK;
+}
+
+static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
+  memset(p, 0, sizeof(*p));
+  const double pi = OD_PI_D;
+  p->N = N; p->Npad = Npad; p->P = c->n_grains; p->dist = c->distribution;
+  p->coll = c->collision_model; p->method = c->force_method; p->sim = c->sim_id;
+  p->nwords = Npad / 32;
+  p->seed_lo = (uint32_t)(c->seed & 0xffffffffu);
+  p->seed_hi = (uint32_t)(c->seed >> 32);
+  const double lam = c->r_D_e, dt = c->d_t;
+  const double k = 1.0 / (c->eps_0 * 4.0 * pi);
+  const double q_s = fabs(c->e) * c->N_s;
+  const double m_s = c->m_i * c->N_s;
+  const double sc = dt * dt / (m_s * lam * lam * lam);
+  const double A_ii = k * q_s * q_s * sc;
+  p->A_ii = (float)A_ii;
+  p->A_id_d = k * q_s * sc;
+  p->A_id = (float)p->A_id_d;
+  p->rho0 = (float)(c->r_0 / lam);
+  const double Rh = c->R / lam, Hh = c->H / lam;
+  p->Rh = (float)Rh; p->Hh = (float)Hh; p->Hh_half = (float)(Hh / 2.0);
+  p->a_field = c->distribution == OD_DIST_FIELD_DRIVEN ? (float)(c->E * q_s * dt * dt / (m_s * lam)) : 0.f;
+  const double vunit = lam / dt;
+  p->vT = (float)(c->v_T / vunit);
+  p->vfl = (float)(c->v_fl / vunit);
+  if (c->force_method == OD_FORCE_CUTOFF) {
+    double rc = c->cutoff / lam, rs = c->switch_dist > 0 ? c->switch_dist / lam : rc;
+    p->rc = (float)rc; p->rc2 = (float)(rc * rc); p->rs = (float)rs;
+    p->inv_w = rc > rs ? (float)(1.0 / (rc - rs)) : 0.f;
+  }
+  for (int i = 0; i < 15; i++) {
+    p->trapc[i] = (float)(-2.0 * A_ii * c->alpha[i]);
+    p->alpha[i] = c->alpha[i];
+  }
+  for (int g = 0; g < c->n_grains; g++) {
+    double gx = c->grain_x[g] / lam, gy = c->grain_y[g] / lam, gz = c->grain_z[g] / lam;
+    double r = c->grain_r[g] / lam;
+    p->gx[g] = gx; p->gy[g] = gy; p->gz[g] = gz; p->gr2[g] = r * r;
+    split2(gx, p->gxh[g], p->gxl[g]);
+    split2(gy, p->gyh[g], p->gyl[g]);
+    split2(gz, p->gzh[g], p->gzl[g]);
+    p->gr2f[g] = (float)(r * r);
+    p->gxs[g] = c->grain_x[g]; p->gys[g] = c->grain_y[g]; p->gzs[g] = c->grain_z[g];
+    p->grs[g] = c->grain_r[g];
+    p->gmethod[g] = c->grain_method[g];
+  }
+  p->Rh2 = Rh * Rh;
+  p->Hh_half_d = Hh / 2.0;
+  p->Rh2f = (float)(Rh * Rh);
+  p->Hz_f = float_ceil(Hh / 2.0);
+  p->p_coll = dt * c->w_c;
+  if (c->collision_model == OD_COLL_MFP) {
+    double mfp_h = c->mfp / lam;
+    double vmax = 3.0 * fabs(c->v_fl / vunit) + 10.0 * (c->v_T / vunit);
+    p->mfp_inv = (float)(1.0 / mfp_h);
+    p->vmax_mfp = (float)vmax;
+    p->Pmax_mfp = 1.0 - exp(-vmax / mfp_h);
+  }
+  p->p_t = c->p_top; p->p_s = c->p_side; p->p_b = c->p_bottom;
+  for (int t = 0; t < OD_NTAB; t++) {
+    p->tn[t] = c->tab_n[t];
+    for (int i = 0; i < c->tab_n[t]; i++) {
+      p->tv[t][i] = (float)(c->tab_v[t][i] / vunit);
+      p->txi[t][i] = c->tab_xi[t][i];
+      p->tsl[t][i] = (float)(c->tab_slope[t][i] / vunit);
+    }
+  }
+  p->k = k; p->q_s = q_s; p->m_s = m_s; p->lam = lam; p->dt = dt; p->vunit = vunit;
+  p->n_inf = c->n_inf; p->T_e = c->T_e; p->T_n = c->T_n; p->k_B = c->k_B; p->m_e = c->m_e;
+  p->e = c->e; p->E = c->E; p->v_T_si = c->v_T; p->v_fl_si = c->v_fl;
+  p->n_steps = c->n_steps; p->avg_start = c->avg_start;
+}
+
+// Heuristic work split of the all-pairs kernel: enough blocks for several waves on every SM.
+static od_pair_plan default_plan(int Npad, int sms) {
+  od_pair_plan pl{};
+  pl.nt = 256; pl.ipt = 1; pl.variant = 0;
+  const int nbx = Npad / (pl.nt * pl.ipt);
+  const int target = std::max(1, sms * 8 * 4);
+  int js = std::max(1, (target + nbx - 1) / nbx);
+  js = std::min(js, Npad / OD_TJ);
+  int chunk = (Npad + js - 1) / js;
+  chunk = ((chunk + OD_TJ - 1) / OD_TJ) * OD_TJ;
+  pl.chunk = chunk;
+  pl.jsplit = (Npad + chunk - 1) / chunk;
+  return pl;
+}
+
+template <typename T>
+static cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
+}
+
+static void free_all(od_handle* h) {
+  void* ptrs[] = {h->dp, h->ds, h->b.pos, h->b.vel, h->b.fhi, h->b.flo, h->b.part_hi, h->b.part_lo,
+                  h->b.flags, h->b.list, h->b.list_bits, h->b.list_old, h->b.list_new, h->b.list_v,
+                  h->b.orbit_part, h->b.s_q, h->b.s_orbit, h->b.s_collect, h->b.s_dust,
+                  h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+static od_status alloc_scratch_for_plan(od_handle* h) {
+  if (h->b.part_hi) { cudaFree(h->b.part_hi); h->b.part_hi = nullptr; }
+  if (h->b.part_lo) { cudaFree(h->b.part_lo); h->b.part_lo = nullptr; }
+  size_t n = (size_t)h->plan.jsplit * h->Npad;
+  OD_CK(h, dalloc(&h->b.part_hi, n));
+  OD_CK(h, dalloc(&h->b.part_lo, n));
+  return OD_OK;
+}
+
+extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle** out) {
+  if (!out) return fail(nullptr, OD_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  od_status st = validate(cfg);
+  if (st != OD_OK) return st;
+  if (od_device_count() <= device || device < 0)
+    return fail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  od_handle* h = new (std::nothrow) od_handle();
+  if (!h) return fail(nullptr, OD_ERR_OOM, "host allocation failed");
+  h->device = device;
+  h->cfg = *cfg;
+  h->N = (int)cfg->n_ions;
+  h->Npad = (int)(((cfg->n_ions + OD_PAD - 1) / OD_PAD) * OD_PAD);
+  h->P = cfg->n_grains;
+  h->nb = h->Npad / 256;
+  auto bail = [&](od_status s) {
+    g_err = h->err;
+    free_all(h);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return s;
+  };
+#define OD_CKC(call)                                           \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return bail(cuda_fail(h, e_, #call)); \
+  } while (0)
+  OD_CKC(cudaSetDevice(device));
+  OD_CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  fill_params(cfg, h->N, h->Npad, &h->hp);
+  h->plan = default_plan(h->Npad, od_num_sms(device));
+  const size_t Np = h->Npad, P = std::max(h->P, 1), ns = cfg->n_steps;
+  OD_CKC(dalloc(&h->dp, 1));
+  OD_CKC(dalloc(&h->ds, 1));
+  OD_CKC(dalloc(&h->b.pos, Np));
+  OD_CKC(dalloc(&h->b.vel, Np));
+  OD_CKC(dalloc(&h->b.fhi, Np));
+  OD_CKC(dalloc(&h->b.flo, Np));
+  OD_CKC(dalloc(&h->b.flags, Np / 32));
+  OD_CKC(dalloc(&h->b.list, Np));
+  OD_CKC(dalloc(&h->b.list_bits, Np));
+  OD_CKC(dalloc(&h->b.list_old, Np));
+  OD_CKC(dalloc(&h->b.list_new, Np));
+  OD_CKC(dalloc(&h->b.list_v, Np));
+  OD_CKC(dalloc(&h->b.orbit_part, (size_t)h->nb * P * 3));
+  OD_CKC(dalloc(&h->b.s_q, ns * P));
+  OD_CKC(dalloc(&h->b.s_orbit, ns * P * 3));
+  OD_CKC(dalloc(&h->b.s_collect, ns * P * 3));
+  OD_CKC(dalloc(&h->b.s_dust, ns * P * 3));
+  OD_CKC(dalloc(&h->b.s_field, ns * P * 3));
+  OD_CKC(dalloc(&h->b.cq, OD_MAX_GRAINS));
+  if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
+  OD_CKC(cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
+  od_dstate s0{};
+  for (int g = 0; g < h->P; g++) s0.q_param[g] = cfg->grain_q0[g];
+  OD_CKC(cudaMemcpyAsync(h->ds, &s0, sizeof(s0), cudaMemcpyHostToDevice, h->stream));
+  // padded slots: far-away sources, zero velocity
+  std::vector<float4> pad(Np, make_float4(OD_SENTINEL, OD_SENTINEL, OD_SENTINEL, 0.f));
+  OD_CKC(cudaMemcpy(h->b.pos, pad.data(), sizeof(float4) * Np, cudaMemcpyHostToDevice));
+  OD_CKC(cudaMemset(h->b.vel, 0, sizeof(float4) * Np));
+  OD_CKC(cudaMemset(h->b.fhi, 0, sizeof(float4) * Np));
+  OD_CKC(cudaMemset(h->b.flo, 0, sizeof(float4) * Np));
+  OD_CKC(cudaMemset(h->b.s_q, 0, sizeof(double) * ns * P));
+  OD_CKC(cudaMemset(h->b.s_field, 0, sizeof(double) * ns * P * 3));
+  OD_CKC(od_launch_set_charges(h->dp, h->ds, h->b.cq, h->P, h->stream));
+  OD_CKC(cudaStreamSynchronize(h->stream));
+#undef OD_CKC
+  *out = h;
+  return OD_OK;
+}
+
+extern "C" od_status od_destroy(od_handle* h) {
+  if (!h) return OD_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return OD_OK;
+}
+
+static void to_device_units(const od_handle* h, const double* pos, const double* vel, int64_t n,
+                            std::vector<float4>& xp, std::vector<float4>* vp) {
+  const double lam = h->hp.lam, vunit = h->hp.vunit;
+  xp.resize(n);
+  for (int64_t i = 0; i < n; i++)
+    xp[i] = make_float4((float)(pos[3 * i] / lam), (float)(pos[3 * i + 1] / lam),
+                        (float)(pos[3 * i + 2] / lam), 0.f);
+  if (vp) {
+    vp->resize(n);
+    for (int64_t i = 0; i < n; i++)
+      (*vp)[i] = make_float4((float)(vel[3 * i] / vunit), (float)(vel[3 * i + 1] / vunit),
+                             (float)(vel[3 * i + 2] / vunit), 0.f);
+  }
+}
+
+static od_status check_device_err(od_handle* h) {
+  od_dstate s;
+  OD_CK(h, cudaMemcpyAsync(&s, h->ds, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  if (s.err & OD_DERR_TIMEOUT) return fail(h, OD_ERR_TIMEOUT, "a bounded device wait ran out");
+  if (s.err) return fail(h, OD_ERR_STATE, "device error word set");
+  return OD_OK;
+}
+
+// ion–ion sums of the current positions into fhi/flo (the force the first half kick uses)
+static od_status refresh_forces(od_handle* h) {
+  const float rho0 = h->hp.rho0;
+  OD_CK(h, od_launch_pairs(h->plan, h->b.pos, h->Npad, h->b.part_hi, h->b.part_lo, rho0,
+                           &h->ds->err, h->stream));
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->b.fhi,
+                            h->b.flo, h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!pos || !vel) return fail(h, OD_ERR_INVALID, "pos/vel is NULL");
+  if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
+  if (h->cfg.force_method != OD_FORCE_ALLPAIRS)
+    return fail(h, OD_ERR_UNSUPPORTED, "cutoff force method is not built into this library yet");
+  OD_CK(h, cudaSetDevice(h->device));
+  std::vector<float4> xp, vp;
+  to_device_units(h, pos, vel, n, xp, &vp);
+  OD_CK(h, cudaMemcpyAsync(h->b.pos, xp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, cudaMemcpyAsync(h->b.vel, vp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
+  od_status st = refresh_forces(h);
+  if (st != OD_OK) return st;
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->state_set = true;
+  return check_device_err(h);
+}
+
+extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
+  OD_CK(h, cudaSetDevice(h->device));
+  std::vector<float4> xp(n), vp(n);
+  OD_CK(h, cudaMemcpyAsync(xp.data(), h->b.pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaMemcpyAsync(vp.data(), h->b.vel, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  const double lam = h->hp.lam, vunit = h->hp.vunit;
+  for (int64_t i = 0; i < n; i++) {
+    if (pos) { pos[3 * i] = xp[i].x * lam; pos[3 * i + 1] = xp[i].y * lam; pos[3 * i + 2] = xp[i].z * lam; }
+    if (vel) { vel[3 * i] = vp[i].x * vunit; vel[3 * i + 1] = vp[i].y * vunit; vel[3 * i + 2] = vp[i].z * vunit; }
+  }
+  return OD_OK;
+}
+
+extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!h->state_set) return fail(h, OD_ERR_STATE, "od_set_state has not been called");
+  if (nsteps < 0) return fail(h, OD_ERR_INVALID, "nsteps < 0");
+  if (h->step + nsteps > h->cfg.n_steps)
+    return fail(h, OD_ERR_STATE, "the result series is full (n_steps reached)");
+  OD_CK(h, cudaSetDevice(h->device));
+  for (int64_t s = 0; s < nsteps; s++) {
+    OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0, h->nrec,
+                            h->stream));
+  }
+  h->step += nsteps;
+  return check_device_err(h);
+}
+
+extern "C" int64_t od_step_index(const od_handle* h) { return h ? h->step : -1; }
+
+extern "C" od_status od_get_series(od_handle* h, int64_t first, int64_t count, double* q,
+                                   double* f_orbit, double* f_collect, double* f_dust,
+                                   double* f_field) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (first < 0 || count < 0 || first + count > h->step)
+    return fail(h, OD_ERR_INVALID, "requested steps have not been taken");
+  if (count == 0) return OD_OK;
+  OD_CK(h, cudaSetDevice(h->device));
+  const size_t P = h->P;
+  const size_t o1 = first * P, n1 = count * P;
+  if (q) OD_CK(h, cudaMemcpyAsync(q, h->b.s_q + o1, n1 * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (f_orbit) OD_CK(h, cudaMemcpyAsync(f_orbit, h->b.s_orbit + 3 * o1, 3 * n1 * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (f_collect) OD_CK(h, cudaMemcpyAsync(f_collect, h->b.s_collect + 3 * o1, 3 * n1 * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (f_dust) OD_CK(h, cudaMemcpyAsync(f_dust, h->b.s_dust + 3 * o1, 3 * n1 * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (f_field) OD_CK(h, cudaMemcpyAsync(f_field, h->b.s_field + 3 * o1, 3 * n1 * 8, cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_get_averages(od_handle* h, double* out, int64_t* n_avg) {
+  if (!h || !out) return fail(h, OD_ERR_INVALID, "NULL argument");
+  OD_CK(h, cudaSetDevice(h->device));
+  od_dstate s;
+  OD_CK(h, cudaMemcpyAsync(&s, h->ds, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  const double n = s.n_avg > 0 ? (double)s.n_avg : 1.0;
+  for (int g = 0; g < h->P; g++)
+    for (int m = 0; m < 13; m++) out[g * 13 + m] = s.avg[g][m] / n;
+  if (n_avg) *n_avg = s.n_avg;
+  return OD_OK;
+}
+
+static od_status ensure_snapshot(od_handle* h) {
+  if (h->snap_pos) return OD_OK;
+  OD_CK(h, dalloc(&h->snap_pos, h->Npad));
+  OD_CK(h, dalloc(&h->snap_hi, h->Npad));
+  OD_CK(h, dalloc(&h->snap_lo, h->Npad));
+  OD_CK(h, dalloc(&h->snap_counts, OD_MAX_GRAINS + 1));
+  return OD_OK;
+}
+
+static od_status upload_snapshot(od_handle* h, const double* pos, int64_t n) {
+  od_status st = ensure_snapshot(h);
+  if (st != OD_OK) return st;
+  std::vector<float4> xp;
+  to_device_units(h, pos, nullptr, n, xp, nullptr);
+  xp.resize(h->Npad, make_float4(OD_SENTINEL, OD_SENTINEL, OD_SENTINEL, 0.f));
+  OD_CK(h, cudaMemcpyAsync(h->snap_pos, xp.data(), sizeof(float4) * h->Npad, cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_force_snapshot(od_handle* h, const double* pos, int64_t n, double* force) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!pos || !force) return fail(h, OD_ERR_INVALID, "NULL argument");
+  if (n < 1 || n > h->N) return fail(h, OD_ERR_INVALID, "n must be in [1, n_ions]");
+  if (h->cfg.force_method != OD_FORCE_ALLPAIRS)
+    return fail(h, OD_ERR_UNSUPPORTED, "cutoff force method is not built into this library yet");
+  OD_CK(h, cudaSetDevice(h->device));
+  od_status st = upload_snapshot(h, pos, n);
+  if (st != OD_OK) return st;
+  OD_CK(h, od_launch_pairs(h->plan, h->snap_pos, h->Npad, h->b.part_hi, h->b.part_lo, h->hp.rho0,
+                           &h->ds->err, h->stream));
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->snap_hi,
+                            h->snap_lo, h->stream));
+  std::vector<float4> hi(n), lo(n);
+  OD_CK(h, cudaMemcpyAsync(hi.data(), h->snap_hi, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaMemcpyAsync(lo.data(), h->snap_lo, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  st = check_device_err(h);
+  if (st != OD_OK) return st;
+  const double F = h->hp.k * h->hp.q_s * h->hp.q_s / (h->hp.lam * h->hp.lam);
+  for (int64_t i = 0; i < n; i++) {
+    force[3 * i] = F * ((double)hi[i].x + (double)lo[i].x);
+    force[3 * i + 1] = F * ((double)hi[i].y + (double)lo[i].y);
+    force[3 * i + 2] = F * ((double)hi[i].z + (double)lo[i].z);
+  }
+  return OD_OK;
+}
+
+extern "C" od_status od_snapshot_positions(od_handle* h, const double* pos, int64_t n, double* pos_dev) {
+  if (!h || !pos || !pos_dev) return fail(h, OD_ERR_INVALID, "NULL argument");
+  std::vector<float4> xp;
+  to_device_units(h, pos, nullptr, n, xp, nullptr);
+  for (int64_t i = 0; i < n; i++) {
+    pos_dev[3 * i] = (double)xp[i].x * h->hp.lam;
+    pos_dev[3 * i + 1] = (double)xp[i].y * h->hp.lam;
+    pos_dev[3 * i + 2] = (double)xp[i].z * h->hp.lam;
+  }
+  return OD_OK;
+}
+
+extern "C" od_status od_collect_flags(od_handle* h, const double* pos, int64_t n, int64_t* idx_out,
+                                      int64_t cap, int64_t* count, int64_t* grain_counts) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!pos || !count || (cap > 0 && !idx_out)) return fail(h, OD_ERR_INVALID, "NULL argument");
+  if (n < 1 || n > h->N) return fail(h, OD_ERR_INVALID, "n must be in [1, n_ions]");
+  OD_CK(h, cudaSetDevice(h->device));
+  od_status st = upload_snapshot(h, pos, n);
+  if (st != OD_OK) return st;
+  OD_CK(h, od_launch_snapshot_flags(h->dp, (int)n, h->Npad, h->snap_pos, h->b.flags, h->b.list,
+                                    h->b.list_bits, h->snap_counts, h->stream));
+  double counts[OD_MAX_GRAINS + 1];
+  OD_CK(h, cudaMemcpyAsync(counts, h->snap_counts, sizeof(counts), cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  const int64_t K = (int64_t)counts[OD_MAX_GRAINS];
+  *count = K;
+  if (grain_counts)
+    for (int g = 0; g < h->P; g++) grain_counts[g] = (int64_t)counts[g];
+  const int64_t m = std::min(K, cap);
+  if (m > 0) {
+    std::vector<int32_t> li(m);
+    OD_CK(h, cudaMemcpyAsync(li.data(), h->b.list, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, h->stream));
+    OD_CK(h, cudaStreamSynchronize(h->stream));
+    for (int64_t k = 0; k < m; k++) idx_out[k] = li[k];
+  }
+  if (K > cap) return fail(h, OD_ERR_CAPACITY, "idx_out too small");
+  return OD_OK;
+}
+
+extern "C" od_status od_trap_potential(double Rh, double Hh, int32_t n_r, int32_t n_h,
+                                       int64_t n_points, uint64_t seed, int32_t device, double* pot) {
+  if (!pot || n_r < 2 || n_h < 2 || n_points < 1 || !(Rh > 0) || !(Hh > 0))
+    return fail(nullptr, OD_ERR_INVALID, "bad trap-fit arguments");
+  if (od_device_count() <= device || device < 0)
+    return fail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  const int nn = n_r * n_h;
+  const int nchunks = std::max(1, (int)std::min<int64_t>(od_num_sms(device) * 4, (n_points + 4095) / 4096));
+  double* part = nullptr;
+  e = cudaMalloc(&part, sizeof(double) * nn * nchunks);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  e = od_launch_trap(Rh, Hh, n_r, n_h, n_points, seed, part, nchunks, 0);
+  std::vector<double> hpart((size_t)nn * nchunks);
+  if (e == cudaSuccess) e = cudaMemcpy(hpart.data(), part, sizeof(double) * nn * nchunks, cudaMemcpyDeviceToHost);
+  cudaFree(part);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "trap potential");
+  for (int i = 0; i < nn; i++) {
+    double s = 0;
+    for (int c = 0; c < nchunks; c++) s += hpart[(size_t)c * nn + i];
+    pot[i] = s / (double)n_points;
+  }
+  return OD_OK;
+}

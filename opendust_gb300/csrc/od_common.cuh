@@ -1,0 +1,256 @@
+// od_common.cuh — device-side definitions shared by the superion step kernels.
+//
+// Units on the device: length lambda = r_D_e, time d_t, so a leapfrog half kick is
+// v += 0.5*a and a drift is x += v. Ion state is FP32 (float4 SoA: pos, vel);
+// grain charges, sums, series and averages are FP64.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/opendust_gb300.h"
+
+#define OD_PI_D 3.14159265358979323846
+#define OD_TJ 256              // source positions per shared-memory tile
+#define OD_PAD 512             // ion arrays are padded to a multiple of this
+#define OD_SENTINEL 1.0e4f     // padded sources sit here: exp(-r) underflows to 0
+#define OD_WAIT_LIMIT (1u << 26)
+
+// Device error word bits (reported by the host as OD_ERR_TIMEOUT / OD_ERR_STATE)
+#define OD_DERR_TIMEOUT 1u
+#define OD_DERR_LIST 2u
+
+// Per-simulation constants, resident in device memory.
+struct od_dparams {
+  int32_t N, Npad, P, dist, coll, method, sim, nwords;
+  uint32_t seed_lo, seed_hi;
+  // FP32 hot-loop constants (lambda / d_t units)
+  float A_ii, rho0, Rh, Hh, Hh_half, a_field, vT, vfl;
+  float rc2, rc, rs, inv_w;          // cutoff^2, cutoff, switch start, 1/(rc-rs)
+  float trapc[15];                   // -2*A_ii*alpha[k]
+  float A_id;                        // ion–dust prefactor, times q_p
+  double A_id_d;                     // same in FP64
+  float gxh[OD_MAX_GRAINS], gxl[OD_MAX_GRAINS];  // grain centres as two-float
+  float gyh[OD_MAX_GRAINS], gyl[OD_MAX_GRAINS];
+  float gzh[OD_MAX_GRAINS], gzl[OD_MAX_GRAINS];
+  float gr2f[OD_MAX_GRAINS];
+  float Rh2f, Hz_f;
+  float mfp_inv, vmax_mfp;
+  // FP64 exact-flag constants (identical doubles in the CPU oracle)
+  double gx[OD_MAX_GRAINS], gy[OD_MAX_GRAINS], gz[OD_MAX_GRAINS], gr2[OD_MAX_GRAINS];
+  double Rh2, Hh_half_d;
+  double p_coll, Pmax_mfp, p_t, p_s, p_b;
+  // injection tables (lambda/d_t units for v and slope)
+  int32_t tn[OD_NTAB];
+  float tv[OD_NTAB][OD_MAX_TABLE];
+  double txi[OD_NTAB][OD_MAX_TABLE];
+  float tsl[OD_NTAB][OD_MAX_TABLE];
+  // FP64 tail constants (SI)
+  double k, q_s, m_s, lam, dt, vunit, n_inf, T_e, T_n, k_B, m_e, e, E, v_T_si, v_fl_si;
+  double alpha[15];
+  double gxs[OD_MAX_GRAINS], gys[OD_MAX_GRAINS], gzs[OD_MAX_GRAINS], grs[OD_MAX_GRAINS];
+  int32_t gmethod[OD_MAX_GRAINS];
+  int64_t n_steps, avg_start;
+};
+
+// Per-simulation FP64 accumulators and bookkeeping, resident in device memory.
+struct od_dstate {
+  int64_t step;                       // next step index
+  uint32_t err;                       // OD_DERR_* bits
+  int32_t nlist;                      // flagged ions this step
+  double q_param[OD_MAX_GRAINS];      // charges the ion forces use (q at the previous step)
+  double dN[OD_MAX_GRAINS];           // ions collected this step
+  double M[OD_MAX_GRAINS][3];         // sum of collected velocities (lambda/d_t)
+  double avg[OD_MAX_GRAINS][13];      // running sums over the averaging window
+  int64_t n_avg;
+  int64_t n_inj_total;
+};
+
+// ------------------------------------------------------------------ Philox4x32-10
+struct od_u4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ od_u4 od_philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                           uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  return od_u4{c0, c1, c2, c3};
+}
+__device__ __forceinline__ od_u4 od_draw(const od_dparams& p, uint32_t ion, uint32_t step,
+                                         uint32_t stream) {
+  return od_philox(ion, step, stream, (uint32_t)p.sim, p.seed_lo, p.seed_hi);
+}
+__device__ __forceinline__ float od_u01(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+__device__ __forceinline__ float od_u01c(uint32_t w) {
+  return (float)((w >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+__device__ __forceinline__ void od_gauss2(uint32_t a, uint32_t b, float& g0, float& g1) {
+  float r = sqrtf(-2.0f * logf(od_u01c(a)));
+  float s, c;
+  sincospif(2.0f * od_u01(b), &s, &c);
+  g0 = r * c;
+  g1 = r * s;
+}
+
+// ------------------------------------------------------------------ SFU approximations
+__device__ __forceinline__ float od_rsqrt(float x) {
+  float r; asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r;
+}
+__device__ __forceinline__ float od_rcp(float x) {
+  float r; asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r;
+}
+__device__ __forceinline__ float od_ex2(float x) {
+  float r; asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x)); return r;
+}
+#define OD_NLOG2E (-1.4426950408889634f)
+
+// ------------------------------------------------------------------ two-float sums
+// Knuth TwoSum: hi + lo == a + b exactly.
+__device__ __forceinline__ void od_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// accumulate x into (hi, lo)
+__device__ __forceinline__ void od_acc2(float& hi, float& lo, float x) {
+  float s, e;
+  od_two_sum(hi, x, s, e);
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
+// ------------------------------------------------------------------ pair kernel
+// Radial factor c(r) of the Yukawa pair force: the acceleration on i from j is
+// A_ii * c * (x_i - x_j), c = exp(-r) (1/s + 1/s^2) / r, s = r + rho0 (opendust.py:472).
+// r2 carries +1e-30 so that the self pair (dx = 0) contributes exactly zero.
+__device__ __forceinline__ float od_pair_c(float r2, float rho0) {
+  float ri = od_rsqrt(r2);
+  float r = r2 * ri;
+  float si = od_rcp(r + rho0);
+  float ex = od_ex2(r * OD_NLOG2E);
+  float t = fmaf(si, si, si);
+  return (ex * ri) * t;
+}
+// Same with OpenMM's switching polynomial on the energy and a hard cutoff (opendust.py:481-485).
+__device__ __forceinline__ float od_pair_c_cut(float r2, const od_dparams& p) {
+  float ri = od_rsqrt(r2);
+  float r = r2 * ri;
+  float si = od_rcp(r + p.rho0);
+  float ex = od_ex2(r * OD_NLOG2E);
+  float f = ex * fmaf(si, si, si);
+  float x = fmaxf((r - p.rs) * p.inv_w, 0.0f);
+  // S = 1 - x^3 (10 - 15x + 6x^2), S' = -x^2 (30 - 60x + 30x^2) / (rc - rs)
+  float S = 1.0f - x * x * x * (10.0f - x * (15.0f - 6.0f * x));
+  float dS = -x * x * (30.0f - x * (60.0f - 30.0f * x)) * p.inv_w;
+  float c = (f * S - ex * si * dS) * ri;
+  return r2 < p.rc2 ? c : 0.0f;
+}
+
+// ------------------------------------------------------------------ external forces
+// grains (opendust.py:350-352), trap (opendust.py:552-577), field (opendust.py:580-585)
+__device__ __forceinline__ float3 od_ext_accel(const od_dparams& p, const float* cq, float x,
+                                               float y, float z) {
+  float ax = 0.f, ay = 0.f, az = p.a_field;
+  for (int g = 0; g < p.P; g++) {
+    float dx = (x - p.gxh[g]) - p.gxl[g];
+    float dy = (y - p.gyh[g]) - p.gyl[g];
+    float dz = (z - p.gzh[g]) - p.gzl[g];
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float ri = rsqrtf(r2);
+    float c = cq[g] * ri * ri * ri;
+    ax = fmaf(c, dx, ax); ay = fmaf(c, dy, ay); az = fmaf(c, dz, az);
+  }
+  const float* t = p.trapc;
+  float u = fmaf(x, x, y * y), w = z * z;
+  // P_u and P_w of the 14-term even polynomial; t[k] = -2 A_ii alpha_k
+  float Pu = t[1] + w * (t[3] + w * (t[7] + w * t[12])) +
+             u * (2.f * t[4] + w * (2.f * t[6] + w * 2.f * t[10]) +
+                  u * (3.f * t[8] + w * 3.f * t[11] + u * 4.f * t[13]));
+  float Pw = t[2] + u * (t[3] + u * (t[6] + u * t[11])) +
+             w * (2.f * t[5] + u * (2.f * t[7] + u * 2.f * t[10]) +
+                  w * (3.f * t[9] + u * 3.f * t[12] + w * 4.f * t[14]));
+  ax = fmaf(x, Pu, ax);
+  ay = fmaf(y, Pu, ay);
+  az = fmaf(z, Pw, az);
+  return make_float3(ax, ay, az);
+}
+
+// ------------------------------------------------------------------ exact flags
+// opendust.py:894-910 on squared distances, FP64 with explicit rounding (never contracted);
+// the CPU oracle performs the same operations. An FP32 test with a 1e-5 relative margin
+// decides all but the ions within that margin of a surface.
+__device__ __forceinline__ int od_flag_exact(const od_dparams& p, float xf, float yf, float zf) {
+  double x = xf, y = yf, z = zf;
+  int bits = 0;
+  for (int g = 0; g < p.P; g++) {
+    double dx = __dsub_rn(x, p.gx[g]), dy = __dsub_rn(y, p.gy[g]), dz = __dsub_rn(z, p.gz[g]);
+    double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    d2 = __dadd_rn(d2, __dmul_rn(dz, dz));
+    if (d2 <= p.gr2[g]) bits |= 1 << g;
+  }
+  double rr = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+  if (rr >= p.Rh2) bits |= 1 << 30;
+  if (fabs(z) >= p.Hh_half_d) bits |= 1 << 29;
+  return bits;
+}
+__device__ __forceinline__ int od_flag(const od_dparams& p, float x, float y, float z) {
+  bool near = false;
+  int bits = 0;
+  for (int g = 0; g < p.P; g++) {
+    float dx = (x - p.gxh[g]) - p.gxl[g];
+    float dy = (y - p.gyh[g]) - p.gyl[g];
+    float dz = (z - p.gzh[g]) - p.gzl[g];
+    float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (d2 < p.gr2f[g] * 0.99999f) bits |= 1 << g;
+    else if (d2 <= p.gr2f[g] * 1.00001f) near = true;
+  }
+  float rr = fmaf(x, x, y * y);
+  if (rr > p.Rh2f * 1.00001f) bits |= 1 << 30;
+  else if (rr >= p.Rh2f * 0.99999f) near = true;
+  // |z| >= H/2 (double) is exactly |z| >= Hz_f, the smallest float not below H/2
+  if (fabsf(z) >= p.Hz_f) bits |= 1 << 29;
+  if (near) return od_flag_exact(p, x, y, z);
+  return bits;
+}
+
+// ------------------------------------------------------------------ bounded mbarrier / bulk copy
+__device__ __forceinline__ uint32_t od_smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void od_mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(od_smem_addr(bar)), "r"(count));
+}
+__device__ __forceinline__ void od_fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void od_mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(od_smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// one-dimensional TMA bulk copy global -> shared, completing on an mbarrier
+__device__ __forceinline__ void od_bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                           uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          od_smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(od_smem_addr(bar))
+      : "memory");
+}
+// Wait for phase `parity` of the barrier; gives up after OD_WAIT_LIMIT polls and returns false.
+__device__ __forceinline__ bool od_mbar_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t addr = od_smem_addr(bar);
+  for (uint32_t it = 0; it < OD_WAIT_LIMIT; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}

@@ -1,0 +1,43 @@
+// od_internal.h — launch wrappers shared by the kernel and ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "od_common.cuh"
+
+// Work decomposition of the all-pairs force kernel.
+struct od_pair_plan {
+  int nt;      // threads per block
+  int ipt;     // targets per thread
+  int jsplit;  // source chunks (grid.y); partial slabs written per ion
+  int chunk;   // sources per chunk (multiple of OD_TJ)
+  int variant; // 0: shared-memory broadcast, 1: warp-shuffle broadcast
+};
+
+// Device buffers of one simulation.
+struct od_dbufs {
+  float4 *pos, *vel, *fhi, *flo;        // ion state and ion–ion sums (two-float)
+  float4 *part_hi, *part_lo;            // [jsplit][Npad] partial sums
+  uint32_t* flags;                      // [nwords] ballot words
+  int32_t* list;                        // [Npad] flagged ion indices, increasing
+  int32_t* list_bits;                   // [Npad] flag bits of each entry
+  float4 *list_old, *list_new, *list_v; // [Npad] pre/post re-injection positions, velocities
+  double* orbit_part;                   // [nb_corr][P][3]
+  double *s_q, *s_orbit, *s_collect, *s_dust, *s_field;  // result series
+  float* cq;                            // [P] A_id * q_param, FP32 copy for the ion kernels
+};
+
+int od_num_sms(int device);
+
+cudaError_t od_launch_pairs(const od_pair_plan& pl, const float4* pos, int Npad, float4* part_hi,
+                            float4* part_lo, float rho0, uint32_t* err, cudaStream_t s);
+cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* part_hi,
+                             const float4* part_lo, float4* fhi, float4* flo, cudaStream_t s);
+cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
+                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s);
+cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,
+                                     uint32_t* flags, int32_t* list, int32_t* list_bits,
+                                     double* counts, cudaStream_t s);
+cudaError_t od_launch_set_charges(const od_dparams* dp, od_dstate* ds, float* cq, int P,
+                                  cudaStream_t s);
+cudaError_t od_launch_trap(double Rh, double Hh, int n_r, int n_h, int64_t n_points, uint64_t seed,
+                           double* part, int nchunks, cudaStream_t s);

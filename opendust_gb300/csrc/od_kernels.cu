@@ -1,0 +1,795 @@
+// od_kernels.cu — CUDA kernels of the superion step (sm_103a).
+//
+// One step of the reference program (opendust.py:839-1037 + host tail :1117-1383) runs as
+//   K1 kick_drift      collisions, v += a/2 with forces at the current positions, x += v
+//   K2 pairs           ion–ion sums at the drifted positions (all pairs, N^2)
+//   K3 kick_flag       reduce K2 partials, v += a/2, grain/domain flags -> warp ballots
+//   K4 collect_inject  ordered compaction of flagged ions, per-grain sums, re-injection
+//   K5 correct_orbit   ion–ion sums moved to the re-injected positions, orbit-force sums
+//   K6 tail            FP64 charge update, grain forces, result series, averages
+// The reference evaluates ion–ion forces twice per step (after the drift and again after
+// re-injection, because OpenMM re-evaluates forces whenever positions change). Only the few
+// re-injected ions move between those two evaluations, so K5 applies their O(N*K) difference
+// to K2's sums instead of a second N^2 pass; the result is the same sum.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "od_internal.h"
+
+namespace {
+
+constexpr int kBlk = 256;
+
+// ============================================================== K2: all-pairs ion–ion sums
+// Block = NT threads x IPT targets; grid.y splits the sources into chunks. Source tiles of
+// OD_TJ float4 are staged in shared memory by one-dimensional TMA bulk copies (double
+// buffered, completion on an mbarrier); every thread then reads each source with a
+// broadcast shared-memory load (VARIANT 0) or each warp reads 32 sources and broadcasts
+// them with warp shuffles (VARIANT 1). Per target the tile's pair terms are summed in FP32
+// and folded into a (hi, lo) two-float accumulator once per tile.
+template <int NT, int IPT, int VARIANT>
+__global__ void __launch_bounds__(NT) k_pairs(const float4* __restrict__ pos, int Npad, int chunk,
+                                              float4* __restrict__ part_hi,
+                                              float4* __restrict__ part_lo, float rho0,
+                                              uint32_t* __restrict__ err) {
+  __shared__ __align__(128) float4 tile[2][OD_TJ];
+  __shared__ __align__(8) uint64_t bar[2];
+  const int tid = threadIdx.x;
+  const int ibase = blockIdx.x * (NT * IPT) + tid;
+  const int j0 = blockIdx.y * chunk;
+  const int j1 = min(j0 + chunk, Npad);
+  const int ntiles = (j1 - j0) / OD_TJ;
+
+  float px[IPT], py[IPT], pz[IPT], hx[IPT], hy[IPT], hz[IPT], lx[IPT], ly[IPT], lz[IPT];
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    float4 q = pos[ibase + k * NT];
+    px[k] = q.x; py[k] = q.y; pz[k] = q.z;
+    hx[k] = hy[k] = hz[k] = lx[k] = ly[k] = lz[k] = 0.f;
+  }
+  if (tid == 0) {
+    od_mbar_init(&bar[0], 1);
+    od_mbar_init(&bar[1], 1);
+    od_fence_barrier_init();
+  }
+  __syncthreads();
+  int issued = 0;
+  if (tid == 0) {
+    for (; issued < 2 && issued < ntiles; issued++) {
+      od_mbar_expect_tx(&bar[issued], OD_TJ * 16);
+      od_bulk_g2s(tile[issued], pos + j0 + issued * OD_TJ, OD_TJ * 16, &bar[issued]);
+    }
+  }
+  bool ok = true;
+  int t = 0;
+  for (; t < ntiles; t++) {
+    const int s = t & 1;
+    ok = __syncthreads_and(od_mbar_wait(&bar[s], (t >> 1) & 1));
+    if (!ok) break;
+    float ax[IPT], ay[IPT], az[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; k++) ax[k] = ay[k] = az[k] = 0.f;
+    if (VARIANT == 0) {
+#pragma unroll 8
+      for (int j = 0; j < OD_TJ; j++) {
+        const float4 q = tile[s][j];
+#pragma unroll
+        for (int k = 0; k < IPT; k++) {
+          float dx = px[k] - q.x, dy = py[k] - q.y, dz = pz[k] - q.z;
+          float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+          float c = od_pair_c(r2, rho0);
+          ax[k] = fmaf(c, dx, ax[k]); ay[k] = fmaf(c, dy, ay[k]); az[k] = fmaf(c, dz, az[k]);
+        }
+      }
+    } else {
+      const int lane = tid & 31;
+      for (int jj = 0; jj < OD_TJ; jj += 32) {
+        const float4 mine = tile[s][jj + lane];
+#pragma unroll 8
+        for (int l = 0; l < 32; l++) {
+          float qx = __shfl_sync(0xffffffffu, mine.x, l);
+          float qy = __shfl_sync(0xffffffffu, mine.y, l);
+          float qz = __shfl_sync(0xffffffffu, mine.z, l);
+#pragma unroll
+          for (int k = 0; k < IPT; k++) {
+            float dx = px[k] - qx, dy = py[k] - qy, dz = pz[k] - qz;
+            float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+            float c = od_pair_c(r2, rho0);
+            ax[k] = fmaf(c, dx, ax[k]); ay[k] = fmaf(c, dy, ay[k]); az[k] = fmaf(c, dz, az[k]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+      od_acc2(hx[k], lx[k], ax[k]);
+      od_acc2(hy[k], ly[k], ay[k]);
+      od_acc2(hz[k], lz[k], az[k]);
+    }
+    __syncthreads();  // all threads are done with stage s
+    if (tid == 0 && issued < ntiles) {
+      od_mbar_expect_tx(&bar[s], OD_TJ * 16);
+      od_bulk_g2s(tile[s], pos + j0 + issued * OD_TJ, OD_TJ * 16, &bar[s]);
+      issued++;
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicOr(err, OD_DERR_TIMEOUT);
+      for (int u = t; u < issued; u++) od_mbar_wait(&bar[u & 1], (u >> 1) & 1);
+    }
+    return;
+  }
+  const size_t off = (size_t)blockIdx.y * Npad;
+#pragma unroll
+  for (int k = 0; k < IPT; k++) {
+    const int i = ibase + k * NT;
+    part_hi[off + i] = make_float4(hx[k], hy[k], hz[k], 0.f);
+    part_lo[off + i] = make_float4(lx[k], ly[k], lz[k], 0.f);
+  }
+}
+
+// sum the jsplit partial slabs of ion i into (hi, lo)
+__device__ __forceinline__ void reduce_parts(const float4* __restrict__ ph,
+                                             const float4* __restrict__ pl, int Npad, int jsplit,
+                                             int i, float3& hi, float3& lo) {
+  hi = make_float3(0.f, 0.f, 0.f);
+  lo = make_float3(0.f, 0.f, 0.f);
+  for (int s = 0; s < jsplit; s++) {
+    float4 a = ph[(size_t)s * Npad + i], b = pl[(size_t)s * Npad + i];
+    od_acc2(hi.x, lo.x, a.x); lo.x += b.x;
+    od_acc2(hi.y, lo.y, a.y); lo.y += b.y;
+    od_acc2(hi.z, lo.z, a.z); lo.z += b.z;
+  }
+}
+
+__global__ void k_reduce(int Npad, int jsplit, const float4* __restrict__ ph,
+                         const float4* __restrict__ pl, float4* __restrict__ fhi,
+                         float4* __restrict__ flo) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Npad) return;
+  float3 hi, lo;
+  reduce_parts(ph, pl, Npad, jsplit, i, hi, lo);
+  fhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  flo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+}
+
+// ============================================================== K1: collisions, kick, drift
+__device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint32_t step,
+                                        float4& v) {
+  if (p.coll == OD_COLL_PER_DOF) {
+    // opendust.py:869-873: collision = step(p_collision - uniform) per velocity component
+    od_u4 w = od_draw(p, ion, step, OD_RNG_COLL_TEST);
+    bool c0 = (double)od_u01(w.x) <= p.p_coll, c1 = (double)od_u01(w.y) <= p.p_coll,
+         c2 = (double)od_u01(w.z) <= p.p_coll;
+    if (c0 | c1 | c2) {
+      od_u4 g = od_draw(p, ion, step, OD_RNG_COLL_GAUSS);
+      float gx, gy, gz, dummy;
+      od_gauss2(g.x, g.y, gx, gy);
+      od_gauss2(g.z, g.w, gz, dummy);
+      if (c0) v.x = p.vT * gx;
+      if (c1) v.y = p.vT * gy;
+      if (c2) v.z = p.vT * gz;
+    }
+  } else if (p.coll == OD_COLL_MFP) {
+    // null collision: candidate with probability Pmax, real with probability |v|/vmax
+    od_u4 w = od_draw(p, ion, step, OD_RNG_MFP_TEST);
+    if ((double)od_u01(w.x) < p.Pmax_mfp) {
+      float sp = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+      if (od_u01(w.y) * p.vmax_mfp < sp) {
+        od_u4 g = od_draw(p, ion, step, OD_RNG_MFP_GAUSS);
+        float gx, gy, gz, dummy;
+        od_gauss2(g.x, g.y, gx, gy);
+        od_gauss2(g.z, g.w, gz, dummy);
+        v.x = p.vT * gx; v.y = p.vT * gy; v.z = p.vT * gz;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restrict__ dp,
+                                                     const od_dstate* __restrict__ ds,
+                                                     float4* __restrict__ pos,
+                                                     float4* __restrict__ vel,
+                                                     const float4* __restrict__ fhi,
+                                                     const float4* __restrict__ flo,
+                                                     const float* __restrict__ cq) {
+  const od_dparams& p = *dp;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  float4 x = pos[i], v = vel[i];
+  if (p.coll != OD_COLL_NONE) collide(p, (uint32_t)i, (uint32_t)ds->step, v);
+  const float4 gh = fhi[i], gl = flo[i];
+  float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
+  a.x = fmaf(p.A_ii, gh.x + gl.x, a.x);
+  a.y = fmaf(p.A_ii, gh.y + gl.y, a.y);
+  a.z = fmaf(p.A_ii, gh.z + gl.z, a.z);
+  v.x = fmaf(0.5f, a.x, v.x); v.y = fmaf(0.5f, a.y, v.y); v.z = fmaf(0.5f, a.z, v.z);
+  x.x += v.x; x.y += v.y; x.z += v.z;
+  pos[i] = x;
+  vel[i] = v;
+}
+
+// ============================================================== K3: kick + flags
+__global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict__ dp,
+                                                    const float4* __restrict__ pos,
+                                                    float4* __restrict__ vel,
+                                                    const float4* __restrict__ ph,
+                                                    const float4* __restrict__ pl, int jsplit,
+                                                    float4* __restrict__ fhi,
+                                                    float4* __restrict__ flo,
+                                                    uint32_t* __restrict__ flags,
+                                                    const float* __restrict__ cq) {
+  const od_dparams& p = *dp;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // grid covers Npad exactly
+  int flag = 0;
+  if (i < p.N) {
+    float3 hi, lo;
+    reduce_parts(ph, pl, p.Npad, jsplit, i, hi, lo);
+    fhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+    flo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    const float4 x = pos[i];
+    float4 v = vel[i];
+    float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
+    a.x = fmaf(p.A_ii, hi.x + lo.x, a.x);
+    a.y = fmaf(p.A_ii, hi.y + lo.y, a.y);
+    a.z = fmaf(p.A_ii, hi.z + lo.z, a.z);
+    v.x = fmaf(0.5f, a.x, v.x); v.y = fmaf(0.5f, a.y, v.y); v.z = fmaf(0.5f, a.z, v.z);
+    vel[i] = v;
+    flag = od_flag(p, x.x, x.y, x.z) != 0;
+  }
+  const uint32_t ballot = __ballot_sync(0xffffffffu, flag);
+  if ((threadIdx.x & 31) == 0) flags[i >> 5] = ballot;
+}
+
+__global__ void __launch_bounds__(kBlk) k_flags_only(const od_dparams* __restrict__ dp, int n,
+                                                     const float4* __restrict__ pos,
+                                                     uint32_t* __restrict__ flags) {
+  const od_dparams& p = *dp;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int flag = 0;
+  if (i < n) {
+    const float4 x = pos[i];
+    flag = od_flag(p, x.x, x.y, x.z) != 0;
+  }
+  const uint32_t ballot = __ballot_sync(0xffffffffu, flag);
+  if ((threadIdx.x & 31) == 0) flags[i >> 5] = ballot;
+}
+
+// ============================================================== K4: compaction + re-injection
+// Order-preserving compaction of the ballot words by one 1024-thread block: each thread owns
+// a contiguous range of words, counts its bits, takes an exclusive block scan, then writes
+// its indices in increasing order. Returns the total (same in every thread).
+constexpr int kCT = 1024;
+__device__ int build_list(const uint32_t* __restrict__ flags, int nwords, int32_t* __restrict__ list) {
+  __shared__ int s_warp[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (nwords + kCT - 1) / kCT;
+  const int w0 = min(tid * per, nwords), w1 = min(w0 + per, nwords);
+  int cnt = 0;
+  for (int w = w0; w < w1; w++) cnt += __popc(flags[w]);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int v = s_warp[lane], iv = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, iv, o);
+      if (lane >= o) iv += y;
+    }
+    s_warp[lane] = iv - v;  // exclusive prefix of warp totals
+  }
+  __syncthreads();
+  int off = s_warp[wid] + incl - cnt;
+  for (int w = w0; w < w1; w++) {
+    uint32_t b = flags[w];
+    while (b) {
+      int bit = __ffs(b) - 1;
+      list[off++] = w * 32 + bit;
+      b &= b - 1;
+    }
+  }
+  // total = exclusive prefix of last warp + its inclusive total
+  __shared__ int s_total;
+  if (tid == kCT - 1) s_total = off;
+  __syncthreads();
+  int total = s_total;
+  __syncthreads();
+  return total;
+}
+
+// FP64 block sum over 1024 threads in a fixed order (deterministic)
+__device__ double block_sum_1024(double v) {
+  __shared__ double s_red[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) s_red[wid] = v;
+  __syncthreads();
+  double r = 0;
+  if (wid == 0) {
+    r = s_red[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) s_red[0] = r;
+  }
+  __syncthreads();
+  r = s_red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ float tab_eval(const od_dparams& p, int t, float u) {
+  const int n = p.tn[t];
+  int i = 1;
+  const double ud = u;
+  while (i < n - 1 && ud > p.txi[t][i]) i++;
+  return p.tv[t][i - 1] + (u - (float)p.txi[t][i - 1]) * p.tsl[t][i];
+}
+
+// Re-injection of one ion (opendust.py:923-975); draws keyed by (ion, step).
+__device__ void inject_one(const od_dparams& p, uint32_t ion, uint32_t step, float4& x, float4& v) {
+  od_u4 w = od_draw(p, ion, step, OD_RNG_FACE);
+  const double uf = od_u01(w.x);
+  int face;  // 0 top, 1 side, 2 bottom
+  if (uf <= p.p_t) face = 0;
+  else if (uf <= p.p_t + p.p_s || p.p_b == 0.0) face = 1;
+  else face = 2;
+  if (face != 1) {
+    const bool top = face == 0;
+    w = od_draw(p, ion, step, top ? OD_RNG_TOP_V : OD_RNG_BOT_V);
+    float gx, gy;
+    od_gauss2(w.x, w.y, gx, gy);
+    const float vz = tab_eval(p, top ? OD_TAB_TOP : OD_TAB_BOTTOM, od_u01(w.z));
+    v = make_float4(p.vT * gx, p.vT * gy, vz, 0.f);
+    w = od_draw(p, ion, step, top ? OD_RNG_TOP_X : OD_RNG_BOT_X);
+    const float rr = p.Rh * sqrtf(od_u01(w.x));
+    float s, c;
+    sincospif(2.0f * od_u01(w.y), &s, &c);
+    x = make_float4(rr * c, rr * s, top ? -p.Hh_half : p.Hh_half, 0.f);
+  } else {
+    w = od_draw(p, ion, step, OD_RNG_SIDE_X);
+    float s, c;
+    sincospif(2.0f * od_u01(w.x), &s, &c);
+    x = make_float4(p.Rh * c, p.Rh * s, od_u01(w.y) * p.Hh - p.Hh_half, 0.f);
+    w = od_draw(p, ion, step, OD_RNG_SIDE_V);
+    float gy, gz;
+    od_gauss2(w.x, w.y, gy, gz);
+    const float us = od_u01(w.z);
+    const float vn = tab_eval(p, OD_TAB_SIDE, us);
+    const float cx = x.x / p.Rh, cy = x.y / p.Rh;
+    v.x = -vn * cx + p.vT * gy * cy;
+    v.y = -vn * cy - p.vT * gy * cx;
+    v.z = (p.dist == OD_DIST_MAXWELLIAN) ? gz * p.vT + p.vfl : tab_eval(p, OD_TAB_VZ, us);
+    v.w = 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(kCT) k_collect_inject(
+    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ pos,
+    float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
+    int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
+    float4* __restrict__ list_new, float4* __restrict__ list_v) {
+  const od_dparams& p = *dp;
+  const int tid = threadIdx.x;
+  const int K = build_list(flags, p.nwords, list);
+  if (tid == 0) ds->nlist = K;
+  for (int k = tid; k < K; k += kCT) {
+    const int i = list[k];
+    const float4 x = pos[i], v = vel[i];
+    list_bits[k] = od_flag_exact(p, x.x, x.y, x.z);
+    list_old[k] = x;
+    list_v[k] = v;
+  }
+  __syncthreads();
+  // per-grain collected count and momentum (opendust.py:911-921), fixed-order FP64 sums
+  for (int g = 0; g < p.P; g++) {
+    double dn = 0, mx = 0, my = 0, mz = 0;
+    for (int k = tid; k < K; k += kCT)
+      if ((list_bits[k] >> g) & 1) {
+        const float4 v = list_v[k];
+        dn += 1.0; mx += v.x; my += v.y; mz += v.z;
+      }
+    dn = block_sum_1024(dn); mx = block_sum_1024(mx);
+    my = block_sum_1024(my); mz = block_sum_1024(mz);
+    if (tid == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
+  }
+  const uint32_t step = (uint32_t)ds->step;
+  for (int k = tid; k < K; k += kCT) {
+    const int i = list[k];
+    float4 x, v;
+    inject_one(p, (uint32_t)i, step, x, v);
+    pos[i] = x;
+    vel[i] = v;
+    list_new[k] = x;
+  }
+}
+
+// list + per-grain counts of a snapshot (no state change)
+__global__ void __launch_bounds__(kCT) k_list_only(const od_dparams* __restrict__ dp, int nwords,
+                                                   const float4* __restrict__ pos,
+                                                   const uint32_t* __restrict__ flags,
+                                                   int32_t* __restrict__ list,
+                                                   int32_t* __restrict__ list_bits,
+                                                   double* __restrict__ counts) {
+  const od_dparams& p = *dp;
+  const int tid = threadIdx.x;
+  const int K = build_list(flags, nwords, list);
+  for (int k = tid; k < K; k += kCT) {
+    const float4 x = pos[list[k]];
+    list_bits[k] = od_flag_exact(p, x.x, x.y, x.z);
+  }
+  __syncthreads();
+  for (int g = 0; g < p.P; g++) {
+    double dn = 0;
+    for (int k = tid; k < K; k += kCT) dn += (list_bits[k] >> g) & 1;
+    dn = block_sum_1024(dn);
+    if (tid == 0) counts[g] = dn;
+  }
+  if (tid == 0) counts[OD_MAX_GRAINS] = K;
+}
+
+// ============================================================== K5: correction + orbit sums
+__device__ __forceinline__ double block_sum_256(double v, double* s_red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) s_red[wid] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBlk / 32; w++) r += s_red[w];
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(kBlk) k_correct_orbit(
+    const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+    const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
+    const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
+    const float4* __restrict__ list_old, const float4* __restrict__ list_new,
+    double* __restrict__ orbit_part, int nb) {
+  __shared__ double s_red[kBlk / 32];
+  const od_dparams& p = *dp;
+  const int K = ds->nlist;
+  const int tid = threadIdx.x;
+  if ((int)blockIdx.x < nb) {
+    const int i = blockIdx.x * kBlk + tid;
+    const bool live = i < p.N;
+    const float4 x = live ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // orbit sums (opendust.py:977-1037): exp(-r)(x_p - x)(1/r^3 + 1/r^2), lambda units
+    for (int g = 0; g < p.P; g++) {
+      float tx = 0.f, ty = 0.f, tz = 0.f;
+      if (live) {
+        const float dx = (p.gxh[g] - x.x) + p.gxl[g];
+        const float dy = (p.gyh[g] - x.y) + p.gyl[g];
+        const float dz = (p.gzh[g] - x.z) + p.gzl[g];
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float ri = rsqrtf(r2);
+        const float r = r2 * ri;
+        const float e = od_ex2(r * OD_NLOG2E);
+        const float t = e * ri * ri * (ri + 1.0f);
+        tx = dx * t; ty = dy * t; tz = dz * t;
+      }
+      double sx = block_sum_256(tx, s_red);
+      double sy = block_sum_256(ty, s_red);
+      double sz = block_sum_256(tz, s_red);
+      if (tid == 0) {
+        double* o = orbit_part + ((size_t)blockIdx.x * p.P + g) * 3;
+        o[0] = sx; o[1] = sy; o[2] = sz;
+      }
+    }
+    // move the ion–ion sums of unflagged ions to the re-injected positions
+    if (K > 0 && live && !((flags[i >> 5] >> (i & 31)) & 1u)) {
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+      const bool cut = p.method == OD_FORCE_CUTOFF;
+      for (int k = 0; k < K; k++) {
+        const float4 qn = list_new[k], qo = list_old[k];
+        float dx = x.x - qn.x, dy = x.y - qn.y, dz = x.z - qn.z;
+        float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+        float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+        gx = fmaf(c, dx, gx); gy = fmaf(c, dy, gy); gz = fmaf(c, dz, gz);
+        dx = x.x - qo.x; dy = x.y - qo.y; dz = x.z - qo.z;
+        r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+        c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+        gx = fmaf(-c, dx, gx); gy = fmaf(-c, dy, gy); gz = fmaf(-c, dz, gz);
+      }
+      float4 h = fhi[i], l = flo[i];
+      od_acc2(h.x, l.x, gx); od_acc2(h.y, l.y, gy); od_acc2(h.z, l.z, gz);
+      fhi[i] = h;
+      flo[i] = l;
+    }
+  } else {
+    // full ion–ion sums of the re-injected ions at their new positions
+    __shared__ float s_h[3][kBlk], s_l[3][kBlk];
+    const int nrec = gridDim.x - nb;
+    const bool cut = p.method == OD_FORCE_CUTOFF;
+    for (int k = blockIdx.x - nb; k < K; k += nrec) {
+      const int i = list[k];
+      const float4 xi = list_new[k];
+      float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+      float ax = 0.f, ay = 0.f, az = 0.f;
+      int cnt = 0;
+      for (int j = tid; j < p.N; j += kBlk) {
+        const float4 q = pos[j];
+        const float dx = xi.x - q.x, dy = xi.y - q.y, dz = xi.z - q.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+        const float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+        ax = fmaf(c, dx, ax); ay = fmaf(c, dy, ay); az = fmaf(c, dz, az);
+        if (++cnt == 64) {
+          od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
+          ax = ay = az = 0.f;
+          cnt = 0;
+        }
+      }
+      od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
+      s_h[0][tid] = hx; s_h[1][tid] = hy; s_h[2][tid] = hz;
+      s_l[0][tid] = lx; s_l[1][tid] = ly; s_l[2][tid] = lz;
+      __syncthreads();
+      if (tid < 3) {
+        float h = 0.f, l = 0.f;
+        for (int u = 0; u < kBlk; u++) { od_acc2(h, l, s_h[tid][u]); l += s_l[tid][u]; }
+        s_h[tid][0] = h;
+        s_l[tid][0] = l;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        fhi[i] = make_float4(s_h[0][0], s_h[1][0], s_h[2][0], 0.f);
+        flo[i] = make_float4(s_l[0][0], s_l[1][0], s_l[2][0], 0.f);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ============================================================== K6: FP64 host-tail on device
+// opendust.py:1117-1202 (charge), :1205-1235 (dust–dust), :1237-1331 (orbit + out-of-domain),
+// :1333-1365 (collect), :1367-1383 (field)
+__device__ double charge_update(const od_dparams& p, int g, double q_prev, double dN) {
+  const double r = p.grs[g];
+  const double phi = p.k * q_prev / r;
+  const double gamma_e = p.n_inf * pow(p.T_e * p.k_B / OD_PI_D / p.m_e / 2.0, 0.5) *
+                         exp(-p.e * phi / p.T_e / p.k_B);
+  const double S = r * r * 4.0 * OD_PI_D;
+  if (p.gmethod[g] == OD_CHARGE_CONSISTENT) return q_prev + (dN * p.q_s + gamma_e * p.dt * S * p.e);
+  if (p.gmethod[g] == OD_CHARGE_OML) {
+    const double u = p.v_fl_si / p.v_T_si / sqrt(2.0);
+    const double chi = p.e * phi / p.T_n / p.k_B;
+    const double v_ti = p.v_T_si * sqrt(2.0);
+    const double gamma_i = p.n_inf * v_ti * u / 4.0 *
+                           ((1.0 + 1.0 / (2.0 * u * 2) + chi / (u * u)) * erf(u) +
+                            1.0 / u / sqrt(OD_PI_D) * exp(-(u * u)));
+    return q_prev + (gamma_i * p.dt * S * fabs(p.e) + gamma_e * p.dt * S * p.e);
+  }
+  return q_prev;
+}
+
+__device__ void out_domain_force(const od_dparams& p, double x, double y, double z, double q,
+                                 double* f) {
+  const double* a = p.alpha;
+  const double L = p.lam, L2 = L * L, L4 = L2 * L2, L6 = L4 * L2, L8 = L4 * L4;
+  const double r = sqrt(x * x + y * y);
+  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r5 = r4 * r, r6 = r4 * r2, r7 = r6 * r;
+  const double z2 = z * z, z3 = z2 * z, z4 = z2 * z2, z5 = z4 * z, z6 = z4 * z2, z7 = z6 * z;
+  double fR = (-2 * a[1] * r) / L2;
+  fR += (-2 * a[3] * r * z2 - 4 * a[4] * r3) / L4;
+  fR += (-4 * a[6] * r3 * z2 - 2 * a[7] * r * z4 - 6 * a[8] * r5) / L6;
+  fR += (-4 * a[10] * r3 * z4 - 6 * a[11] * r5 * z2 - 2 * a[12] * r * z6 - 8 * a[13] * r7) / L8;
+  fR *= p.k * q * p.q_s / L;
+  double fH = (-2 * a[2] * z) / L2;
+  fH += (-2 * a[3] * r2 * z - 4 * a[5] * z3) / L4;
+  fH += (-2 * a[6] * r4 * z - 4 * a[7] * r2 * z3 - 6 * a[9] * z5) / L6;
+  fH += (-4 * a[10] * r4 * z3 - 2 * a[11] * r6 * z - 6 * a[12] * r2 * z5 - 8 * a[14] * z7) / L8;
+  fH *= p.k * q * p.q_s / L;
+  if (r == 0) { f[0] = 0; f[1] = 0; }
+  else { f[0] = fR * x / r; f[1] = fR * y / r; }
+  f[2] = fH;
+}
+
+__global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp,
+                                               od_dstate* __restrict__ ds,
+                                               const double* __restrict__ orbit_part, int nb,
+                                               double* __restrict__ s_q, double* __restrict__ s_orbit,
+                                               double* __restrict__ s_collect,
+                                               double* __restrict__ s_dust,
+                                               double* __restrict__ s_field, float* __restrict__ cq) {
+  __shared__ double s_red[kBlk];
+  __shared__ double S[OD_MAX_GRAINS * 3];
+  const od_dparams& p = *dp;
+  const int tid = threadIdx.x;
+  const int nc = p.P * 3;
+  for (int c = 0; c < nc; c++) {
+    double v = 0;
+    for (int b = tid; b < nb; b += kBlk) v += orbit_part[(size_t)b * nc + c];
+    s_red[tid] = v;
+    __syncthreads();
+    for (int w = kBlk / 2; w > 0; w >>= 1) {
+      if (tid < w) s_red[tid] += s_red[tid + w];
+      __syncthreads();
+    }
+    if (tid == 0) S[c] = s_red[0];
+    __syncthreads();
+  }
+  if (tid != 0) return;
+  const int64_t step = ds->step;
+  const int P = p.P;
+  double qn[OD_MAX_GRAINS];
+  for (int g = 0; g < P; g++)
+    qn[g] = step > 0 ? charge_update(p, g, ds->q_param[g], ds->dN[g]) : ds->q_param[g];
+  const bool avg = step >= p.avg_start;
+  for (int g = 0; g < P; g++) {
+    double fd[3] = {0, 0, 0};
+    for (int j = 0; j < P; j++) {
+      if (j == g) continue;
+      const double dx = p.gxs[g] - p.gxs[j], dy = p.gys[g] - p.gys[j], dz = p.gzs[g] - p.gzs[j];
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      const double kk = p.k * qn[g] * qn[j] / (r * r * r);
+      fd[0] += kk * dx; fd[1] += kk * dy; fd[2] += kk * dz;
+    }
+    double fo[3];
+    out_domain_force(p, p.gxs[g], p.gys[g], p.gzs[g], qn[g], fo);
+    const double so = qn[g] * p.k * p.q_s / (p.lam * p.lam);
+    const double sc = p.vunit * p.m_s / p.dt;
+    double vals[13];
+    vals[0] = qn[g];
+    for (int d = 0; d < 3; d++) {
+      vals[1 + d] = S[g * 3 + d] * so + fo[d];
+      vals[4 + d] = ds->M[g][d] * sc;
+      vals[7 + d] = fd[d];
+      vals[10 + d] = (d == 2 && p.dist == OD_DIST_FIELD_DRIVEN) ? qn[g] * p.E : 0.0;
+    }
+    const size_t r = (size_t)step * P + g;
+    s_q[r] = vals[0];
+    for (int d = 0; d < 3; d++) {
+      s_orbit[r * 3 + d] = vals[1 + d];
+      s_collect[r * 3 + d] = vals[4 + d];
+      s_dust[r * 3 + d] = vals[7 + d];
+      s_field[r * 3 + d] = vals[10 + d];
+    }
+    if (avg)
+      for (int m = 0; m < 13; m++) ds->avg[g][m] += vals[m];
+  }
+  for (int g = 0; g < P; g++) {
+    ds->q_param[g] = qn[g];
+    cq[g] = (float)(p.A_id_d * qn[g]);
+  }
+  if (avg) ds->n_avg += 1;
+  ds->n_inj_total += ds->nlist;
+  ds->step = step + 1;
+}
+
+__global__ void k_set_charges(const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+                              float* __restrict__ cq, int P) {
+  const int g = threadIdx.x;
+  if (g < P) cq[g] = (float)(dp->A_id_d * ds->q_param[g]);
+}
+
+// ============================================================== trap-fit potential grid
+constexpr int kTrapPts = 2048;
+__global__ void __launch_bounds__(kBlk) k_trap(double Rh, double Hh, int n_r, int n_h,
+                                               int64_t n_points, int64_t pts_per_block,
+                                               uint32_t k0, uint32_t k1,
+                                               double* __restrict__ part) {
+  __shared__ float4 s_pts[kTrapPts];
+  const int node = blockIdx.x * kBlk + threadIdx.x;
+  const int nn = n_r * n_h;
+  float gr = 0.f, gh = 0.f;
+  if (node < nn) {
+    const int i = node / n_h, j = node % n_h;
+    gr = (float)((i == n_r - 1) ? Rh : i * (Rh / (n_r - 1)));
+    gh = (float)((j == n_h - 1) ? Hh / 2.0 : j * ((Hh / 2.0) / (n_h - 1)));
+  }
+  const int64_t p0 = blockIdx.y * pts_per_block;
+  const int64_t p1 = min(p0 + pts_per_block, n_points);
+  double acc = 0.0;
+  for (int64_t t0 = p0; t0 < p1; t0 += kTrapPts) {
+    const int cnt = (int)min((int64_t)kTrapPts, p1 - t0);
+    __syncthreads();
+    for (int q = threadIdx.x; q < cnt; q += kBlk) {
+      od_u4 w = od_philox((uint32_t)(t0 + q), 0u, OD_RNG_TRAP, 0u, k0, k1);
+      const float r = sqrtf(od_u01(w.x));
+      float s, c;
+      sincospif(2.0f * od_u01(w.y), &s, &c);
+      s_pts[q] = make_float4((float)Rh * r * c, (float)Rh * r * s,
+                             (float)Hh * od_u01(w.z) - (float)Hh * 0.5f, 0.f);
+    }
+    __syncthreads();
+    float a = 0.f;
+    for (int q = 0; q < cnt; q++) {
+      const float4 pt = s_pts[q];
+      const float dx = gr - pt.x, dy = pt.y, dz = gh - pt.z;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float ri = od_rsqrt(fmaxf(r2, 1e-30f));
+      const float r = r2 * ri;
+      a += od_ex2(r * OD_NLOG2E) * od_rcp(r + 0.001f);
+    }
+    acc += a;
+  }
+  if (node < nn) part[(size_t)blockIdx.y * nn + node] = acc;
+}
+
+}  // namespace
+
+// ============================================================== launch wrappers
+int od_num_sms(int device) {
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
+  return n;
+}
+
+template <int NT, int IPT, int V>
+static void launch_pairs_t(const od_pair_plan& pl, const float4* pos, int Npad, float4* ph,
+                           float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
+  dim3 grid(Npad / (NT * IPT), pl.jsplit);
+  k_pairs<NT, IPT, V><<<grid, NT, 0, s>>>(pos, Npad, pl.chunk, ph, plo, rho0, err);
+}
+
+cudaError_t od_launch_pairs(const od_pair_plan& pl, const float4* pos, int Npad, float4* ph,
+                            float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
+  const int key = pl.nt * 100 + pl.ipt * 10 + pl.variant;
+  switch (key) {
+    case 12810: launch_pairs_t<128, 1, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 12820: launch_pairs_t<128, 2, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 25610: launch_pairs_t<256, 1, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 25620: launch_pairs_t<256, 2, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 12811: launch_pairs_t<128, 1, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 25611: launch_pairs_t<256, 1, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 25621: launch_pairs_t<256, 2, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* ph,
+                             const float4* pl, float4* fhi, float4* flo, cudaStream_t s) {
+  (void)dp;
+  k_reduce<<<(Npad + kBlk - 1) / kBlk, kBlk, 0, s>>>(Npad, jsplit, ph, pl, fhi, flo);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
+                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s) {
+  (void)P;
+  const int nb = Npad / kBlk;
+  k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq);
+  cudaError_t e = od_launch_pairs(pl, b.pos, Npad, b.part_hi, b.part_lo, rho0, &ds->err, s);
+  if (e != cudaSuccess) return e;
+  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, pl.jsplit, b.fhi, b.flo,
+                                  b.flags, b.cq);
+  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
+                                     b.list_old, b.list_new, b.list_v);
+  k_correct_orbit<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
+                                            b.list_old, b.list_new, b.orbit_part, nb);
+  k_tail<<<1, kBlk, 0, s>>>(dp, ds, b.orbit_part, nb, b.s_q, b.s_orbit, b.s_collect, b.s_dust,
+                           b.s_field, b.cq);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,
+                                     uint32_t* flags, int32_t* list, int32_t* list_bits,
+                                     double* counts, cudaStream_t s) {
+  k_flags_only<<<Npad / kBlk, kBlk, 0, s>>>(dp, n, pos, flags);
+  k_list_only<<<1, kCT, 0, s>>>(dp, Npad / 32, pos, flags, list, list_bits, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_set_charges(const od_dparams* dp, od_dstate* ds, float* cq, int P,
+                                  cudaStream_t s) {
+  k_set_charges<<<1, 32, 0, s>>>(dp, ds, cq, P);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_trap(double Rh, double Hh, int n_r, int n_h, int64_t n_points, uint64_t seed,
+                           double* part, int nchunks, cudaStream_t s) {
+  const int nn = n_r * n_h;
+  const int64_t per = (n_points + nchunks - 1) / nchunks;
+  dim3 grid((nn + kBlk - 1) / kBlk, nchunks);
+  k_trap<<<grid, kBlk, 0, s>>>(Rh, Hh, n_r, n_h, n_points, per, (uint32_t)(seed & 0xffffffffu),
+                               (uint32_t)(seed >> 32), part);
+  return cudaGetLastError();
+}
