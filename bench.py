@@ -1,0 +1,327 @@
+#!/usr/bin/env python
+"""Benchmark of the per-timestep superion update (one JSON line on stdout).
+
+Workload (default "full_plain"): Ar+ plasma at Mach 1 around one grain, R = 3 lambda,
+H = 6 lambda, N = 2^20 superions, all-pairs screened ion–ion forces, charge-exchange
+collisions with a 2 lambda mean free path, d_t = 1e-10 s (opendust_gb300.workloads).
+One "step" is one pass of the superion update over all N ions (kick, drift, N^2 force,
+kick, flags, ordered compaction, re-injection, grain sums, FP64 tail).
+
+  value      ion-steps/s from CUDA events on the library's stream over K timed steps, inputs
+             resident in HBM, L2 flushed (512 MB write) before every timed step.
+  e2e        the same metric through the C ABI with host arrays: od_set_state (host->device),
+             od_step, od_get_series + od_get_state (device->host), wall clock.
+  roofline   the all-pairs force kernel: N(N-1) pair interactions x 25 FP32 flops per launch
+             over its CUDA-event duration, against the FP32 FMA peak measured on the same GPU.
+  cpu_baseline  the CPU oracle (FP64 C restatement of the reference step, OpenMP over all host
+             cores) on a bounded sample: the reference's two ion–ion evaluations per step for T
+             target ions against all N sources plus one linear pass over all N ions.
+
+--impl reference times that CPU restatement alone (the reference's own OpenMM/CuPy path
+cannot be installed or run on this machine) and prints the same metric.
+Multi-GPU (torchrun, N > 1): independent replicas, one per GPU (the plain path does not
+shard); value = ion-steps of all ranks / max over ranks of the timed duration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_PAIR = 25
+KERNELS_PER_STEP = 6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="full_plain", choices=["full_plain", "small_plain"])
+    ap.add_argument("--cpu-sample-targets", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self, backend):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            if backend == "nccl":
+                import torch
+
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        dev = f"cuda:{self.local}" if self.dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX if op == "max" else self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        mhz = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(mhz) if mhz else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def workload(name: str, n_total: int):
+    from opendust_gb300 import workloads
+
+    if name == "full_plain":
+        return workloads.full_plain(n=n_total)
+    return workloads.small_plain(n=n_total)
+
+
+def describe(name, sim, ext):
+    w = {"full_plain": "Ar+ Mach 1 flow past one grain (r=10 um, consistent charging), "
+                       "N=2^20 superions, all-pairs Yukawa, charge-exchange mfp 2 lambda, d_t=1e-10 s",
+         "small_plain": "Ar+ Mach 1 flow past one grain, N=16384, all-pairs Yukawa, no collisions, "
+                        "d_t=1e-10 s"}[name]
+    return {"workload": f"{name}: {w}", "n_ions": int(sim.N), "grains": 1,
+            "force": "all-pairs", "collisions": ext.get("collisions", "none"),
+            "l2": "flushed (512 MB write) before every timed step",
+            "steps_in_workload": {"full_plain": 20000, "small_plain": 2000}[name]}
+
+
+def cpu_sample(holder, pos, targets: int, repeats: int = 2):
+    """Seconds per full reference step on the host, estimated from a bounded sample."""
+    import numpy as np
+
+    from oracle import oracle
+
+    n = pos.shape[0]
+    idx = np.linspace(0, n - 1, targets).astype(np.int64)
+    best = None
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        oracle.force_targets(holder, pos, idx)  # ion–ion evaluation A (opendust.py:864)
+        oracle.force_targets(holder, pos, idx)  # ion–ion evaluation B (opendust.py:866)
+        t1 = time.perf_counter()
+        oracle.collect_flags(holder, pos)       # one linear pass over all N ions
+        t2 = time.perf_counter()
+        est = (t1 - t0) * (n / targets) + (t2 - t1)
+        best = est if best is None else min(best, est)
+    return best, oracle.max_threads()
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return 0
+    import numpy as np
+
+    from opendust_gb300 import build_simulation, setup_host
+    from oracle import oracle
+
+    plasma, sim, grains, d, ext = workload(args.workload, 10)
+    holder, _ = build_simulation(plasma, sim, grains, d, seed=1, trap=np.zeros(15), **ext)
+    pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
+                                        plasma.v_fl, plasma.v_T, d, 1)
+    T = args.cpu_sample_targets or (256 if sim.N > 100000 else 4096)
+    oracle.set_threads(os.cpu_count() or 1)
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(holder, pos, T, repeats=1)
+    per_step = []
+    for _ in range(args.steps):
+        s, cores = cpu_sample(holder, pos, T, repeats=1)
+        per_step.append(s)
+    sec = sum(per_step) / len(per_step)
+    value = sim.N / sec
+    sample = (f"{T} of {sim.N} target ions x 2 ion-ion evaluations against all sources + one "
+              f"linear pass over all ions per step; time per full step extrapolated by N/T")
+    line = {
+        "impl": "reference", "metric": "ion-steps/s", "value": value, "unit": "ion-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": describe(args.workload, sim, ext),
+        "cpu_baseline": {"value": value, "unit": "ion-steps/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "ion-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's OpenMM/CuPy path cannot be installed here; this is the FP64 C "
+                "restatement of its step (oracle/od_oracle.c) on the host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic(n_ions: int):
+    """DRAM bytes per all-pairs launch from the committed ncu summary, scaled to n_ions."""
+    path = os.path.join(ROOT, "profiles", "allpairs_traffic.json")
+    try:
+        d = json.load(open(path))
+    except (OSError, ValueError):
+        return None
+    per_ion = d.get("dram_bytes_per_launch_per_ion")
+    return None if per_ion is None else per_ion * n_ions
+
+
+def run_ours(args, dist: Dist):
+    import numpy as np
+    import torch
+
+    from opendust_gb300 import _lib, build_simulation, setup_host
+
+    device = dist.local
+    torch.cuda.set_device(device)
+    K, W = args.steps, args.warmup
+    K_e2e = max(2, K)
+    n_total = W + K + K_e2e + 4
+    plasma, sim, grains, d, ext = workload(args.workload, n_total)
+    seed = 1000 + dist.rank
+    holder, _ = build_simulation(plasma, sim, grains, d, seed=seed, device=device, **ext)
+    pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
+                                        plasma.v_fl, plasma.v_T, d, seed)
+    N = int(sim.N)
+    peak = _lib.fp32_peak_tflops(device)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
+    eng = _lib.Engine(holder, device)
+    eng.set_state(pos, vel)
+    eng.step(W)  # warm-up (graph replay path)
+    eng.set_timing(True)
+    clocks = Clocks(device)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for _ in range(K):
+        flush.zero_()
+        torch.cuda.synchronize()
+        eng.step(1)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    step_ms, nsteps, pair_ms, pair_launches = eng.timing()
+    eng.set_timing(False)
+    t_max = dist.reduce(step_ms, "max")
+    ions_all = dist.reduce(float(N * K), "sum")
+    value = ions_all / (t_max * 1e-3)
+    pair_avg_s = pair_ms / pair_launches * 1e-3
+    achieved = N * (N - 1) * FLOPS_PER_PAIR / pair_avg_s / 1e12
+    traffic = load_traffic(N)
+
+    # e2e through the C ABI with host buffers (the calls simulate() makes)
+    eng.close()
+    eng = _lib.Engine(holder, device)
+    dist.barrier()
+    t0 = time.perf_counter()
+    eng.set_state(pos, vel)
+    eng.step(K_e2e)
+    ser = eng.series(0, K_e2e)
+    p_out, v_out = eng.get_state()
+    t1 = time.perf_counter()
+    e2e_t = dist.reduce(t1 - t0, "max")
+    e2e_value = dist.reduce(float(N * K_e2e), "sum") / e2e_t
+    h2d = 2 * N * 16
+    d2h = sum(a.nbytes for a in ser.values()) // 2 + 2 * N * 16  # float4 state copies
+    eng.close()
+    assert np.isfinite(ser["q"]).all() and np.isfinite(p_out).all()
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        T = args.cpu_sample_targets or (512 if N > 100000 else 4096)
+        sec, cores = cpu_sample(holder, pos, T, repeats=2)
+        cpu = {"value": N / sec, "unit": "ion-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{T} of {N} target ions x 2 ion-ion evaluations + one linear pass; "
+                         f"full-step time extrapolated by N/T (FP64 C oracle, OpenMP)"}
+    if dist.rank == 0:
+        line = {
+            "metric": "ion-steps/s", "value": value, "unit": "ion-steps/s", "n_gpus": dist.world,
+            "steps": K, "warmup": W, "ms_per_step": t_max / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded initial state and Philox streams)",
+            "config": {**describe(args.workload, sim, ext),
+                       "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
+            "pair_interactions_per_s": value * (N - 1),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_pairs (all-pairs ion-ion)",
+                         "peak_source": "FP32 FMA probe measured on this GPU in this run",
+                         "flops_per_pair": FLOPS_PER_PAIR, "pair_ms_avg": pair_avg_s * 1e3},
+            "e2e": {"value": e2e_value, "unit": "ion-steps/s", "h2d_bytes_per_step": h2d // K_e2e,
+                    "d2h_bytes_per_step": d2h // K_e2e},
+            "gpu_launches": KERNELS_PER_STEP * K,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    dist = Dist("gloo" if args.impl == "reference" else "nccl")
+    try:
+        rc = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+    finally:
+        dist.close()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

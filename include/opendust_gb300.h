@@ -169,6 +169,29 @@ od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n);
  * series (cfg->n_steps entries) is full. */
 od_status od_step(od_handle* h, int64_t nsteps);
 
+/* Device timing of od_step (no counterpart in the reference, which times simulate() with
+ * time.time(), performance/NVIDIA-V100/benchmark.py:82-87). With timing enabled, od_step
+ * launches kernel by kernel and records CUDA events on the handle's stream around every step
+ * and every all-pairs force launch; od_get_timing returns the summed device milliseconds.
+ * Enabling resets the sums. Without timing, od_step replays a CUDA graph of one step. */
+od_status od_set_timing(od_handle* h, int32_t enable);
+od_status od_get_timing(od_handle* h, double* step_ms, int64_t* steps, double* pair_ms,
+                        int64_t* pair_launches);
+/* Use (1, default) or bypass (0) the CUDA-graph replay of a step. */
+od_status od_set_graph(od_handle* h, int32_t enable);
+/* Work decomposition of the all-pairs force kernel (OpenMM picks its own nonbonded
+ * kernel configuration; this exposes ours). variant 0: shared-memory broadcast of each
+ * source, 1: warp-shuffle broadcast, 2: packed f32x2 pair arithmetic on SoA tiles (two
+ * targets per thread), 3: as 2 with Newton reciprocals for half of the targets.
+ * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
+od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
+                           int32_t variant, int32_t jsplit);
+/* plan5 = {threads, targets_per_thread, variant, jsplit, chunk} */
+od_status od_get_pair_plan(const od_handle* h, int32_t* plan5);
+/* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured by a short probe
+ * kernel: the denominator of the all-pairs kernel's roofline. */
+od_status od_probe_fp32_peak(int32_t device, double* tflops);
+
 /* Index of the next step (number of steps taken so far). */
 int64_t od_step_index(const od_handle* h);
 

@@ -133,6 +133,12 @@ def load(path: str | None = None):
             c_int32,
             [H, _DP, c_int64, POINTER(c_int64), c_int64, POINTER(c_int64), POINTER(c_int64)],
         ),
+        "od_set_timing": (c_int32, [H, c_int32]),
+        "od_get_timing": (c_int32, [H, _DP, POINTER(c_int64), _DP, POINTER(c_int64)]),
+        "od_set_graph": (c_int32, [H, c_int32]),
+        "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
+        "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
+        "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
         "od_trap_potential": (
             c_int32,
             [c_double, c_double, c_int32, c_int32, c_int64, c_uint64, c_int32, _DP],
@@ -307,6 +313,28 @@ class Engine:
         check(self._lib.od_get_averages(self.h, _dptr(out), ctypes.byref(n)), self.h)
         return out, int(n.value)
 
+    def set_timing(self, enable: bool = True):
+        check(self._lib.od_set_timing(self.h, int(bool(enable))), self.h)
+
+    def timing(self):
+        """(step_ms, steps, pair_ms, pair_launches) summed since timing was enabled."""
+        sm, pm = c_double(), c_double()
+        st, pl = c_int64(), c_int64()
+        check(self._lib.od_get_timing(self.h, ctypes.byref(sm), ctypes.byref(st), ctypes.byref(pm),
+                                      ctypes.byref(pl)), self.h)
+        return sm.value, st.value, pm.value, pl.value
+
+    def set_pair_plan(self, threads: int, targets_per_thread: int, variant: int, jsplit: int = 0):
+        check(self._lib.od_set_pair_plan(self.h, threads, targets_per_thread, variant, jsplit), self.h)
+
+    def pair_plan(self):
+        a = (c_int32 * 5)()
+        check(self._lib.od_get_pair_plan(self.h, a), self.h)
+        return dict(zip(("threads", "targets_per_thread", "variant", "jsplit", "chunk"), list(a)))
+
+    def set_graph(self, enable: bool = True):
+        check(self._lib.od_set_graph(self.h, int(bool(enable))), self.h)
+
     def force_snapshot(self, pos: np.ndarray) -> np.ndarray:
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         f = np.empty_like(pos)
@@ -336,6 +364,13 @@ class Engine:
         )
         check(st, self.h)
         return idx[: cnt.value].copy(), int(cnt.value), gc[: self.P].copy()
+
+
+def fp32_peak_tflops(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+    t = c_double()
+    check(load().od_probe_fp32_peak(int(device), ctypes.byref(t)), None)
+    return t.value
 
 
 def trap_potential(Rh: float, Hh: float, n_r: int, n_h: int, n_points: int, seed: int, device: int = 0):

@@ -29,6 +29,16 @@ struct od_handle {
   // snapshot scratch (allocated on first use)
   float4 *snap_pos = nullptr, *snap_hi = nullptr, *snap_lo = nullptr;
   double* snap_counts = nullptr;
+  // CUDA graph of one step (production path)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  bool use_graph = true;
+  // device timing (events on the handle's stream)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> ev_step, ev_pair;  // indices into ev_pool
+  double t_step_ms = 0, t_pair_ms = 0;
+  int64_t t_steps = 0, t_pair_launches = 0;
   std::string err;
 };
 
@@ -184,10 +194,11 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->n_steps = c->n_steps; p->avg_start = c->avg_start;
 }
 
-// Heuristic work split of the all-pairs kernel: enough blocks for several waves on every SM.
+// Default all-pairs plan: packed f32x2 arithmetic on SoA tiles (fastest variant measured on
+// GB300 from 2^16 to 2^20 ions), with enough source chunks for several waves on every SM.
 static od_pair_plan default_plan(int Npad, int sms) {
   od_pair_plan pl{};
-  pl.nt = 256; pl.ipt = 1; pl.variant = 0;
+  pl.nt = 256; pl.ipt = 2; pl.variant = 2;
   const int nbx = Npad / (pl.nt * pl.ipt);
   const int target = std::max(1, sms * 8 * 4);
   int js = std::max(1, (target + nbx - 1) / nbx);
@@ -204,11 +215,22 @@ static cudaError_t dalloc(T** p, size_t n) {
   return cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(n, 1));
 }
 
+static void free_timing(od_handle* h) {
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  h->ev_pool.clear();
+  h->ev_step.clear();
+  h->ev_pair.clear();
+}
+
 static void free_all(od_handle* h) {
+  if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  free_timing(h);
   void* ptrs[] = {h->dp, h->ds, h->b.pos, h->b.vel, h->b.fhi, h->b.flo, h->b.part_hi, h->b.part_lo,
                   h->b.flags, h->b.list, h->b.list_bits, h->b.list_old, h->b.list_new, h->b.list_v,
                   h->b.orbit_part, h->b.s_q, h->b.s_orbit, h->b.s_collect, h->b.s_dust,
-                  h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts};
+                  h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
+                  h->b.sx, h->b.sy, h->b.sz};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -273,6 +295,9 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
   OD_CKC(dalloc(&h->b.s_dust, ns * P * 3));
   OD_CKC(dalloc(&h->b.s_field, ns * P * 3));
   OD_CKC(dalloc(&h->b.cq, OD_MAX_GRAINS));
+  OD_CKC(dalloc(&h->b.sx, Np));
+  OD_CKC(dalloc(&h->b.sy, Np));
+  OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
   OD_CKC(cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
   od_dstate s0{};
@@ -281,6 +306,7 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
   // padded slots: far-away sources, zero velocity
   std::vector<float4> pad(Np, make_float4(OD_SENTINEL, OD_SENTINEL, OD_SENTINEL, 0.f));
   OD_CKC(cudaMemcpy(h->b.pos, pad.data(), sizeof(float4) * Np, cudaMemcpyHostToDevice));
+  OD_CKC(od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
   OD_CKC(cudaMemset(h->b.vel, 0, sizeof(float4) * Np));
   OD_CKC(cudaMemset(h->b.fhi, 0, sizeof(float4) * Np));
   OD_CKC(cudaMemset(h->b.flo, 0, sizeof(float4) * Np));
@@ -330,8 +356,9 @@ static od_status check_device_err(od_handle* h) {
 // ion–ion sums of the current positions into fhi/flo (the force the first half kick uses)
 static od_status refresh_forces(od_handle* h) {
   const float rho0 = h->hp.rho0;
-  OD_CK(h, od_launch_pairs(h->plan, h->b.pos, h->Npad, h->b.part_hi, h->b.part_lo, rho0,
-                           &h->ds->err, h->stream));
+  OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
+  OD_CK(h, od_launch_pairs(h->plan, od_pair_io{h->b.pos, h->b.sx, h->b.sy, h->b.sz}, h->Npad,
+                           h->b.part_hi, h->b.part_lo, rho0, &h->ds->err, h->stream));
   OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->b.fhi,
                             h->b.flo, h->stream));
   return OD_OK;
@@ -371,6 +398,72 @@ extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_
   return OD_OK;
 }
 
+static od_status event_at(od_handle* h, size_t slot, int* idx) {
+  while (h->ev_pool.size() <= slot) {
+    cudaEvent_t e;
+    OD_CK(h, cudaEventCreate(&e));
+    h->ev_pool.push_back(e);
+  }
+  *idx = (int)slot;
+  return OD_OK;
+}
+
+// Steps launched one kernel at a time with CUDA events around every step and every all-pairs
+// launch (timing mode).
+static od_status step_timed(od_handle* h, int64_t nsteps) {
+  size_t slot = 0;
+  h->ev_step.clear();
+  h->ev_pair.clear();
+  for (int64_t s = 0; s < nsteps; s++) {
+    int a, b, c, d;
+    if (event_at(h, slot++, &a) || event_at(h, slot++, &b) || event_at(h, slot++, &c) ||
+        event_at(h, slot++, &d))
+      return OD_ERR_CUDA;
+    OD_CK(h, cudaEventRecord(h->ev_pool[a], h->stream));
+    const int nb = h->Npad / 256;
+    OD_CK(h, od_launch_step_part(0, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+                                 h->nrec, h->stream));
+    OD_CK(h, cudaEventRecord(h->ev_pool[c], h->stream));
+    OD_CK(h, od_launch_step_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+                                 h->nrec, h->stream));
+    OD_CK(h, cudaEventRecord(h->ev_pool[d], h->stream));
+    OD_CK(h, od_launch_step_part(2, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+                                 h->nrec, h->stream));
+    OD_CK(h, cudaEventRecord(h->ev_pool[b], h->stream));
+    (void)nb;
+    h->ev_step.push_back({a, b});
+    h->ev_pair.push_back({c, d});
+  }
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  for (auto& p : h->ev_step) {
+    float ms;
+    OD_CK(h, cudaEventElapsedTime(&ms, h->ev_pool[p.first], h->ev_pool[p.second]));
+    h->t_step_ms += ms;
+    h->t_steps++;
+  }
+  for (auto& p : h->ev_pair) {
+    float ms;
+    OD_CK(h, cudaEventElapsedTime(&ms, h->ev_pool[p.first], h->ev_pool[p.second]));
+    h->t_pair_ms += ms;
+    h->t_pair_launches++;
+  }
+  return OD_OK;
+}
+
+static od_status ensure_graph(od_handle* h) {
+  if (h->graph_exec) return OD_OK;
+  OD_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+                                 h->nrec, h->stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(h, e, "step capture"); }
+  if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+  h->graph = g;
+  OD_CK(h, cudaGraphInstantiate(&h->graph_exec, g, 0));
+  return OD_OK;
+}
+
 extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!h->state_set) return fail(h, OD_ERR_STATE, "od_set_state has not been called");
@@ -378,12 +471,100 @@ extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
   if (h->step + nsteps > h->cfg.n_steps)
     return fail(h, OD_ERR_STATE, "the result series is full (n_steps reached)");
   OD_CK(h, cudaSetDevice(h->device));
-  for (int64_t s = 0; s < nsteps; s++) {
-    OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0, h->nrec,
-                            h->stream));
+  if (h->timing) {
+    od_status st = step_timed(h, nsteps);
+    if (st != OD_OK) return st;
+  } else if (h->use_graph) {
+    od_status st = ensure_graph(h);
+    if (st != OD_OK) return st;
+    for (int64_t s = 0; s < nsteps; s++) OD_CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  } else {
+    for (int64_t s = 0; s < nsteps; s++)
+      OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+                              h->nrec, h->stream));
   }
   h->step += nsteps;
   return check_device_err(h);
+}
+
+extern "C" od_status od_set_timing(od_handle* h, int32_t enable) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  h->timing = enable != 0;
+  h->t_step_ms = h->t_pair_ms = 0;
+  h->t_steps = h->t_pair_launches = 0;
+  return OD_OK;
+}
+
+extern "C" od_status od_get_timing(od_handle* h, double* step_ms, int64_t* steps, double* pair_ms,
+                                   int64_t* pair_launches) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (step_ms) *step_ms = h->t_step_ms;
+  if (steps) *steps = h->t_steps;
+  if (pair_ms) *pair_ms = h->t_pair_ms;
+  if (pair_launches) *pair_launches = h->t_pair_launches;
+  return OD_OK;
+}
+
+extern "C" od_status od_set_graph(od_handle* h, int32_t enable) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  h->use_graph = enable != 0;
+  return OD_OK;
+}
+
+static bool plan_supported(int nt, int ipt, int variant) {
+  const int key = nt * 100 + ipt * 10 + variant;
+  switch (key) {
+    case 12810: case 12820: case 25610: case 25620: case 12811: case 25611: case 25621:
+    case 12822: case 25622: case 12823: case 25623:
+      return true;
+    default:
+      return false;
+  }
+}
+
+extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
+                                      int32_t variant, int32_t jsplit) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!plan_supported(threads, targets_per_thread, variant))
+    return fail(h, OD_ERR_INVALID, "unsupported (threads, targets_per_thread, variant)");
+  if (h->Npad % (threads * targets_per_thread) != 0)
+    return fail(h, OD_ERR_INVALID, "block does not divide the padded ion count");
+  od_pair_plan pl{};
+  pl.nt = threads; pl.ipt = targets_per_thread; pl.variant = variant;
+  if (jsplit <= 0) {
+    pl = default_plan(h->Npad, od_num_sms(h->device));
+    pl.nt = threads; pl.ipt = targets_per_thread; pl.variant = variant;
+    const int nbx = h->Npad / (threads * targets_per_thread);
+    jsplit = std::max(1, (od_num_sms(h->device) * 8 * 4 + nbx - 1) / nbx);
+  }
+  jsplit = std::min(jsplit, h->Npad / OD_TJ);
+  int chunk = (h->Npad + jsplit - 1) / jsplit;
+  chunk = ((chunk + OD_TJ - 1) / OD_TJ) * OD_TJ;
+  pl.chunk = chunk;
+  pl.jsplit = (h->Npad + chunk - 1) / chunk;
+  const bool grow = pl.jsplit > h->plan.jsplit;
+  h->plan = pl;
+  if (grow && alloc_scratch_for_plan(h) != OD_OK) return OD_ERR_OOM;
+  if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  return OD_OK;
+}
+
+extern "C" od_status od_get_pair_plan(const od_handle* h, int32_t* plan5) {
+  if (!h || !plan5) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
+  plan5[0] = h->plan.nt; plan5[1] = h->plan.ipt; plan5[2] = h->plan.variant;
+  plan5[3] = h->plan.jsplit; plan5[4] = h->plan.chunk;
+  return OD_OK;
+}
+
+extern "C" od_status od_probe_fp32_peak(int32_t device, double* tflops) {
+  if (!tflops) return fail(nullptr, OD_ERR_INVALID, "tflops is NULL");
+  if (od_device_count() <= device || device < 0)
+    return fail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = od_run_fp32_probe(device, tflops);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "fp32 probe");
+  return OD_OK;
 }
 
 extern "C" int64_t od_step_index(const od_handle* h) { return h ? h->step : -1; }
@@ -449,8 +630,10 @@ extern "C" od_status od_force_snapshot(od_handle* h, const double* pos, int64_t 
   OD_CK(h, cudaSetDevice(h->device));
   od_status st = upload_snapshot(h, pos, n);
   if (st != OD_OK) return st;
-  OD_CK(h, od_launch_pairs(h->plan, h->snap_pos, h->Npad, h->b.part_hi, h->b.part_lo, h->hp.rho0,
-                           &h->ds->err, h->stream));
+  // the snapshot borrows the SoA source buffers; od_step rewrites them before its next use
+  OD_CK(h, od_launch_aos_to_soa(h->snap_pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
+  OD_CK(h, od_launch_pairs(h->plan, od_pair_io{h->snap_pos, h->b.sx, h->b.sy, h->b.sz}, h->Npad,
+                           h->b.part_hi, h->b.part_lo, h->hp.rho0, &h->ds->err, h->stream));
   OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->snap_hi,
                             h->snap_lo, h->stream));
   std::vector<float4> hi(n), lo(n);

@@ -10,7 +10,14 @@ struct od_pair_plan {
   int ipt;     // targets per thread
   int jsplit;  // source chunks (grid.y); partial slabs written per ion
   int chunk;   // sources per chunk (multiple of OD_TJ)
-  int variant; // 0: shared-memory broadcast, 1: warp-shuffle broadcast
+  int variant; // 0: shared-memory broadcast, 1: warp-shuffle broadcast, 2: packed f32x2 with
+               // SoA tiles (ipt 2), 3: as 2 with Newton reciprocals for half of the targets
+};
+
+// Position views the all-pairs kernels read: float4 AoS, and SoA slices for variants 2-3.
+struct od_pair_io {
+  const float4* pos;
+  const float *sx, *sy, *sz;
 };
 
 // Device buffers of one simulation.
@@ -24,16 +31,23 @@ struct od_dbufs {
   double* orbit_part;                   // [nb_corr][P][3]
   double *s_q, *s_orbit, *s_collect, *s_dust, *s_field;  // result series
   float* cq;                            // [P] A_id * q_param, FP32 copy for the ion kernels
+  float *sx, *sy, *sz;                  // [Npad] SoA copy of positions (all-pairs sources)
 };
 
 int od_num_sms(int device);
 
-cudaError_t od_launch_pairs(const od_pair_plan& pl, const float4* pos, int Npad, float4* part_hi,
+cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* part_hi,
                             float4* part_lo, float rho0, uint32_t* err, cudaStream_t s);
+cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,
+                                 cudaStream_t s);
 cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* part_hi,
                              const float4* part_lo, float4* fhi, float4* flo, cudaStream_t s);
 cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
                            int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s);
+cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                int N, int Npad, int P, const od_pair_plan& pl, float rho0, int nrec,
+                                cudaStream_t s);
+cudaError_t od_run_fp32_probe(int device, double* tflops);
 cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,
                                      uint32_t* flags, int32_t* list, int32_t* list_bits,
                                      double* counts, cudaStream_t s);

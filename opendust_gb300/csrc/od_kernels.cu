@@ -128,6 +128,193 @@ __global__ void __launch_bounds__(NT) k_pairs(const float4* __restrict__ pos, in
   }
 }
 
+// ------------------------------------------------------------------ packed f32x2 variant
+// Blackwell executes two FP32 lanes per instruction with the f32x2 forms of add/sub/mul/fma.
+// Sources are staged as SoA slices (x[], y[], z[]) so that one 128-bit shared load gives two
+// packed source pairs (x0,x1),(x2,x3). Each thread owns two targets; a packed operation then
+// evaluates two pairs in one issue slot. The SFU (rsqrt, rcp, ex2) stays scalar per pair.
+// NEWTON = 1: target 1 takes 1/s from two packed Newton steps seeded with 1/r (error
+// (r0/r)^4); when any lane of the warp saw r^2 < newton_r2 in the tile, the tile is redone
+// for target 1 with the SFU reciprocal.
+typedef unsigned long long od_u64;
+__device__ __forceinline__ od_u64 p2(float lo, float hi) {
+  od_u64 r; asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi)); return r;
+}
+__device__ __forceinline__ float2 up2(od_u64 v) {
+  float2 r; asm("mov.b64 {%0,%1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v)); return r;
+}
+__device__ __forceinline__ od_u64 fma2(od_u64 a, od_u64 b, od_u64 c) {
+  od_u64 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d;
+}
+__device__ __forceinline__ od_u64 add2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+__device__ __forceinline__ od_u64 sub2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+__device__ __forceinline__ od_u64 mul2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+
+struct od_pk {
+  od_u64 eps, rho, nrho, nl2e, one;
+};
+
+// two pair terms (target vs sources a and b), SFU reciprocal
+__device__ __forceinline__ void pair2_sfu(const od_pk& k, od_u64 X, od_u64 Y, od_u64 Z, od_u64 QX,
+                                          od_u64 QY, od_u64 QZ, od_u64& AX, od_u64& AY, od_u64& AZ) {
+  const od_u64 DX = sub2(X, QX), DY = sub2(Y, QY), DZ = sub2(Z, QZ);
+  od_u64 R2 = fma2(DX, DX, k.eps);
+  R2 = fma2(DY, DY, R2);
+  R2 = fma2(DZ, DZ, R2);
+  const float2 r2 = up2(R2);
+  const od_u64 RI = p2(od_rsqrt(r2.x), od_rsqrt(r2.y));
+  const od_u64 R = mul2(R2, RI);
+  const float2 s = up2(add2(R, k.rho));
+  const od_u64 SI = p2(od_rcp(s.x), od_rcp(s.y));
+  const float2 ea = up2(mul2(R, k.nl2e));
+  const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
+  const od_u64 C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
+  AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
+}
+// same with 1/s from Newton steps seeded with 1/r; tracks the smallest r^2 seen
+__device__ __forceinline__ void pair2_newton(const od_pk& k, od_u64 X, od_u64 Y, od_u64 Z, od_u64 QX,
+                                             od_u64 QY, od_u64 QZ, od_u64& AX, od_u64& AY,
+                                             od_u64& AZ, float& mr2) {
+  const od_u64 DX = sub2(X, QX), DY = sub2(Y, QY), DZ = sub2(Z, QZ);
+  od_u64 R2 = fma2(DX, DX, k.eps);
+  R2 = fma2(DY, DY, R2);
+  R2 = fma2(DZ, DZ, R2);
+  const float2 r2 = up2(R2);
+  mr2 = fminf(mr2, fminf(r2.x, r2.y));
+  const od_u64 RI = p2(od_rsqrt(r2.x), od_rsqrt(r2.y));
+  const od_u64 R = mul2(R2, RI);
+  const od_u64 NS = sub2(k.nrho, R);  // -(r + rho0)
+  od_u64 E = fma2(NS, RI, k.one);
+  od_u64 SI = fma2(RI, E, RI);
+  E = fma2(NS, SI, k.one);
+  SI = fma2(SI, E, SI);
+  const float2 ea = up2(mul2(R, k.nl2e));
+  const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
+  const od_u64 C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
+  AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
+}
+
+__device__ __forceinline__ float sum2(od_u64 v) {
+  const float2 f = up2(v);
+  return f.x + f.y;
+}
+
+template <int NT, int NEWTON>
+__global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
+                                                 const float* __restrict__ sy,
+                                                 const float* __restrict__ sz, int Npad, int chunk,
+                                                 float4* __restrict__ part_hi,
+                                                 float4* __restrict__ part_lo, float rho0,
+                                                 float newton_r2, uint32_t* __restrict__ err) {
+  __shared__ __align__(128) float tx[2][OD_TJ];
+  __shared__ __align__(128) float ty[2][OD_TJ];
+  __shared__ __align__(128) float tz[2][OD_TJ];
+  __shared__ __align__(8) uint64_t bar[2];
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * (2 * NT) + tid, i1 = i0 + NT;
+  const int j0 = blockIdx.y * chunk;
+  const int j1 = min(j0 + chunk, Npad);
+  const int ntiles = (j1 - j0) / OD_TJ;
+  const od_u64 X0 = p2(sx[i0], sx[i0]), Y0 = p2(sy[i0], sy[i0]), Z0 = p2(sz[i0], sz[i0]);
+  const od_u64 X1 = p2(sx[i1], sx[i1]), Y1 = p2(sy[i1], sy[i1]), Z1 = p2(sz[i1], sz[i1]);
+  od_pk k;
+  k.eps = p2(1e-30f, 1e-30f);
+  k.rho = p2(rho0, rho0);
+  k.nrho = p2(-rho0, -rho0);
+  k.nl2e = p2(OD_NLOG2E, OD_NLOG2E);
+  k.one = p2(1.0f, 1.0f);
+  float h0x = 0.f, h0y = 0.f, h0z = 0.f, l0x = 0.f, l0y = 0.f, l0z = 0.f;
+  float h1x = 0.f, h1y = 0.f, h1z = 0.f, l1x = 0.f, l1y = 0.f, l1z = 0.f;
+  if (tid == 0) {
+    od_mbar_init(&bar[0], 1);
+    od_mbar_init(&bar[1], 1);
+    od_fence_barrier_init();
+  }
+  __syncthreads();
+  constexpr uint32_t kBytes = OD_TJ * 4;
+  int issued = 0;
+  if (tid == 0) {
+    for (; issued < 2 && issued < ntiles; issued++) {
+      const int jb = j0 + issued * OD_TJ;
+      od_mbar_expect_tx(&bar[issued], 3 * kBytes);
+      od_bulk_g2s(tx[issued], sx + jb, kBytes, &bar[issued]);
+      od_bulk_g2s(ty[issued], sy + jb, kBytes, &bar[issued]);
+      od_bulk_g2s(tz[issued], sz + jb, kBytes, &bar[issued]);
+    }
+  }
+  bool ok = true;
+  int t = 0;
+  for (; t < ntiles; t++) {
+    const int s = t & 1;
+    ok = __syncthreads_and(od_mbar_wait(&bar[s], (t >> 1) & 1));
+    if (!ok) break;
+    od_u64 A0x = 0, A0y = 0, A0z = 0, A1x = 0, A1y = 0, A1z = 0;
+    float mr2 = 3.0e38f;
+#pragma unroll 2
+    for (int j = 0; j < OD_TJ; j += 4) {
+      const ulonglong2 qx = *reinterpret_cast<const ulonglong2*>(&tx[s][j]);
+      const ulonglong2 qy = *reinterpret_cast<const ulonglong2*>(&ty[s][j]);
+      const ulonglong2 qz = *reinterpret_cast<const ulonglong2*>(&tz[s][j]);
+      pair2_sfu(k, X0, Y0, Z0, qx.x, qy.x, qz.x, A0x, A0y, A0z);
+      pair2_sfu(k, X0, Y0, Z0, qx.y, qy.y, qz.y, A0x, A0y, A0z);
+      if (NEWTON) {
+        pair2_newton(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z, mr2);
+        pair2_newton(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z, mr2);
+      } else {
+        pair2_sfu(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z);
+        pair2_sfu(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z);
+      }
+    }
+    if (NEWTON && __any_sync(0xffffffffu, mr2 < newton_r2)) {
+      A1x = A1y = A1z = 0;
+      for (int j = 0; j < OD_TJ; j += 4) {
+        const ulonglong2 qx = *reinterpret_cast<const ulonglong2*>(&tx[s][j]);
+        const ulonglong2 qy = *reinterpret_cast<const ulonglong2*>(&ty[s][j]);
+        const ulonglong2 qz = *reinterpret_cast<const ulonglong2*>(&tz[s][j]);
+        pair2_sfu(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z);
+        pair2_sfu(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z);
+      }
+    }
+    od_acc2(h0x, l0x, sum2(A0x)); od_acc2(h0y, l0y, sum2(A0y)); od_acc2(h0z, l0z, sum2(A0z));
+    od_acc2(h1x, l1x, sum2(A1x)); od_acc2(h1y, l1y, sum2(A1y)); od_acc2(h1z, l1z, sum2(A1z));
+    __syncthreads();
+    if (tid == 0 && issued < ntiles) {
+      const int jb = j0 + issued * OD_TJ;
+      od_mbar_expect_tx(&bar[s], 3 * kBytes);
+      od_bulk_g2s(tx[s], sx + jb, kBytes, &bar[s]);
+      od_bulk_g2s(ty[s], sy + jb, kBytes, &bar[s]);
+      od_bulk_g2s(tz[s], sz + jb, kBytes, &bar[s]);
+      issued++;
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicOr(err, OD_DERR_TIMEOUT);
+      for (int u = t; u < issued; u++) od_mbar_wait(&bar[u & 1], (u >> 1) & 1);
+    }
+    return;
+  }
+  const size_t off = (size_t)blockIdx.y * Npad;
+  part_hi[off + i0] = make_float4(h0x, h0y, h0z, 0.f);
+  part_lo[off + i0] = make_float4(l0x, l0y, l0z, 0.f);
+  part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
+  part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+}
+
+__global__ void k_aos_to_soa(const float4* __restrict__ pos, int Npad, float* __restrict__ sx,
+                             float* __restrict__ sy, float* __restrict__ sz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Npad) return;
+  const float4 p = pos[i];
+  sx[i] = p.x; sy[i] = p.y; sz[i] = p.z;
+}
+
 // sum the jsplit partial slabs of ion i into (hi, lo)
 __device__ __forceinline__ void reduce_parts(const float4* __restrict__ ph,
                                              const float4* __restrict__ pl, int Npad, int jsplit,
@@ -192,7 +379,9 @@ __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restric
                                                      float4* __restrict__ vel,
                                                      const float4* __restrict__ fhi,
                                                      const float4* __restrict__ flo,
-                                                     const float* __restrict__ cq) {
+                                                     const float* __restrict__ cq,
+                                                     float* __restrict__ sx, float* __restrict__ sy,
+                                                     float* __restrict__ sz) {
   const od_dparams& p = *dp;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= p.N) return;
@@ -207,6 +396,7 @@ __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restric
   x.x += v.x; x.y += v.y; x.z += v.z;
   pos[i] = x;
   vel[i] = v;
+  sx[i] = x.x; sy[i] = x.y; sz[i] = x.z;
 }
 
 // ============================================================== K3: kick + flags
@@ -728,10 +918,19 @@ static void launch_pairs_t(const od_pair_plan& pl, const float4* pos, int Npad, 
   dim3 grid(Npad / (NT * IPT), pl.jsplit);
   k_pairs<NT, IPT, V><<<grid, NT, 0, s>>>(pos, Npad, pl.chunk, ph, plo, rho0, err);
 }
+template <int NT, int NEWTON>
+static void launch_pairs_x2(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
+                            float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
+  dim3 grid(Npad / (NT * 2), pl.jsplit);
+  const float nr = 64.0f * rho0;  // Newton (2 steps) keeps 1/s within 2^-24 for r > 64 r0
+  k_pairs_x2<NT, NEWTON><<<grid, NT, 0, s>>>(io.sx, io.sy, io.sz, Npad, pl.chunk, ph, plo, rho0,
+                                             nr * nr, err);
+}
 
-cudaError_t od_launch_pairs(const od_pair_plan& pl, const float4* pos, int Npad, float4* ph,
+cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
                             float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
   const int key = pl.nt * 100 + pl.ipt * 10 + pl.variant;
+  const float4* pos = io.pos;
   switch (key) {
     case 12810: launch_pairs_t<128, 1, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
     case 12820: launch_pairs_t<128, 2, 0>(pl, pos, Npad, ph, plo, rho0, err, s); break;
@@ -740,8 +939,18 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const float4* pos, int Npad,
     case 12811: launch_pairs_t<128, 1, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
     case 25611: launch_pairs_t<256, 1, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
     case 25621: launch_pairs_t<256, 2, 1>(pl, pos, Npad, ph, plo, rho0, err, s); break;
+    case 12822: launch_pairs_x2<128, 0>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 25622: launch_pairs_x2<256, 0>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 12823: launch_pairs_x2<128, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 25623: launch_pairs_x2<256, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,
+                                 cudaStream_t s) {
+  k_aos_to_soa<<<(Npad + kBlk - 1) / kBlk, kBlk, 0, s>>>(pos, Npad, sx, sy, sz);
   return cudaGetLastError();
 }
 
@@ -752,13 +961,20 @@ cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const f
   return cudaGetLastError();
 }
 
-cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
-                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s) {
+// part 0: K1 (kick/drift); part 1: K2 (all pairs); part 2: K3..K6
+cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                int N, int Npad, int P, const od_pair_plan& pl, float rho0, int nrec,
+                                cudaStream_t s) {
   (void)P;
   const int nb = Npad / kBlk;
-  k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq);
-  cudaError_t e = od_launch_pairs(pl, b.pos, Npad, b.part_hi, b.part_lo, rho0, &ds->err, s);
-  if (e != cudaSuccess) return e;
+  if (part == 0) {
+    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq,
+                                                        b.sx, b.sy, b.sz);
+    return cudaGetLastError();
+  }
+  if (part == 1)
+    return od_launch_pairs(pl, od_pair_io{b.pos, b.sx, b.sy, b.sz}, Npad, b.part_hi, b.part_lo,
+                           rho0, &ds->err, s);
   k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, pl.jsplit, b.fhi, b.flo,
                                   b.flags, b.cq);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
@@ -768,6 +984,52 @@ cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& 
   k_tail<<<1, kBlk, 0, s>>>(dp, ds, b.orbit_part, nb, b.s_q, b.s_orbit, b.s_collect, b.s_dust,
                            b.s_field, b.cq);
   return cudaGetLastError();
+}
+
+cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
+                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s) {
+  for (int part = 0; part < 3; part++) {
+    cudaError_t e = od_launch_step_part(part, dp, ds, b, N, Npad, P, pl, rho0, nrec, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread, 8 blocks of 256 per SM.
+__global__ void k_ffma_probe(float* out, float a, float b, int iters) {
+  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+        x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t od_run_fp32_probe(int device, double* tflops) {
+  const int blocks = od_num_sms(device) * 8, threads = 256, iters = 1 << 14;
+  float* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(float) * blocks * threads);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int r = 0; r < 6; r++) {
+    cudaEventRecord(e0);
+    k_ffma_probe<<<blocks, threads>>>(out, 0.999f, 0.001f, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r >= 2 && ms < best) best = ms;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+  return e;
 }
 
 cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,

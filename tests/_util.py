@@ -16,10 +16,13 @@ def oracle_trap(n_points_cap: int = 200_000):
     return f
 
 
-def case(N=2048, n=16, seed=3, trap=None, builder=workloads.small_plain, state_seed=None, **kw):
-    """(holder, pos, vel, plasma, sim, grains) for a small seeded case."""
-    plasma, sim, grains, dist, ext = builder(N=N, n=n) if builder is not workloads.field_chain \
-        else builder(N=N, n=n)
+def case(N=2048, n=16, seed=3, trap=None, builder=workloads.small_plain, state_seed=None, q0=-2e-15,
+         **kw):
+    """(holder, pos, vel, plasma, sim, grains) for a small seeded case; grains start at charge q0
+    (non-zero, so that the orbit force of the first step is non-zero)."""
+    plasma, sim, grains, dist, ext = builder(N=N, n=n)
+    for g in grains:
+        g.q = q0
     ext = {**ext, **kw}
     holder, info = build_simulation(plasma, sim, grains, dist, seed=seed, trap=trap, **ext)
     pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],

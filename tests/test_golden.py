@@ -1,0 +1,60 @@
+"""Statistical parity with the reference's own published runs (tests/golden/).
+
+The reference's example scripts print time-averaged grain forces (examples/Piel2017/...);
+tests/golden/make_golden.py copied those numbers, with the run parameters, into
+reference_examples.json. The GPU test re-runs a subset through the drop-in Python API
+(OpenDust.simulate) with the same parameters and compares the same averages. The reference
+runs are single unseeded Monte-Carlo runs, so the comparison is statistical: the tolerance
+below is set from the spread of seeded runs of this engine.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+RUNS = {r["name"]: r for r in json.load(open(os.path.join(HERE, "golden", "reference_examples.json")))["runs"]}
+
+
+def test_golden_fixture_consistent():
+    from opendust_gb300 import PlasmaParametersInSIUnitsMaxwell, SimulationParametersInSIUnits
+
+    assert len(RUNS) == 15
+    r = RUNS["piel2017_fig5_M2.0"]
+    p = PlasmaParametersInSIUnitsMaxwell(r["T_i"], r["T_e"], r["n_inf"], r["M"], r["m_i"])
+    s = SimulationParametersInSIUnits(3 * p.r_D_e, 6 * p.r_D_e, r["N"], r["n"], r["d_t"], p)
+    # N_s printed by the reference run (examples/Piel2017/Figure5/outputPiel2017Fig5)
+    assert s.N_s == pytest.approx(420.3631132989799, rel=1e-12)
+    for run in RUNS.values():
+        assert run["F_orbit_z"] > 0
+
+
+def run_example(r, seed):
+    from opendust_gb300 import (DustParticle, OpenDust, OutputParameters,
+                                PlasmaParametersInSIUnitsMaxwell, SimulationParametersInSIUnits)
+
+    p = PlasmaParametersInSIUnitsMaxwell(r["T_i"], r["T_e"], r["n_inf"], r["M"], r["m_i"])
+    s = SimulationParametersInSIUnits(r["R_lambda"] * p.r_D_e, r["H_lambda"] * p.r_D_e, r["N"], r["n"],
+                                      r["d_t"], p)
+    g = DustParticle(0, 0, r["grain_z_lambda"] * p.r_D_e, r["grain_r"], r["method"], r["q0_e"] * p.e)
+    od = OpenDust(p, s, OutputParameters(nOutput=10**9, nFileOutput=10**9), [g], "Maxwellian")
+    od.simulate("0", seed=seed, quiet=True)
+    k = r["avg_after"]
+    d = od.dustParticles[0]
+    return d.forceIonsOrbit[k + 1:, 2].mean(), d.forceIonsCollect[k + 1:, 2].mean()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["piel2017_fig1_consistent", "piel2017_fig1_oml",
+                                  "piel2017_fig5_M0.49799", "piel2017_fig5_M0.99598",
+                                  "piel2017_fig5_M2.0"])
+def test_reference_example(gpu_lib, name):
+    r = RUNS[name]
+    orb, col = run_example(r, seed=1)
+    d_orb = (orb - r["F_orbit_z"]) / r["F_orbit_z"]
+    d_col = (col - r["F_collect_z"]) / r["F_orbit_z"]
+    print(f"{name}: F_orbit {orb:.4e} (ref {r['F_orbit_z']:.4e}, {100 * d_orb:+.1f}%), "
+          f"F_collect {col:.4e} (ref {r['F_collect_z']:.4e}, {100 * d_col:+.1f}% of F_orbit)")
+    assert abs(d_orb) < 0.10
+    assert abs(d_col) < 0.10

@@ -18,22 +18,29 @@ from tests._util import case, plant_close_pairs, rel_err_per_ion
 pytestmark = pytest.mark.gpu
 
 
-def test_force_snapshot_all_targets(gpu_lib):
+PLANS = [(256, 1, 0), (128, 2, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3)]
+
+
+@pytest.mark.parametrize("plan", PLANS)
+def test_force_snapshot_all_targets(gpu_lib, plan):
     holder, pos, vel, plasma, sim, grains = case(N=4096, n=4, seed=11)
     rng = np.random.default_rng(5)
-    pos = plant_close_pairs(pos, plasma.r_D_e, rng)
+    pos = plant_close_pairs(pos, plasma.r_D_e, rng, n_pairs=64, dmin=2e-4)
     with _lib.Engine(holder) as eng:
+        eng.set_pair_plan(*plan)
         f = eng.force_snapshot(pos)
     ref = oracle.force_snapshot(holder, pos, round32=True)
     err = rel_err_per_ion(f, ref)
-    print(f"N=4096 per-ion rel err: max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
+    print(f"plan {plan} N=4096 per-ion rel err: max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
     assert err.max() <= 1e-5
 
 
-@pytest.mark.parametrize("N", [2**18, 2**20])
-def test_force_snapshot_large(gpu_lib, N):
+@pytest.mark.parametrize("N,plan", [(2**18, None), (2**20, None), (2**20, (256, 2, 3))])
+def test_force_snapshot_large(gpu_lib, N, plan):
     holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=12)
     with _lib.Engine(holder) as eng:
+        if plan:
+            eng.set_pair_plan(*plan)
         f = eng.force_snapshot(pos)
     rng = np.random.default_rng(1)
     idx = np.sort(rng.choice(N, 1024 if N > 2**18 else 2048, replace=False))
