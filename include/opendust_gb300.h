@@ -231,6 +231,23 @@ od_status od_collect_flags(od_handle* h, const double* pos, int64_t n, int64_t* 
 od_status od_trap_potential(double R_over_lambda, double H_over_lambda, int32_t n_r, int32_t n_h,
                             int64_t n_points, uint64_t seed, int32_t device, double* pot);
 
+/* Ion–ion forces for callers that cannot allocate device memory (no counterpart in the
+ * reference). Plug-ins that live inside another runtime's allocator, loops that forbid
+ * cudaMalloc after start-up, or frameworks that own every device buffer can still evaluate
+ * the screened ion–ion force of opendust.py:472: the caller passes device arrays pos_dev
+ * (n x 3 doubles, metres) and force_dev (n x 3 doubles, newtons, written), the Debye length
+ * r_D_e, the softening r_0 and the prefactor kq_sq_s = k q_s^2 (J m, the reference's
+ * "kq_sq_s" parameter). The call allocates and frees nothing: its scratch (positions in
+ * device units, partial sums, an error word) is one file-scope device array of about 8.8 MB
+ * that every GPU which loads this library holds until the process exits; it limits n to
+ * 2..32768 (larger n returns OD_ERR_INVALID). The call runs on the calling thread's current
+ * device and on `stream` (a cudaStream_t, NULL for the default stream) and returns after the
+ * stream has finished it. The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture. All calls share
+ * the array: calls that overlap on the GPU (other streams, other host threads) race. */
+od_status od_ion_forces_static(const double* pos_dev, int64_t n, double r_D_e, double r_0,
+                               double kq_sq_s, double* force_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -139,6 +139,8 @@ def load(path: str | None = None):
         "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
         "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
         "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
+        "od_ion_forces_static": (c_int32, [c_void_p, c_int64, c_double, c_double, c_double, c_void_p,
+                                           c_void_p]),
         "od_trap_potential": (
             c_int32,
             [c_double, c_double, c_int32, c_int32, c_int64, c_uint64, c_int32, _DP],

@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 #include "od_internal.h"
@@ -714,5 +715,79 @@ extern "C" od_status od_trap_potential(double Rh, double Hh, int32_t n_r, int32_
     for (int c = 0; c < nchunks; c++) s += hpart[(size_t)c * nn + i];
     pot[i] = s / (double)n_points;
   }
+  return OD_OK;
+}
+
+// ============================================================== allocation-free ion–ion forces
+// Some callers cannot create device allocations at the moment they need forces: code that runs
+// inside another runtime's memory pool or allocator callbacks, real-time loops that forbid
+// cudaMalloc after start-up, or plug-ins whose host framework owns every device buffer and
+// hands them only pointers. od_ion_forces_static serves them: the caller passes device
+// arrays for the positions and the forces, and every scratch byte the kernels need (a padded
+// SoA copy of the positions, the partial sums of the source split, and an error word) lives
+// in the file-scope array below, which each GPU that loads this library holds until the
+// process exits.
+#define OD_STATIC_MAX_IONS 32768
+#define OD_STATIC_MAX_SPLIT 8
+static constexpr size_t kStaticSoA = (size_t)OD_STATIC_MAX_IONS * sizeof(float);
+static constexpr size_t kStaticSlab = (size_t)OD_STATIC_MAX_SPLIT * OD_STATIC_MAX_IONS * sizeof(float4);
+static constexpr size_t kStaticBytes = 256 + 3 * kStaticSoA + 2 * kStaticSlab;  // about 8.8 MB
+static __device__ __align__(256) unsigned char od_static_scratch[kStaticBytes];
+
+// Device address of od_static_scratch on each device. In host code the array's name is only a
+// host-side stand-in, so its device address is looked up once per device, with that device
+// current, on the first call made on it.
+static std::mutex g_static_mu;
+static void* g_static_addr[64];
+
+static cudaError_t static_scratch_addr(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, od_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_static_addr[dev];
+  return cudaSuccess;
+}
+
+extern "C" od_status od_ion_forces_static(const double* pos_dev, int64_t n, double r_D_e,
+                                          double r_0, double kq_sq_s, double* force_dev,
+                                          void* stream) {
+  if (!pos_dev || !force_dev) return fail(nullptr, OD_ERR_INVALID, "pos_dev/force_dev is NULL");
+  if (n < 2 || n > OD_STATIC_MAX_IONS)
+    return fail(nullptr, OD_ERR_INVALID,
+                "od_ion_forces_static takes 2 to 32768 ions (its scratch array is sized for "
+                "32768); use od_force_snapshot for larger systems");
+  if (!(r_D_e > 0) || !(r_0 >= 0))
+    return fail(nullptr, OD_ERR_INVALID, "r_D_e must be positive and r_0 non-negative");
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");
+  unsigned char* base = nullptr;
+  e = static_scratch_addr(dev, &base);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetSymbolAddress(od_static_scratch)");
+  od_static_view v{};
+  v.err = (uint32_t*)base;
+  v.sx = (float*)(base + 256);
+  v.sy = (float*)(base + 256 + kStaticSoA);
+  v.sz = (float*)(base + 256 + 2 * kStaticSoA);
+  v.part_hi = (float4*)(base + 256 + 3 * kStaticSoA);
+  v.part_lo = (float4*)(base + 256 + 3 * kStaticSoA + kStaticSlab);
+  v.max_split = OD_STATIC_MAX_SPLIT;
+  cudaStream_t s = (cudaStream_t)stream;
+  // the error word keeps the previous call's value: clear it
+  e = cudaMemsetAsync(v.err, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemsetAsync(error word)");
+  const double scale = kq_sq_s / (r_D_e * r_D_e);
+  e = od_launch_static_forces(v, pos_dev, (int)n, r_D_e, r_0, scale, force_dev, s);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "all-pairs launch");
+  uint32_t err = 0;
+  e = cudaMemcpyAsync(&err, v.err, sizeof(err), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "od_ion_forces_static");
+  if (err & OD_DERR_TIMEOUT) return fail(nullptr, OD_ERR_TIMEOUT, "a bounded device wait ran out");
   return OD_OK;
 }

@@ -36,6 +36,16 @@ struct od_dbufs {
 
 int od_num_sms(int device);
 
+// Pointers into the allocation-free scratch array of od_ion_forces_static.
+struct od_static_view {
+  uint32_t* err;
+  float *sx, *sy, *sz;
+  float4 *part_hi, *part_lo;
+  int max_split;
+};
+cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, int n, double lam,
+                                    double r0, double scale, double* force, cudaStream_t s);
+
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* part_hi,
                             float4* part_lo, float rho0, uint32_t* err, cudaStream_t s);
 cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,

@@ -1055,3 +1055,52 @@ cudaError_t od_launch_trap(double Rh, double Hh, int n_r, int n_h, int64_t n_poi
                                (uint32_t)(seed >> 32), part);
   return cudaGetLastError();
 }
+
+// ============================================================== scratch-array variant
+// Kernels behind od_ion_forces_static: the same packed all-pairs kernel, reading positions
+// and writing partial sums in a caller-independent scratch region (see od_api.cu).
+namespace {
+__global__ void k_static_pack(const double* __restrict__ pos, int n, int Npad, double inv_lam,
+                              float* __restrict__ sx, float* __restrict__ sy,
+                              float* __restrict__ sz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Npad) return;
+  if (i < n) {
+    sx[i] = (float)(pos[3 * i] * inv_lam);
+    sy[i] = (float)(pos[3 * i + 1] * inv_lam);
+    sz[i] = (float)(pos[3 * i + 2] * inv_lam);
+  } else {
+    sx[i] = OD_SENTINEL; sy[i] = OD_SENTINEL; sz[i] = OD_SENTINEL;
+  }
+}
+
+__global__ void k_static_finish(const float4* __restrict__ ph, const float4* __restrict__ pl,
+                                int n, int Npad, int jsplit, double scale,
+                                double* __restrict__ force) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 hi, lo;
+  reduce_parts(ph, pl, Npad, jsplit, i, hi, lo);
+  force[3 * i] = scale * ((double)hi.x + (double)lo.x);
+  force[3 * i + 1] = scale * ((double)hi.y + (double)lo.y);
+  force[3 * i + 2] = scale * ((double)hi.z + (double)lo.z);
+}
+}  // namespace
+
+cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, int n, double lam,
+                                    double r0, double scale, double* force, cudaStream_t s) {
+  const int Npad = ((n + OD_PAD - 1) / OD_PAD) * OD_PAD;
+  int jsplit = v.max_split < Npad / OD_TJ ? v.max_split : Npad / OD_TJ;
+  int chunk = (Npad + jsplit - 1) / jsplit;
+  chunk = ((chunk + OD_TJ - 1) / OD_TJ) * OD_TJ;
+  jsplit = (Npad + chunk - 1) / chunk;
+  k_static_pack<<<(Npad + kBlk - 1) / kBlk, kBlk, 0, s>>>(pos, n, Npad, 1.0 / lam, v.sx, v.sy, v.sz);
+  const float rho0 = (float)(r0 / lam);
+  const float nr = 64.0f * rho0;
+  dim3 grid(Npad / 512, jsplit);
+  k_pairs_x2<256, 0><<<grid, 256, 0, s>>>(v.sx, v.sy, v.sz, Npad, chunk, v.part_hi, v.part_lo,
+                                          rho0, nr * nr, v.err);
+  k_static_finish<<<(n + kBlk - 1) / kBlk, kBlk, 0, s>>>(v.part_hi, v.part_lo, n, Npad, jsplit,
+                                                        scale, force);
+  return cudaGetLastError();
+}
