@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="full_plain", choices=["full_plain", "small_plain"])
+    ap.add_argument("--workload", default="full_plain", choices=["full_plain", "small_plain", "field_chain"])
     ap.add_argument("--cpu-sample-targets", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -133,6 +133,8 @@ def workload(name: str, n_total: int):
 
     if name == "full_plain":
         return workloads.full_plain(n=n_total)
+    if name == "field_chain":
+        return workloads.field_chain(n=n_total)
     return workloads.small_plain(n=n_total)
 
 
@@ -140,11 +142,20 @@ def describe(name, sim, ext):
     w = {"full_plain": "Ar+ Mach 1 flow past one grain (r=10 um, consistent charging), "
                        "N=2^20 superions, all-pairs Yukawa, charge-exchange mfp 2 lambda, d_t=1e-10 s",
          "small_plain": "Ar+ Mach 1 flow past one grain, N=16384, all-pairs Yukawa, no collisions, "
-                        "d_t=1e-10 s"}[name]
-    return {"workload": f"{name}: {w}", "n_ions": int(sim.N), "grains": 1,
-            "force": "all-pairs", "collisions": ext.get("collisions", "none"),
+                        "d_t=1e-10 s",
+         "field_chain": "field-driven Ar+ (Mach 0.5, charge-exchange mfp 1 lambda) past a chain of 5 "
+                        "grains (r=5 um, 1 lambda apart), N=2^19, cutoff 2 lambda over a device cell "
+                        "list, d_t=1e-10 s"}[name]
+    cut = "cutoff_distance" in ext
+    return {"workload": f"{name}: {w}", "n_ions": int(sim.N), "grains": len(sim_grains(name)),
+            "force": "cutoff over cell list" if cut else "all-pairs",
+            "collisions": ext.get("collisions", "none"),
             "l2": "flushed (512 MB write) before every timed step",
-            "steps_in_workload": {"full_plain": 20000, "small_plain": 2000}[name]}
+            "steps_in_workload": {"full_plain": 20000, "small_plain": 2000, "field_chain": 30000}[name]}
+
+
+def sim_grains(name):
+    return [0] * (5 if name == "field_chain" else 1)
 
 
 def cpu_sample(holder, pos, targets: int, repeats: int = 2):
@@ -209,14 +220,13 @@ def run_reference(args, dist: Dist):
 
 
 def load_traffic(n_ions: int):
-    """DRAM bytes per all-pairs launch from the committed ncu summary, scaled to n_ions."""
+    """DRAM bytes per all-pairs launch from the committed ncu capture of the same size."""
     path = os.path.join(ROOT, "profiles", "allpairs_traffic.json")
     try:
         d = json.load(open(path))
     except (OSError, ValueError):
         return None
-    per_ion = d.get("dram_bytes_per_launch_per_ion")
-    return None if per_ion is None else per_ion * n_ions
+    return d.get("dram_bytes_per_launch") if d.get("n_ions") == n_ions else None
 
 
 def run_ours(args, dist: Dist):
@@ -254,12 +264,15 @@ def run_ours(args, dist: Dist):
     clk = clocks.stop()
     dist.barrier()
     step_ms, nsteps, pair_ms, pair_launches = eng.timing()
+    cut_pairs = eng.cutoff_pairs()
     eng.set_timing(False)
     t_max = dist.reduce(step_ms, "max")
     ions_all = dist.reduce(float(N * K), "sum")
     value = ions_all / (t_max * 1e-3)
     pair_avg_s = pair_ms / pair_launches * 1e-3
-    achieved = N * (N - 1) * FLOPS_PER_PAIR / pair_avg_s / 1e12
+    cutoff = cut_pairs > 0
+    pairs_per_launch = cut_pairs / pair_launches if cutoff else N * (N - 1)
+    achieved = pairs_per_launch * FLOPS_PER_PAIR / pair_avg_s / 1e12
     traffic = load_traffic(N)
 
     # e2e through the C ABI with host buffers (the calls simulate() makes)
@@ -297,10 +310,11 @@ def run_ours(args, dist: Dist):
             "data": "synthetic (seeded initial state and Philox streams)",
             "config": {**describe(args.workload, sim, ext),
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
-            "pair_interactions_per_s": value * (N - 1),
+            "pair_interactions_per_s": (pairs_per_launch * K * dist.world / (t_max * 1e-3)),
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_pairs (all-pairs ion-ion)",
+                         "frac": achieved / peak, "traffic": None if cutoff else traffic,
+                         "kernel": ("cell-list build + k_pairs_cut (pairs inside the cutoff)" if cutoff
+                                    else "k_pairs_x2 (all-pairs ion-ion)"),
                          "peak_source": "FP32 FMA probe measured on this GPU in this run",
                          "flops_per_pair": FLOPS_PER_PAIR, "pair_ms_avg": pair_avg_s * 1e3},
             "e2e": {"value": e2e_value, "unit": "ion-steps/s", "h2d_bytes_per_step": h2d // K_e2e,

@@ -177,6 +177,9 @@ od_status od_step(od_handle* h, int64_t nsteps);
 od_status od_set_timing(od_handle* h, int32_t enable);
 od_status od_get_timing(od_handle* h, double* step_ms, int64_t* steps, double* pair_ms,
                         int64_t* pair_launches);
+/* Pairs inside the cutoff evaluated by the cutoff force kernel while timing was enabled
+ * (0 for the all-pairs method). */
+od_status od_get_cutoff_pairs(od_handle* h, int64_t* pairs);
 /* Use (1, default) or bypass (0) the CUDA-graph replay of a step. */
 od_status od_set_graph(od_handle* h, int32_t enable);
 /* Work decomposition of the all-pairs force kernel (OpenMM picks its own nonbonded

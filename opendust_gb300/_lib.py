@@ -136,6 +136,7 @@ def load(path: str | None = None):
         "od_set_timing": (c_int32, [H, c_int32]),
         "od_get_timing": (c_int32, [H, _DP, POINTER(c_int64), _DP, POINTER(c_int64)]),
         "od_set_graph": (c_int32, [H, c_int32]),
+        "od_get_cutoff_pairs": (c_int32, [H, POINTER(c_int64)]),
         "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
         "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
         "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
@@ -333,6 +334,12 @@ class Engine:
         a = (c_int32 * 5)()
         check(self._lib.od_get_pair_plan(self.h, a), self.h)
         return dict(zip(("threads", "targets_per_thread", "variant", "jsplit", "chunk"), list(a)))
+
+    def cutoff_pairs(self) -> int:
+        """Pairs inside the cutoff evaluated while timing was enabled."""
+        v = c_int64()
+        check(self._lib.od_get_cutoff_pairs(self.h, ctypes.byref(v)), self.h)
+        return v.value
 
     def set_graph(self, enable: bool = True):
         check(self._lib.od_set_graph(self.h, int(bool(enable))), self.h)

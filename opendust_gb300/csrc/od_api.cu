@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -27,6 +28,10 @@ struct od_handle {
   int64_t step = 0;
   bool state_set = false;
   od_pair_plan plan{};
+  // cutoff path (force_method == OD_FORCE_CUTOFF)
+  bool has_cut = false;
+  od_cutlist cut{};
+  unsigned long long* d_pairs = nullptr;  // pairs inside the cutoff, counted in timing mode
   // snapshot scratch (allocated on first use)
   float4 *snap_pos = nullptr, *snap_hi = nullptr, *snap_lo = nullptr;
   double* snap_counts = nullptr;
@@ -80,6 +85,18 @@ static void split2(double d, float& hi, float& lo) {
   hi = (float)d;
   lo = (float)(d - (double)hi);
 }
+
+static od_force_ctx force_ctx(const od_handle* h, bool count_pairs) {
+  od_force_ctx fc{};
+  fc.plan = h->plan;
+  fc.cut = h->has_cut ? &h->cut : nullptr;
+  fc.rho0 = h->hp.rho0;
+  fc.rc = h->hp.rc;
+  fc.rs = h->hp.rs;
+  fc.pair_count = (count_pairs && h->has_cut) ? h->d_pairs : nullptr;
+  return fc;
+}
+static int force_jsplit(const od_handle* h) { return h->has_cut ? 1 : h->plan.jsplit; }
 
 static od_status validate(const od_config* c) {
   if (!c) return fail(nullptr, OD_ERR_INVALID, "config is NULL");
@@ -231,7 +248,9 @@ static void free_all(od_handle* h) {
                   h->b.flags, h->b.list, h->b.list_bits, h->b.list_old, h->b.list_new, h->b.list_v,
                   h->b.orbit_part, h->b.s_q, h->b.s_orbit, h->b.s_collect, h->b.s_dust,
                   h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
-                  h->b.sx, h->b.sy, h->b.sz};
+                  h->b.sx, h->b.sy, h->b.sz, h->cut.cell_of, h->cut.count, h->cut.fill,
+                  h->cut.start, h->cut.chunk_prefix, h->cut.perm, h->cut.ox, h->cut.oy, h->cut.oz,
+                  h->cut.stencil, h->d_pairs};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -300,6 +319,46 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
   OD_CKC(dalloc(&h->b.sy, Np));
   OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
+  if (cfg->force_method == OD_FORCE_CUTOFF) {
+    // cells of side rc/k: k = 4 unless that leaves more than ~800 ions per cell on average
+    const double rc = h->hp.rc, Rh = h->hp.Rh, Hh = h->hp.Hh;
+    const double dens = cfg->n_ions / (OD_PI_D * Rh * Rh * Hh);
+    int kk = 4;
+    while (kk < 8 && dens * pow(rc / kk, 3) > 800.0) kk++;
+    const double c = rc / kk;
+    od_cellgeom& g = h->cut.g;
+    g.c = (float)c;
+    g.inv_c = (float)(1.0 / c);
+    g.lox = g.loy = (float)(-Rh - c);
+    g.loz = (float)(-Hh / 2 - c);
+    g.gx = g.gy = (int)ceil((2 * Rh + 2 * c) / c);
+    g.gz = (int)ceil((Hh + 2 * c) / c);
+    g.ncells = g.gx * g.gy * g.gz;
+    std::vector<int4> st;
+    for (int dz = -kk - 1; dz <= kk + 1; dz++)
+      for (int dy = -kk - 1; dy <= kk + 1; dy++)
+        for (int dx = -kk - 1; dx <= kk + 1; dx++) {
+          auto m = [&](int d) { double v = std::max(std::abs(d) - 1, 0) * c; return v * v; };
+          if (m(dx) + m(dy) + m(dz) < rc * rc) st.push_back(make_int4(dx, dy, dz, 0));
+        }
+    h->cut.nstencil = (int)st.size();
+    h->cut.cap = h->Npad + 8 * g.ncells;
+    const size_t nc = g.ncells;
+    OD_CKC(dalloc(&h->cut.cell_of, Np));
+    OD_CKC(dalloc(&h->cut.count, nc));
+    OD_CKC(dalloc(&h->cut.fill, nc));
+    OD_CKC(dalloc(&h->cut.start, nc + 1));
+    OD_CKC(dalloc(&h->cut.chunk_prefix, nc + 1));
+    OD_CKC(dalloc(&h->cut.perm, h->cut.cap));
+    OD_CKC(dalloc(&h->cut.ox, h->cut.cap));
+    OD_CKC(dalloc(&h->cut.oy, h->cut.cap));
+    OD_CKC(dalloc(&h->cut.oz, h->cut.cap));
+    OD_CKC(dalloc(&h->cut.stencil, st.size()));
+    OD_CKC(dalloc(&h->d_pairs, 1));
+    OD_CKC(cudaMemcpy(h->cut.stencil, st.data(), sizeof(int4) * st.size(), cudaMemcpyHostToDevice));
+    OD_CKC(cudaMemset(h->d_pairs, 0, sizeof(unsigned long long)));
+    h->has_cut = true;
+  }
   OD_CKC(cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
   od_dstate s0{};
   for (int g = 0; g < h->P; g++) s0.q_param[g] = cfg->grain_q0[g];
@@ -350,6 +409,8 @@ static od_status check_device_err(od_handle* h) {
   OD_CK(h, cudaMemcpyAsync(&s, h->ds, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
   OD_CK(h, cudaStreamSynchronize(h->stream));
   if (s.err & OD_DERR_TIMEOUT) return fail(h, OD_ERR_TIMEOUT, "a bounded device wait ran out");
+  if (s.err & OD_DERR_CELL)
+    return fail(h, OD_ERR_CAPACITY, "a cutoff cell holds more than 4096 ions (density too high)");
   if (s.err) return fail(h, OD_ERR_STATE, "device error word set");
   return OD_OK;
 }
@@ -358,9 +419,10 @@ static od_status check_device_err(od_handle* h) {
 static od_status refresh_forces(od_handle* h) {
   const float rho0 = h->hp.rho0;
   OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
-  OD_CK(h, od_launch_pairs(h->plan, od_pair_io{h->b.pos, h->b.sx, h->b.sy, h->b.sz}, h->Npad,
-                           h->b.part_hi, h->b.part_lo, rho0, &h->ds->err, h->stream));
-  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->b.fhi,
+  (void)rho0;
+  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->b.pos, h->b.sx, h->b.sy, h->b.sz}, h->N,
+                           h->Npad, h->b.part_hi, h->b.part_lo, &h->ds->err, h->stream));
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, force_jsplit(h), h->b.part_hi, h->b.part_lo, h->b.fhi,
                             h->b.flo, h->stream));
   return OD_OK;
 }
@@ -369,8 +431,6 @@ extern "C" od_status od_set_state(od_handle* h, const double* pos, const double*
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!pos || !vel) return fail(h, OD_ERR_INVALID, "pos/vel is NULL");
   if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
-  if (h->cfg.force_method != OD_FORCE_ALLPAIRS)
-    return fail(h, OD_ERR_UNSUPPORTED, "cutoff force method is not built into this library yet");
   OD_CK(h, cudaSetDevice(h->device));
   std::vector<float4> xp, vp;
   to_device_units(h, pos, vel, n, xp, &vp);
@@ -413,6 +473,7 @@ static od_status event_at(od_handle* h, size_t slot, int* idx) {
 // launch (timing mode).
 static od_status step_timed(od_handle* h, int64_t nsteps) {
   size_t slot = 0;
+  const od_force_ctx fc = force_ctx(h, true);
   h->ev_step.clear();
   h->ev_pair.clear();
   for (int64_t s = 0; s < nsteps; s++) {
@@ -422,14 +483,14 @@ static od_status step_timed(od_handle* h, int64_t nsteps) {
       return OD_ERR_CUDA;
     OD_CK(h, cudaEventRecord(h->ev_pool[a], h->stream));
     const int nb = h->Npad / 256;
-    OD_CK(h, od_launch_step_part(0, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
-                                 h->nrec, h->stream));
+    OD_CK(h, od_launch_step_part(0, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
+                                 h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[c], h->stream));
-    OD_CK(h, od_launch_step_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
-                                 h->nrec, h->stream));
+    OD_CK(h, od_launch_step_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
+                                 h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[d], h->stream));
-    OD_CK(h, od_launch_step_part(2, h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
-                                 h->nrec, h->stream));
+    OD_CK(h, od_launch_step_part(2, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
+                                 h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[b], h->stream));
     (void)nb;
     h->ev_step.push_back({a, b});
@@ -454,7 +515,7 @@ static od_status step_timed(od_handle* h, int64_t nsteps) {
 static od_status ensure_graph(od_handle* h) {
   if (h->graph_exec) return OD_OK;
   OD_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
+  cudaError_t e = od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, force_ctx(h, false),
                                  h->nrec, h->stream);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
@@ -481,8 +542,8 @@ extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
     for (int64_t s = 0; s < nsteps; s++) OD_CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
   } else {
     for (int64_t s = 0; s < nsteps; s++)
-      OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, h->plan, h->hp.rho0,
-                              h->nrec, h->stream));
+      OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, force_ctx(h, false), h->nrec,
+                              h->stream));
   }
   h->step += nsteps;
   return check_device_err(h);
@@ -493,6 +554,18 @@ extern "C" od_status od_set_timing(od_handle* h, int32_t enable) {
   h->timing = enable != 0;
   h->t_step_ms = h->t_pair_ms = 0;
   h->t_steps = h->t_pair_launches = 0;
+  if (h->d_pairs) OD_CK(h, cudaMemsetAsync(h->d_pairs, 0, sizeof(unsigned long long), h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_get_cutoff_pairs(od_handle* h, int64_t* pairs) {
+  if (!h || !pairs) return fail(h, OD_ERR_INVALID, "NULL argument");
+  unsigned long long v = 0;
+  if (h->d_pairs) {
+    OD_CK(h, cudaMemcpyAsync(&v, h->d_pairs, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    OD_CK(h, cudaStreamSynchronize(h->stream));
+  }
+  *pairs = (int64_t)v;
   return OD_OK;
 }
 
@@ -626,16 +699,14 @@ extern "C" od_status od_force_snapshot(od_handle* h, const double* pos, int64_t 
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!pos || !force) return fail(h, OD_ERR_INVALID, "NULL argument");
   if (n < 1 || n > h->N) return fail(h, OD_ERR_INVALID, "n must be in [1, n_ions]");
-  if (h->cfg.force_method != OD_FORCE_ALLPAIRS)
-    return fail(h, OD_ERR_UNSUPPORTED, "cutoff force method is not built into this library yet");
   OD_CK(h, cudaSetDevice(h->device));
   od_status st = upload_snapshot(h, pos, n);
   if (st != OD_OK) return st;
   // the snapshot borrows the SoA source buffers; od_step rewrites them before its next use
   OD_CK(h, od_launch_aos_to_soa(h->snap_pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
-  OD_CK(h, od_launch_pairs(h->plan, od_pair_io{h->snap_pos, h->b.sx, h->b.sy, h->b.sz}, h->Npad,
-                           h->b.part_hi, h->b.part_lo, h->hp.rho0, &h->ds->err, h->stream));
-  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->snap_hi,
+  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->snap_pos, h->b.sx, h->b.sy, h->b.sz},
+                           (int)n, h->Npad, h->b.part_hi, h->b.part_lo, &h->ds->err, h->stream));
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, force_jsplit(h), h->b.part_hi, h->b.part_lo, h->snap_hi,
                             h->snap_lo, h->stream));
   std::vector<float4> hi(n), lo(n);
   OD_CK(h, cudaMemcpyAsync(hi.data(), h->snap_hi, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));

@@ -17,6 +17,7 @@
 // Device error word bits (reported by the host as OD_ERR_TIMEOUT / OD_ERR_STATE)
 #define OD_DERR_TIMEOUT 1u
 #define OD_DERR_LIST 2u
+#define OD_DERR_CELL 4u            // a cell holds more ions than the in-block sort takes
 
 // Per-simulation constants, resident in device memory.
 struct od_dparams {
@@ -142,9 +143,12 @@ __device__ __forceinline__ float od_pair_c_cut(float r2, const od_dparams& p) {
   float ex = od_ex2(r * OD_NLOG2E);
   float f = ex * fmaf(si, si, si);
   float x = fmaxf((r - p.rs) * p.inv_w, 0.0f);
-  // S = 1 - x^3 (10 - 15x + 6x^2), S' = -x^2 (30 - 60x + 30x^2) / (rc - rs)
-  float S = 1.0f - x * x * x * (10.0f - x * (15.0f - 6.0f * x));
-  float dS = -x * x * (30.0f - x * (60.0f - 30.0f * x)) * p.inv_w;
+  // S = 1 - 10x^3 + 15x^4 - 6x^5 = (1-x)^3 (1 + 3x + 6x^2) (no cancellation as x -> 1),
+  // S' = -30 x^2 (1-x)^2 / (rc - rs)
+  const float om = 1.0f - x;
+  float S = om * om * om * fmaf(x, fmaf(6.0f, x, 3.0f), 1.0f);
+  const float q = x * om;
+  float dS = -30.0f * q * q * p.inv_w;
   float c = (f * S - ex * si * dS) * ri;
   return r2 < p.rc2 ? c : 0.0f;
 }

@@ -36,6 +36,24 @@ struct od_dbufs {
 
 int od_num_sms(int device);
 
+// Uniform cell grid of the cutoff path (lambda units): cell (cx, cy, cz) spans
+// [lo + c*cx, lo + c*(cx+1)) per axis; ions outside the grid are clamped into border cells.
+struct od_cellgeom {
+  int gx, gy, gz, ncells;
+  float c, inv_c, lox, loy, loz;
+};
+// Device cell list of the cutoff path.
+struct od_cutlist {
+  od_cellgeom g;
+  int32_t *cell_of, *count, *fill, *start, *chunk_prefix, *perm;  // start/chunk_prefix: ncells+1
+  float *ox, *oy, *oz;   // sorted cell-relative offsets, 8-padded segments
+  int4* stencil;         // source-cell offsets within the cutoff of a target cell
+  int nstencil, cap;
+};
+cudaError_t od_launch_cutoff(const od_cutlist& L, const float4* pos, int n, int Npad,
+                             float4* part_hi, float4* part_lo, float rho0, float rc, float rs,
+                             uint32_t* err, unsigned long long* pair_count, cudaStream_t s);
+
 // Pointers into the allocation-free scratch array of od_ion_forces_static.
 struct od_static_view {
   uint32_t* err;
@@ -52,10 +70,19 @@ cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* 
                                  cudaStream_t s);
 cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* part_hi,
                              const float4* part_lo, float4* fhi, float4* flo, cudaStream_t s);
+// Force-evaluation context of one simulation: the all-pairs plan, or the cell list when cut != 0.
+struct od_force_ctx {
+  od_pair_plan plan;
+  const od_cutlist* cut;
+  float rho0, rc, rs;
+  unsigned long long* pair_count;  // pairs inside the cutoff (cutoff path, optional)
+};
+cudaError_t od_launch_force(const od_force_ctx& fc, const od_pair_io& io, int n, int Npad,
+                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s);
 cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
-                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s);
+                           int P, const od_force_ctx& fc, int nrec, cudaStream_t s);
 cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
-                                int N, int Npad, int P, const od_pair_plan& pl, float rho0, int nrec,
+                                int N, int Npad, int P, const od_force_ctx& fc, int nrec,
                                 cudaStream_t s);
 cudaError_t od_run_fp32_probe(int device, double* tflops);
 cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,

@@ -961,9 +961,17 @@ cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const f
   return cudaGetLastError();
 }
 
-// part 0: K1 (kick/drift); part 1: K2 (all pairs); part 2: K3..K6
+cudaError_t od_launch_force(const od_force_ctx& fc, const od_pair_io& io, int n, int Npad,
+                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s) {
+  if (fc.cut)
+    return od_launch_cutoff(*fc.cut, io.pos, n, Npad, part_hi, part_lo, fc.rho0, fc.rc, fc.rs, err,
+                            fc.pair_count, s);
+  return od_launch_pairs(fc.plan, io, Npad, part_hi, part_lo, fc.rho0, err, s);
+}
+
+// part 0: K1 (kick/drift); part 1: K2 (ion–ion sums); part 2: K3..K6
 cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
-                                int N, int Npad, int P, const od_pair_plan& pl, float rho0, int nrec,
+                                int N, int Npad, int P, const od_force_ctx& fc, int nrec,
                                 cudaStream_t s) {
   (void)P;
   const int nb = Npad / kBlk;
@@ -973,9 +981,10 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
     return cudaGetLastError();
   }
   if (part == 1)
-    return od_launch_pairs(pl, od_pair_io{b.pos, b.sx, b.sy, b.sz}, Npad, b.part_hi, b.part_lo,
-                           rho0, &ds->err, s);
-  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, pl.jsplit, b.fhi, b.flo,
+    return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz}, N, Npad, b.part_hi, b.part_lo,
+                           &ds->err, s);
+  const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
+  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
                                   b.flags, b.cq);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
@@ -987,9 +996,9 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
 }
 
 cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
-                           int P, const od_pair_plan& pl, float rho0, int nrec, cudaStream_t s) {
+                           int P, const od_force_ctx& fc, int nrec, cudaStream_t s) {
   for (int part = 0; part < 3; part++) {
-    cudaError_t e = od_launch_step_part(part, dp, ds, b, N, Npad, P, pl, rho0, nrec, s);
+    cudaError_t e = od_launch_step_part(part, dp, ds, b, N, Npad, P, fc, nrec, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

@@ -1,0 +1,80 @@
+"""GPU tests of the cutoff force path (device cell list) against the CPU oracle.
+
+Tolerances:
+  * with OpenMM's switching polynomial (the reference's cutOff=True: cutoff 3.2 lambda, switch
+    from 3.0 lambda) the pair force goes to zero smoothly at the cutoff, so FP32 and FP64 may
+    disagree on the inclusion of a pair at r = r_c without changing the force: per-ion relative
+    error <= 1e-5, as for all pairs;
+  * with a hard cutoff (no switching) a pair within rounding of r_c can be included on one side
+    only; the bound is 1e-5 for 99.9 % of ions and 1e-3 for all.
+"""
+import numpy as np
+import pytest
+
+from opendust_gb300 import _lib, workloads
+from oracle import oracle
+from tests._util import case, plant_close_pairs, rel_err_per_ion
+
+pytestmark = pytest.mark.gpu
+
+
+def _cut_case(N, seed, **kw):
+    return case(N=N, n=4, seed=seed, **kw)
+
+
+def test_cutoff_switching_snapshot(gpu_lib):
+    holder, pos, vel, plasma, sim, grains = _cut_case(4096, 21, cutOff=True)
+    assert holder.cfg.force_method == _lib.OD_FORCE_CUTOFF
+    pos = plant_close_pairs(pos, plasma.r_D_e, np.random.default_rng(3), n_pairs=32, dmin=2e-4)
+    with _lib.Engine(holder) as eng:
+        f = eng.force_snapshot(pos)
+    ref = oracle.force_snapshot(holder, pos, round32=True)
+    err = rel_err_per_ion(f, ref)
+    print(f"cutoff 3.2/3.0: per-ion rel err max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
+    assert err.max() <= 1e-5
+
+
+@pytest.mark.parametrize("N", [4096, 2**17])
+def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N):
+    spatial = pytest.importorskip("scipy.spatial")
+    holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=22, builder=workloads.field_chain,
+                                                 switch_distance=0.0)
+    assert holder.cfg.switch_dist == 0.0
+    with _lib.Engine(holder) as eng:
+        f = eng.force_snapshot(pos)
+        eng.set_state(pos, vel)
+        eng.set_timing(True)
+        eng.step(1)
+        pairs = eng.cutoff_pairs()
+        eng.set_timing(False)
+    idx = np.arange(N) if N <= 4096 else np.sort(np.random.default_rng(0).choice(N, 2048, replace=False))
+    ref = oracle.force_targets(holder, pos, idx, round32=True)
+    err = rel_err_per_ion(f[idx], ref)
+    print(f"hard cutoff N={N}: max {err.max():.3e} p99.9 {np.quantile(err, 0.999):.3e}, pairs {pairs}")
+    assert np.quantile(err, 0.999) <= 1e-5
+    assert err.max() <= 1e-3
+    # directed pairs inside the cutoff at the step's drifted positions, within rounding
+    lam = plasma.r_D_e
+    assert pairs > 0
+    tree = spatial.cKDTree(pos / lam)
+    approx = tree.count_neighbors(tree, holder.cfg.cutoff / lam) - N  # directed, self excluded
+    assert abs(pairs - approx) / approx < 0.01
+
+
+def test_cutoff_deterministic_and_one_step(gpu_lib):
+    holder, pos, vel, plasma, sim, grains = _cut_case(4096, 23, cutOff=True)
+    runs = []
+    for _ in range(2):
+        with _lib.Engine(holder) as eng:
+            eng.set_state(pos, vel)
+            eng.step(1)
+            s = eng.series(0, 1)
+            p, v = eng.get_state()
+        runs.append((s, p, v))
+    assert np.array_equal(runs[0][1], runs[1][1]) and np.array_equal(runs[0][2], runs[1][2])
+    ref = oracle.run(holder, pos, vel, 0, 1, round32=True)
+    dpos = np.max(np.abs(runs[0][1] - ref["pos"])) / plasma.r_D_e
+    dvel = np.max(np.abs(runs[0][2] - ref["vel"])) / plasma.v_T
+    print(f"cutoff one step: max |dx| {dpos:.3e} lambda, max |dv| {dvel:.3e} v_T")
+    assert dpos < 1e-5
+    assert dvel < 1e-4
