@@ -45,7 +45,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="full_plain", choices=["full_plain", "small_plain", "field_chain"])
+    ap.add_argument("--workload", default="full_plain",
+                    choices=["full_plain", "small_plain", "field_chain", "sweep", "serve"])
+    ap.add_argument("--sweep-sims", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--window", type=int, default=50)
     ap.add_argument("--cpu-sample-targets", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -327,10 +332,94 @@ def run_ours(args, dist: Dist):
     return 0
 
 
+def run_sweep(args, dist: Dist):
+    """Batched sweep (64 independent simulations drawn from seeds) against the same
+    simulations run back to back on the plain path; K steps each, wall clock, same GPU."""
+    import numpy as np
+
+    from opendust_gb300 import _lib, build_simulation, setup_host, workloads
+
+    if dist.rank != 0:
+        return 0
+    K, S = args.steps, args.sweep_sims
+    window = 5000
+    members = []
+    t_setup = time.perf_counter()
+    for k in range(S):
+        plasma, sim, grains, d, ext = workloads.sweep_member(seed=k, n_steps=K + args.warmup)
+        holder, _ = build_simulation(plasma, sim, grains, d, seed=k, **ext)
+        pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
+                                            plasma.v_fl, plasma.v_T, d, k)
+        members.append((holder, pos, vel, sim.N))
+    t_setup = time.perf_counter() - t_setup
+    ion_steps = sum(m[3] for m in members) * K
+    # plain path, back to back
+    plain_s = 0.0
+    plain_series = []
+    for holder, pos, vel, _ in members:
+        with _lib.Engine(holder) as eng:
+            eng.set_state(pos, vel)
+            eng.step(args.warmup)
+            t0 = time.perf_counter()
+            eng.step(K)
+            plain_s += time.perf_counter() - t0
+            plain_series.append(eng.series(0, K + args.warmup))
+    # batched
+    with _lib.Batch() as batch:
+        slots = [batch.add(h, p, v) for h, p, v, _ in members]
+        batch.step(args.warmup)
+        t0 = time.perf_counter()
+        batch.step(K)
+        batch_s = time.perf_counter() - t0
+        batch_dev_ms = batch.last_step_ms()
+        same = all(all(np.array_equal(batch.member(s).series(0, K + args.warmup)[q], ps[q]) for q in ps)
+                   for s, ps in zip(slots, plain_series))
+    per_sim_window_s = lambda sec: sec / K * window / S
+    line = {"metric": "sweep sims/hour", "value": 3600.0 / per_sim_window_s(batch_s),
+            "unit": "simulations/hour (5000-step windows, 64 seeded members)",
+            "plain_value": 3600.0 / per_sim_window_s(plain_s), "ratio_batched_vs_plain": plain_s / batch_s,
+            "steps": K, "warmup": args.warmup, "batched_step_ms": batch_s / K * 1e3,
+            "batched_device_step_ms": batch_dev_ms / K, "plain_step_ms_sum": plain_s / K * 1e3,
+            "ion_steps_per_s_batched": ion_steps / batch_s, "ion_steps_per_s_plain": ion_steps / plain_s,
+            "results_equal_bitwise": bool(same), "force_error_vs_plain": 0.0 if same else None,
+            "host_setup_s": t_setup, "n_ions": [int(m[3]) for m in members],
+            "config": {"workload": "sweep: 64 members, N log-uniform 2^14-2^18, Mach 0.1-2, grain radius "
+                                   "1-20 um log-uniform, 1-4 grains, mfp collisions with p=0.5"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serve(args, dist: Dist):
+    """Poisson request stream through the continuous-batching server vs the plain path."""
+    import copy
+
+    from opendust_gb300 import serve
+
+    if dist.rank != 0:
+        return 0
+    reqs = serve.poisson_requests(rate=args.rate, duration=args.duration, seed=7, log2n=(14, 16),
+                                  window=args.window)
+    pool = serve.start_pool(8)
+    list(pool.map(int, range(8)))  # start the workers before the timed run
+    s = serve.Server(chunk=10).run(copy.deepcopy(reqs), pool=pool)
+    pool.shutdown()
+    p = serve.run_plain(copy.deepcopy(reqs))
+    line = {"metric": "request latency p99 (s)", "value": s["latency_p99_s"], "unit": "s",
+            "higher_is_better": False, "server": s, "plain": p,
+            "throughput_ratio_server_vs_plain": s["throughput_req_per_s"] / p["throughput_req_per_s"],
+            "config": {"workload": f"serve: Poisson {args.rate}/s for {args.duration} s, N log-uniform "
+                                   f"2^14-2^16, 1-8 grains, Mach 0.1-2, Maxwellian or field-driven, "
+                                   f"{args.window}-step windows, 80% HBM budget"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     dist = Dist("gloo" if args.impl == "reference" else "nccl")
     try:
+        if args.workload in ("sweep", "serve") and args.impl == "ours":
+            return run_sweep(args, dist) if args.workload == "sweep" else run_serve(args, dist)
         rc = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
     finally:
         dist.close()

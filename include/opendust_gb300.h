@@ -189,6 +189,11 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);
+/* Autotuner: times every supported (threads, targets_per_thread, variant) and three source
+ * splits on the handle's current positions and keeps the fastest; with use_cache the result
+ * cached for this (device, padded size) in the process is reused. *best_pairs_per_s receives
+ * the measured rate (0 when cached). All-pairs method only. */
+od_status od_autotune(od_handle* h, int32_t use_cache, double* best_pairs_per_s);
 /* plan5 = {threads, targets_per_thread, variant, jsplit, chunk} */
 od_status od_get_pair_plan(const od_handle* h, int32_t* plan5);
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured by a short probe
@@ -233,6 +238,33 @@ od_status od_collect_flags(od_handle* h, const double* pos, int64_t n, int64_t* 
  * Points come from Philox stream OD_RNG_TRAP with the given seed. */
 od_status od_trap_potential(double R_over_lambda, double H_over_lambda, int32_t n_r, int32_t n_h,
                             int64_t n_points, uint64_t seed, int32_t device, double* pot);
+
+/* ---- Batches: many independent simulations stepped together (no counterpart in the
+ * reference, whose parameter sweeps call simulate() once per point, e.g.
+ * examples/Piel2017/Figure5/launchPiel2017Figure5.py:32-106). Every stage of a batch step is
+ * one launch for all members; the N^2 stage is one persistent launch over work items of all
+ * members. Members are ordinary handles: read their results with od_get_series /
+ * od_get_averages / od_get_state on od_batch_member(). A member's results are bitwise those of
+ * the same simulation stepped alone. Members use the all-pairs force method. */
+typedef struct od_batch od_batch;
+od_status od_batch_create(int32_t device, od_batch** out);
+/* Creates a member from cfg with initial state pos/vel (as od_create + od_set_state); *slot
+ * receives its slot index. May be called between steps (continuous batching). */
+od_status od_batch_add(od_batch* b, const od_config* cfg, const double* pos, const double* vel,
+                       int32_t* slot);
+od_status od_batch_remove(od_batch* b, int32_t slot);
+od_handle* od_batch_member(od_batch* b, int32_t slot);
+int32_t od_batch_size(const od_batch* b);
+/* Advances every member by nsteps (fails with OD_ERR_STATE if a member's series would overflow). */
+od_status od_batch_step(od_batch* b, int64_t nsteps);
+/* Device milliseconds of the last od_batch_step (CUDA events on the batch stream). */
+od_status od_batch_last_step_ms(const od_batch* b, double* ms);
+od_status od_batch_destroy(od_batch* b);
+const char* od_batch_last_error(const od_batch* b);
+/* Free and total device memory (admission control of a request server). */
+od_status od_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
+/* Device bytes a simulation with this configuration allocates (admission control). */
+od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes);
 
 /* Ion–ion forces for callers that cannot allocate device memory (no counterpart in the
  * reference). Plug-ins that live inside another runtime's allocator, loops that forbid

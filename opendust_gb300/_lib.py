@@ -140,6 +140,18 @@ def load(path: str | None = None):
         "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
         "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
         "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
+        "od_autotune": (c_int32, [H, c_int32, _DP]),
+        "od_batch_create": (c_int32, [c_int32, POINTER(c_void_p)]),
+        "od_batch_add": (c_int32, [c_void_p, POINTER(od_config), _DP, _DP, POINTER(c_int32)]),
+        "od_batch_remove": (c_int32, [c_void_p, c_int32]),
+        "od_batch_member": (c_void_p, [c_void_p, c_int32]),
+        "od_batch_size": (c_int32, [c_void_p]),
+        "od_batch_step": (c_int32, [c_void_p, c_int64]),
+        "od_batch_last_step_ms": (c_int32, [c_void_p, _DP]),
+        "od_batch_destroy": (c_int32, [c_void_p]),
+        "od_batch_last_error": (c_char_p, [c_void_p]),
+        "od_config_device_bytes": (c_int32, [POINTER(od_config), POINTER(c_int64)]),
+        "od_device_memory": (c_int32, [c_int32, POINTER(c_int64), POINTER(c_int64)]),
         "od_ion_forces_static": (c_int32, [c_void_p, c_int64, c_double, c_double, c_double, c_void_p,
                                            c_void_p]),
         "od_trap_potential": (
@@ -250,20 +262,25 @@ def make_config(
 class Engine:
     """One simulation resident on one GPU (an ``od_handle``)."""
 
-    def __init__(self, holder: ConfigHolder, device: int = 0):
+    def __init__(self, holder: ConfigHolder, device: int = 0, _handle=None):
         lib = load()
         self._lib = lib
         self.holder = holder
         self.n = int(holder.cfg.n_ions)
         self.P = int(holder.cfg.n_grains)
         self.n_steps = int(holder.cfg.n_steps)
-        h = c_void_p()
-        check(lib.od_create(holder.ptr(), int(device), ctypes.byref(h)), None)
-        self.h = h
+        self._owned = _handle is None
+        if _handle is None:
+            h = c_void_p()
+            check(lib.od_create(holder.ptr(), int(device), ctypes.byref(h)), None)
+            self.h = h
+        else:
+            self.h = c_void_p(_handle)
 
     def close(self):
         if getattr(self, "h", None):
-            self._lib.od_destroy(self.h)
+            if self._owned:
+                self._lib.od_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -330,6 +347,12 @@ class Engine:
     def set_pair_plan(self, threads: int, targets_per_thread: int, variant: int, jsplit: int = 0):
         check(self._lib.od_set_pair_plan(self.h, threads, targets_per_thread, variant, jsplit), self.h)
 
+    def autotune(self, use_cache: bool = True) -> float:
+        """Pick the fastest all-pairs plan on the current positions; returns pairs/s measured."""
+        v = c_double()
+        check(self._lib.od_autotune(self.h, int(use_cache), ctypes.byref(v)), self.h)
+        return v.value
+
     def pair_plan(self):
         a = (c_int32 * 5)()
         check(self._lib.od_get_pair_plan(self.h, a), self.h)
@@ -373,6 +396,77 @@ class Engine:
         )
         check(st, self.h)
         return idx[: cnt.value].copy(), int(cnt.value), gc[: self.P].copy()
+
+
+def config_device_bytes(holder: ConfigHolder) -> int:
+    """Device bytes a simulation with this configuration allocates (admission control)."""
+    v = c_int64()
+    check(load().od_config_device_bytes(holder.ptr(), ctypes.byref(v)), None)
+    return int(v.value)
+
+
+class Batch:
+    """Many independent simulations stepped together (``od_batch``)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        b = c_void_p()
+        self._check(self._lib.od_batch_create(int(device), ctypes.byref(b)), None)
+        self.b = b
+        self._holders = {}
+
+    def _check(self, st, b):
+        if st != 0:
+            msg = self._lib.od_batch_last_error(b)
+            raise OpenDustError(st, msg.decode() if msg else "")
+
+    def add(self, holder: ConfigHolder, pos: np.ndarray, vel: np.ndarray) -> int:
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        slot = c_int32()
+        self._check(self._lib.od_batch_add(self.b, holder.ptr(), _dptr(pos), _dptr(vel),
+                                           ctypes.byref(slot)), self.b)
+        self._holders[slot.value] = holder
+        return slot.value
+
+    def remove(self, slot: int):
+        self._check(self._lib.od_batch_remove(self.b, int(slot)), self.b)
+        self._holders.pop(slot, None)
+
+    def member(self, slot: int) -> Engine:
+        """Non-owning view of a member (series, averages, state)."""
+        h = self._lib.od_batch_member(self.b, int(slot))
+        if not h:
+            raise OpenDustError(1, f"no batch member in slot {slot}")
+        return Engine(self._holders[slot], _handle=h)
+
+    def step(self, nsteps: int):
+        self._check(self._lib.od_batch_step(self.b, int(nsteps)), self.b)
+
+    def last_step_ms(self) -> float:
+        v = c_double()
+        self._lib.od_batch_last_step_ms(self.b, ctypes.byref(v))
+        return v.value
+
+    def __len__(self):
+        return int(self._lib.od_batch_size(self.b))
+
+    def close(self):
+        if getattr(self, "b", None):
+            self._lib.od_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def fp32_peak_tflops(device: int = 0) -> float:

@@ -320,19 +320,23 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
   OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
   if (cfg->force_method == OD_FORCE_CUTOFF) {
-    // cells of side rc/k: k = 4 unless that leaves more than ~800 ions per cell on average
+    // Cells of side c = a power of two not above rc/4 (halved while the mean occupancy exceeds
+    // ~800 ions), on a grid whose origin is a multiple of c: cell origins and the shifts between
+    // cells are then exact in FP32, so a target moved into a neighbour cell's frame is rounded
+    // once, to within half an ulp of 2c.
     const double rc = h->hp.rc, Rh = h->hp.Rh, Hh = h->hp.Hh;
     const double dens = cfg->n_ions / (OD_PI_D * Rh * Rh * Hh);
-    int kk = 4;
-    while (kk < 8 && dens * pow(rc / kk, 3) > 800.0) kk++;
-    const double c = rc / kk;
+    double c = std::ldexp(1.0, (int)std::floor(std::log2(rc / 4.0)));
+    while (dens * c * c * c > 800.0 && c > rc / 64.0) c *= 0.5;
+    const int kk = (int)std::ceil(rc / c);
     od_cellgeom& g = h->cut.g;
     g.c = (float)c;
     g.inv_c = (float)(1.0 / c);
-    g.lox = g.loy = (float)(-Rh - c);
-    g.loz = (float)(-Hh / 2 - c);
-    g.gx = g.gy = (int)ceil((2 * Rh + 2 * c) / c);
-    g.gz = (int)ceil((Hh + 2 * c) / c);
+    const double mx = std::ceil(Rh / c + 1.0), mz = std::ceil(Hh / 2 / c + 1.0);
+    g.lox = g.loy = (float)(-mx * c);
+    g.loz = (float)(-mz * c);
+    g.gx = g.gy = (int)(2 * mx);
+    g.gz = (int)(2 * mz);
     g.ncells = g.gx * g.gy * g.gz;
     std::vector<int4> st;
     for (int dz = -kk - 1; dz <= kk + 1; dz++)
@@ -624,6 +628,76 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
   return OD_OK;
 }
 
+// Autotuner: times each supported (threads, targets per thread, variant) with the default split
+// and with half and twice as many source chunks, on the handle's current positions, over the
+// first target blocks only (enough for several waves), and keeps the fastest plan. Results are
+// cached per (device, padded ion count) for the process.
+#include <map>
+static std::mutex g_tune_mu;
+static std::map<std::pair<int, int>, od_pair_plan> g_tuned;
+
+extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_pairs_per_s) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (h->has_cut) return fail(h, OD_ERR_UNSUPPORTED, "the autotuner covers the all-pairs method");
+  OD_CK(h, cudaSetDevice(h->device));
+  const auto key = std::make_pair(h->device, h->Npad);
+  if (use_cache) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      const od_pair_plan& p = it->second;
+      if (best_pairs_per_s) *best_pairs_per_s = 0;
+      return od_set_pair_plan(h, p.nt, p.ipt, p.variant, p.jsplit);
+    }
+  }
+  OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
+  const int shapes[][3] = {{256, 1, 0}, {128, 1, 0}, {256, 1, 1}, {128, 2, 2}, {256, 2, 2},
+                           {128, 2, 3}, {256, 2, 3}};
+  const int sms = od_num_sms(h->device);
+  cudaEvent_t e0, e1;
+  OD_CK(h, cudaEventCreate(&e0));
+  OD_CK(h, cudaEventCreate(&e1));
+  double best = -1;
+  od_pair_plan best_plan = h->plan;
+  for (const auto& sh : shapes) {
+    const int nbx = h->Npad / (sh[0] * sh[1]);
+    const int js0 = std::max(1, (sms * 8 * 4 + nbx - 1) / nbx);
+    for (int mult = 0; mult < 3; mult++) {
+      const int js = mult == 0 ? js0 : (mult == 1 ? std::max(1, js0 / 2) : js0 * 2);
+      if (od_set_pair_plan(h, sh[0], sh[1], sh[2], js) != OD_OK) continue;
+      const od_pair_plan& pl = h->plan;
+      // enough target blocks for ~8 waves of the source split, at most the full grid
+      const int limit = std::min(nbx, std::max(1, (sms * 32 + pl.jsplit - 1) / pl.jsplit));
+      const od_pair_io io{h->b.pos, h->b.sx, h->b.sy, h->b.sz};
+      OD_CK(h, od_launch_pairs_probe(pl, io, h->Npad, limit, h->b.part_hi, h->b.part_lo, h->hp.rho0,
+                                     &h->ds->err, h->stream));
+      OD_CK(h, cudaEventRecord(e0, h->stream));
+      for (int r = 0; r < 2; r++)
+        OD_CK(h, od_launch_pairs_probe(pl, io, h->Npad, limit, h->b.part_hi, h->b.part_lo,
+                                       h->hp.rho0, &h->ds->err, h->stream));
+      OD_CK(h, cudaEventRecord(e1, h->stream));
+      OD_CK(h, cudaEventSynchronize(e1));
+      float ms = 0;
+      OD_CK(h, cudaEventElapsedTime(&ms, e0, e1));
+      const double pairs = 2.0 * limit * (double)(sh[0] * sh[1]) * h->Npad;
+      const double rate = pairs / (ms * 1e-3);
+      if (rate > best) { best = rate; best_plan = pl; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  od_status st = od_set_pair_plan(h, best_plan.nt, best_plan.ipt, best_plan.variant, best_plan.jsplit);
+  if (st != OD_OK) return st;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = h->plan;
+  }
+  if (best_pairs_per_s) *best_pairs_per_s = best;
+  // the probes overwrote the partial slabs: restore the ion–ion sums of the current state
+  if (h->state_set) return refresh_forces(h);
+  return OD_OK;
+}
+
 extern "C" od_status od_get_pair_plan(const od_handle* h, int32_t* plan5) {
   if (!h || !plan5) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
   plan5[0] = h->plan.nt; plan5[1] = h->plan.ipt; plan5[2] = h->plan.variant;
@@ -860,5 +934,278 @@ extern "C" od_status od_ion_forces_static(const double* pos_dev, int64_t n, doub
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "od_ion_forces_static");
   if (err & OD_DERR_TIMEOUT) return fail(nullptr, OD_ERR_TIMEOUT, "a bounded device wait ran out");
+  return OD_OK;
+}
+
+// ============================================================== batches of simulations
+// A batch owns member handles (ordinary od_handle objects) and steps all of them with one set
+// of batch-wide launches per step (od_launch_batch_step), replayed from a CUDA graph that is
+// rebuilt whenever members join or leave.
+struct od_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<od_handle*> members;  // nullptr marks a free slot
+  bool dirty = true;
+  od_simdesc* d_sims = nullptr;
+  int2* d_blk_ion = nullptr;
+  int4* d_items = nullptr;
+  int2* d_blk_corr = nullptr;
+  size_t c_sims = 0, c_blk_ion = 0, c_items = 0, c_blk_corr = 0;
+  unsigned int* d_next = nullptr;
+  uint32_t* d_err = nullptr;
+  od_batchview view{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  std::string err;
+};
+
+static od_status bfail(od_batch* b, od_status st, const std::string& msg) {
+  if (b) b->err = msg; else g_err = msg;
+  return st;
+}
+#define OD_BCK(b, call)                                                                  \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return bfail(b, e_ == cudaErrorMemoryAllocation ? OD_ERR_OOM : OD_ERR_CUDA,        \
+                   std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+  } while (0)
+
+extern "C" const char* od_batch_last_error(const od_batch* b) { return b ? b->err.c_str() : g_err.c_str(); }
+
+extern "C" od_status od_batch_create(int32_t device, od_batch** out) {
+  if (!out) return bfail(nullptr, OD_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (od_device_count() <= device || device < 0)
+    return bfail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  od_batch* b = new (std::nothrow) od_batch();
+  if (!b) return bfail(nullptr, OD_ERR_OOM, "host allocation failed");
+  b->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_err, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(b->d_err, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+  if (e != cudaSuccess) {
+    g_err = std::string("od_batch_create: ") + cudaGetErrorString(e);
+    if (b->d_next) cudaFree(b->d_next);
+    if (b->d_err) cudaFree(b->d_err);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return OD_ERR_CUDA;
+  }
+  *out = b;
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const double* pos,
+                                  const double* vel, int32_t* slot) {
+  if (!b || !cfg || !pos || !vel || !slot) return bfail(b, OD_ERR_INVALID, "NULL argument");
+  if (cfg->force_method != OD_FORCE_ALLPAIRS)
+    return bfail(b, OD_ERR_UNSUPPORTED, "batch members use the all-pairs force method");
+  od_handle* h = nullptr;
+  od_status st = od_create(cfg, b->device, &h);
+  if (st != OD_OK) return bfail(b, st, g_err);
+  if (h->plan.variant != 2 || h->plan.nt != 256 || h->plan.ipt != 2) {
+    st = od_set_pair_plan(h, 256, 2, 2, 0);
+    if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
+  }
+  st = od_set_state(h, pos, vel, cfg->n_ions);
+  if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
+  int s = -1;
+  for (size_t k = 0; k < b->members.size(); k++)
+    if (!b->members[k]) { s = (int)k; break; }
+  if (s < 0) { s = (int)b->members.size(); b->members.push_back(nullptr); }
+  b->members[s] = h;
+  b->dirty = true;
+  *slot = s;
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_remove(od_batch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int32_t)b->members.size() || !b->members[slot])
+    return bfail(b, OD_ERR_INVALID, "no batch member in that slot");
+  od_destroy(b->members[slot]);
+  b->members[slot] = nullptr;
+  b->dirty = true;
+  return OD_OK;
+}
+
+extern "C" od_handle* od_batch_member(od_batch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int32_t)b->members.size()) return nullptr;
+  return b->members[slot];
+}
+
+extern "C" int32_t od_batch_size(const od_batch* b) {
+  if (!b) return 0;
+  int32_t n = 0;
+  for (od_handle* h : b->members) n += h != nullptr;
+  return n;
+}
+
+template <typename T>
+static od_status upload_table(od_batch* b, T** dptr, size_t* cap, const std::vector<T>& v) {
+  if (v.size() > *cap) {
+    if (*dptr) cudaFree(*dptr);
+    *dptr = nullptr;
+    *cap = 0;
+    OD_BCK(b, cudaMalloc((void**)dptr, sizeof(T) * std::max<size_t>(v.size(), 1)));
+    *cap = v.size();
+  }
+  if (!v.empty())
+    OD_BCK(b, cudaMemcpyAsync(*dptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, b->stream));
+  return OD_OK;
+}
+
+static od_status batch_rebuild(od_batch* b) {
+  std::vector<od_simdesc> sims;
+  std::vector<int2> blk_ion, blk_corr;
+  struct item { int4 w; long long work; };
+  std::vector<item> items;
+  for (od_handle* h : b->members) {
+    if (!h) continue;
+    const int m = (int)sims.size();
+    od_simdesc d{};
+    d.dp = h->dp; d.ds = h->ds; d.b = h->b;
+    d.N = h->N; d.Npad = h->Npad; d.nb = h->Npad / 256;
+    d.jsplit = h->plan.jsplit; d.chunk = h->plan.chunk; d.nrec = h->nrec;
+    d.rho0 = h->hp.rho0;
+    const float nr = 64.0f * h->hp.rho0;
+    d.newton_r2 = nr * nr;
+    sims.push_back(d);
+    for (int lb = 0; lb < d.nb; lb++) blk_ion.push_back(make_int2(m, lb));
+    for (int lb = 0; lb < d.nb + d.nrec; lb++) blk_corr.push_back(make_int2(m, lb));
+    for (int ib = 0; ib < d.Npad / 512; ib++)
+      for (int js = 0; js < d.jsplit; js++) {
+        const int j0 = js * d.chunk, j1 = std::min(j0 + d.chunk, d.Npad);
+        if (j1 > j0) items.push_back({make_int4(m, ib, j0, j1), (long long)(j1 - j0)});
+      }
+  }
+  std::stable_sort(items.begin(), items.end(), [](const item& a, const item& c) { return a.work > c.work; });
+  std::vector<int4> w(items.size());
+  for (size_t k = 0; k < items.size(); k++) w[k] = items[k].w;
+  od_status st;
+  if ((st = upload_table(b, &b->d_sims, &b->c_sims, sims)) != OD_OK) return st;
+  if ((st = upload_table(b, &b->d_blk_ion, &b->c_blk_ion, blk_ion)) != OD_OK) return st;
+  if ((st = upload_table(b, &b->d_items, &b->c_items, w)) != OD_OK) return st;
+  if ((st = upload_table(b, &b->d_blk_corr, &b->c_blk_corr, blk_corr)) != OD_OK) return st;
+  OD_BCK(b, cudaStreamSynchronize(b->stream));
+  od_batchview& v = b->view;
+  v.sims = b->d_sims; v.nsims = (int)sims.size();
+  v.blk_ion = b->d_blk_ion; v.nblk_ion = (int)blk_ion.size();
+  v.items = b->d_items; v.nitems = (int)w.size();
+  v.blk_corr = b->d_blk_corr; v.nblk_corr = (int)blk_corr.size();
+  v.pair_grid = od_num_sms(b->device) * 4;
+  v.next = b->d_next; v.err = b->d_err;
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+  if (v.nsims > 0) {
+    OD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = od_launch_batch_step(v, b->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return bfail(b, OD_ERR_CUDA, std::string("batch step capture: ") +
+                                       cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    b->graph = g;
+    OD_BCK(b, cudaGraphInstantiate(&b->exec, g, 0));
+  }
+  b->dirty = false;
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_step(od_batch* b, int64_t nsteps) {
+  if (!b) return bfail(nullptr, OD_ERR_INVALID, "batch is NULL");
+  if (nsteps < 0) return bfail(b, OD_ERR_INVALID, "nsteps < 0");
+  for (od_handle* h : b->members)
+    if (h && h->step + nsteps > h->cfg.n_steps)
+      return bfail(b, OD_ERR_STATE, "a member's result series would overflow (n_steps reached)");
+  OD_BCK(b, cudaSetDevice(b->device));
+  if (b->dirty) {
+    od_status st = batch_rebuild(b);
+    if (st != OD_OK) return st;
+  }
+  if (!b->exec || nsteps == 0) { b->last_ms = 0; return OD_OK; }
+  OD_BCK(b, cudaEventRecord(b->ev0, b->stream));
+  for (int64_t s = 0; s < nsteps; s++) OD_BCK(b, cudaGraphLaunch(b->exec, b->stream));
+  OD_BCK(b, cudaEventRecord(b->ev1, b->stream));
+  OD_BCK(b, cudaStreamSynchronize(b->stream));
+  float ms = 0;
+  OD_BCK(b, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+  b->last_ms = ms;
+  uint32_t berr = 0;
+  OD_BCK(b, cudaMemcpy(&berr, b->d_err, sizeof(berr), cudaMemcpyDeviceToHost));
+  for (od_handle* h : b->members) {
+    if (!h) continue;
+    h->step += nsteps;
+    od_status st = check_device_err(h);
+    if (st != OD_OK) return bfail(b, st, h->err);
+  }
+  if (berr & OD_DERR_TIMEOUT) return bfail(b, OD_ERR_TIMEOUT, "a bounded device wait ran out");
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_last_step_ms(const od_batch* b, double* ms) {
+  if (!b || !ms) return OD_ERR_INVALID;
+  *ms = b->last_ms;
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_destroy(od_batch* b) {
+  if (!b) return OD_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (od_handle* h : b->members)
+    if (h) od_destroy(h);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  void* ptrs[] = {b->d_sims, b->d_blk_ion, b->d_items, b->d_blk_corr, b->d_next, b->d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return OD_OK;
+}
+
+extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes) {
+  if (!cfg || !bytes) return bfail(nullptr, OD_ERR_INVALID, "NULL argument");
+  od_status st = validate(cfg);
+  if (st != OD_OK) return st;
+  const int64_t Np = ((cfg->n_ions + OD_PAD - 1) / OD_PAD) * OD_PAD;
+  const od_pair_plan pl = default_plan((int)Np, 152);
+  const int64_t P = std::max(cfg->n_grains, 1);
+  int64_t b = 0;
+  b += Np * 16 * 4;                 // pos, vel, fhi, flo
+  b += Np * 12;                     // SoA copy
+  b += (int64_t)pl.jsplit * Np * 32;  // partial slabs
+  b += Np / 32 * 4 + Np * (4 + 4 + 48);  // flags, list, list bits, list positions/velocities
+  b += (Np / 256) * P * 3 * 8;      // orbit partials
+  b += cfg->n_steps * P * 13 * 8;   // result series
+  b += sizeof(od_dparams) + sizeof(od_dstate) + 4096;
+  *bytes = b;
+  return OD_OK;
+}
+
+extern "C" od_status od_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes) {
+  if (!free_bytes || !total_bytes) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
+  if (od_device_count() <= device || device < 0)
+    return fail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaError_t e = cudaSetDevice(device);
+  size_t f = 0, t = 0;
+  if (e == cudaSuccess) e = cudaMemGetInfo(&f, &t);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemGetInfo");
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
   return OD_OK;
 }

@@ -227,6 +227,9 @@ __device__ __forceinline__ uint32_t od_smem_addr(const void* p) {
 __device__ __forceinline__ void od_mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(od_smem_addr(bar)), "r"(count));
 }
+__device__ __forceinline__ void od_mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(od_smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ void od_fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }

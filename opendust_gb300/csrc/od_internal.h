@@ -36,6 +36,30 @@ struct od_dbufs {
 
 int od_num_sms(int device);
 
+// One member of a batch, as the batched kernels see it.
+struct od_simdesc {
+  const od_dparams* dp;
+  od_dstate* ds;
+  od_dbufs b;
+  int N, Npad, nb, jsplit, chunk, nrec;
+  float rho0, newton_r2;
+};
+// Device tables of one batch step.
+struct od_batchview {
+  const od_simdesc* sims;
+  int nsims;
+  const int2* blk_ion;   // (member, local 256-ion block) for the ion-parallel stages
+  int nblk_ion;
+  const int4* items;     // (member, 512-target block, j0, j1) all-pairs work items
+  int nitems;
+  const int2* blk_corr;  // (member, local block in [0, nb + nrec)) for correction/orbit sums
+  int nblk_corr;
+  int pair_grid;         // persistent blocks of the all-pairs stage
+  unsigned int* next;    // work counter of the all-pairs stage
+  uint32_t* err;
+};
+cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s);
+
 // Uniform cell grid of the cutoff path (lambda units): cell (cx, cy, cz) spans
 // [lo + c*cx, lo + c*(cx+1)) per axis; ions outside the grid are clamped into border cells.
 struct od_cellgeom {
@@ -66,6 +90,10 @@ cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, 
 
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* part_hi,
                             float4* part_lo, float rho0, uint32_t* err, cudaStream_t s);
+// the same launch restricted to the first gridx_limit target blocks (autotuner probes)
+cudaError_t od_launch_pairs_probe(const od_pair_plan& pl, const od_pair_io& io, int Npad,
+                                  int gridx_limit, float4* part_hi, float4* part_lo, float rho0,
+                                  uint32_t* err, cudaStream_t s);
 cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,
                                  cudaStream_t s);
 cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* part_hi,

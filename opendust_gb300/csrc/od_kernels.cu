@@ -205,21 +205,22 @@ __device__ __forceinline__ float sum2(od_u64 v) {
   return f.x + f.y;
 }
 
+// One block's share of the packed all-pairs sums: targets iblk*2*NT .. +2*NT, sources
+// [j0, j1); partial sums written at part_*[slab_off + i]. Returns false after a wait timeout.
 template <int NT, int NEWTON>
-__global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
-                                                 const float* __restrict__ sy,
-                                                 const float* __restrict__ sz, int Npad, int chunk,
-                                                 float4* __restrict__ part_hi,
-                                                 float4* __restrict__ part_lo, float rho0,
-                                                 float newton_r2, uint32_t* __restrict__ err) {
+__device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
+                                              const float* __restrict__ sy,
+                                              const float* __restrict__ sz, int iblk, int j0,
+                                              int j1, size_t slab_off,
+                                              float4* __restrict__ part_hi,
+                                              float4* __restrict__ part_lo, float rho0,
+                                              float newton_r2, uint32_t* __restrict__ err) {
   __shared__ __align__(128) float tx[2][OD_TJ];
   __shared__ __align__(128) float ty[2][OD_TJ];
   __shared__ __align__(128) float tz[2][OD_TJ];
   __shared__ __align__(8) uint64_t bar[2];
   const int tid = threadIdx.x;
-  const int i0 = blockIdx.x * (2 * NT) + tid, i1 = i0 + NT;
-  const int j0 = blockIdx.y * chunk;
-  const int j1 = min(j0 + chunk, Npad);
+  const int i0 = iblk * (2 * NT) + tid, i1 = i0 + NT;
   const int ntiles = (j1 - j0) / OD_TJ;
   const od_u64 X0 = p2(sx[i0], sx[i0]), Y0 = p2(sy[i0], sy[i0]), Z0 = p2(sz[i0], sz[i0]);
   const od_u64 X1 = p2(sx[i1], sx[i1]), Y1 = p2(sy[i1], sy[i1]), Z1 = p2(sz[i1], sz[i1]);
@@ -298,13 +299,29 @@ __global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
       atomicOr(err, OD_DERR_TIMEOUT);
       for (int u = t; u < issued; u++) od_mbar_wait(&bar[u & 1], (u >> 1) & 1);
     }
-    return;
+    return false;
   }
-  const size_t off = (size_t)blockIdx.y * Npad;
+  const size_t off = slab_off;
   part_hi[off + i0] = make_float4(h0x, h0y, h0z, 0.f);
   part_lo[off + i0] = make_float4(l0x, l0y, l0z, 0.f);
   part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
   part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+  // release the barriers so that the next call of this body (persistent loop) can init them
+  __syncthreads();
+  if (tid == 0) { od_mbar_inval(&bar[0]); od_mbar_inval(&bar[1]); }
+  return true;
+}
+
+template <int NT, int NEWTON>
+__global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
+                                                 const float* __restrict__ sy,
+                                                 const float* __restrict__ sz, int Npad, int chunk,
+                                                 float4* __restrict__ part_hi,
+                                                 float4* __restrict__ part_lo, float rho0,
+                                                 float newton_r2, uint32_t* __restrict__ err) {
+  const int j0 = blockIdx.y * chunk;
+  pairs_x2_body<NT, NEWTON>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, Npad),
+                            (size_t)blockIdx.y * Npad, part_hi, part_lo, rho0, newton_r2, err);
 }
 
 __global__ void k_aos_to_soa(const float4* __restrict__ pos, int Npad, float* __restrict__ sx,
@@ -373,17 +390,13 @@ __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint3
   }
 }
 
-__global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restrict__ dp,
-                                                     const od_dstate* __restrict__ ds,
-                                                     float4* __restrict__ pos,
-                                                     float4* __restrict__ vel,
-                                                     const float4* __restrict__ fhi,
-                                                     const float4* __restrict__ flo,
-                                                     const float* __restrict__ cq,
-                                                     float* __restrict__ sx, float* __restrict__ sy,
-                                                     float* __restrict__ sz) {
-  const od_dparams& p = *dp;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void kick_drift_body(const od_dparams& p, const od_dstate* __restrict__ ds,
+                                                float4* __restrict__ pos, float4* __restrict__ vel,
+                                                const float4* __restrict__ fhi,
+                                                const float4* __restrict__ flo,
+                                                const float* __restrict__ cq,
+                                                float* __restrict__ sx, float* __restrict__ sy,
+                                                float* __restrict__ sz, int i) {
   if (i >= p.N) return;
   float4 x = pos[i], v = vel[i];
   if (p.coll != OD_COLL_NONE) collide(p, (uint32_t)i, (uint32_t)ds->step, v);
@@ -399,18 +412,27 @@ __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restric
   sx[i] = x.x; sy[i] = x.y; sz[i] = x.z;
 }
 
+__global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restrict__ dp,
+                                                     const od_dstate* __restrict__ ds,
+                                                     float4* __restrict__ pos,
+                                                     float4* __restrict__ vel,
+                                                     const float4* __restrict__ fhi,
+                                                     const float4* __restrict__ flo,
+                                                     const float* __restrict__ cq,
+                                                     float* __restrict__ sx, float* __restrict__ sy,
+                                                     float* __restrict__ sz) {
+  kick_drift_body(*dp, ds, pos, vel, fhi, flo, cq, sx, sy, sz, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ============================================================== K3: kick + flags
-__global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict__ dp,
-                                                    const float4* __restrict__ pos,
-                                                    float4* __restrict__ vel,
-                                                    const float4* __restrict__ ph,
-                                                    const float4* __restrict__ pl, int jsplit,
-                                                    float4* __restrict__ fhi,
-                                                    float4* __restrict__ flo,
-                                                    uint32_t* __restrict__ flags,
-                                                    const float* __restrict__ cq) {
-  const od_dparams& p = *dp;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // grid covers Npad exactly
+// all 32 lanes of a warp call this (warp ballot); i covers [0, Npad)
+__device__ __forceinline__ void kick_flag_body(const od_dparams& p, const float4* __restrict__ pos,
+                                               float4* __restrict__ vel,
+                                               const float4* __restrict__ ph,
+                                               const float4* __restrict__ pl, int jsplit,
+                                               float4* __restrict__ fhi, float4* __restrict__ flo,
+                                               uint32_t* __restrict__ flags,
+                                               const float* __restrict__ cq, int i) {
   int flag = 0;
   if (i < p.N) {
     float3 hi, lo;
@@ -429,6 +451,19 @@ __global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict
   }
   const uint32_t ballot = __ballot_sync(0xffffffffu, flag);
   if ((threadIdx.x & 31) == 0) flags[i >> 5] = ballot;
+}
+
+__global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict__ dp,
+                                                    const float4* __restrict__ pos,
+                                                    float4* __restrict__ vel,
+                                                    const float4* __restrict__ ph,
+                                                    const float4* __restrict__ pl, int jsplit,
+                                                    float4* __restrict__ fhi,
+                                                    float4* __restrict__ flo,
+                                                    uint32_t* __restrict__ flags,
+                                                    const float* __restrict__ cq) {
+  kick_flag_body(*dp, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq,
+                 blockIdx.x * blockDim.x + threadIdx.x);  // grid covers Npad exactly
 }
 
 __global__ void __launch_bounds__(kBlk) k_flags_only(const od_dparams* __restrict__ dp, int n,
@@ -560,12 +595,11 @@ __device__ void inject_one(const od_dparams& p, uint32_t ion, uint32_t step, flo
   }
 }
 
-__global__ void __launch_bounds__(kCT) k_collect_inject(
-    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ pos,
+__device__ __forceinline__ void collect_inject_body(
+    const od_dparams& p, od_dstate* __restrict__ ds, float4* __restrict__ pos,
     float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
     int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
     float4* __restrict__ list_new, float4* __restrict__ list_v) {
-  const od_dparams& p = *dp;
   const int tid = threadIdx.x;
   const int K = build_list(flags, p.nwords, list);
   if (tid == 0) ds->nlist = K;
@@ -598,6 +632,14 @@ __global__ void __launch_bounds__(kCT) k_collect_inject(
     vel[i] = v;
     list_new[k] = x;
   }
+}
+
+__global__ void __launch_bounds__(kCT) k_collect_inject(
+    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ pos,
+    float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
+    int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
+    float4* __restrict__ list_new, float4* __restrict__ list_v) {
+  collect_inject_body(*dp, ds, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
 }
 
 // list + per-grain counts of a snapshot (no state change)
@@ -638,18 +680,19 @@ __device__ __forceinline__ double block_sum_256(double v, double* s_red) {
   return r;  // valid in thread 0
 }
 
-__global__ void __launch_bounds__(kBlk) k_correct_orbit(
-    const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+// block blk of nb + nrec: blocks [0, nb) correct and sum orbit terms, the rest recompute the
+// re-injected ions' sums
+__device__ __forceinline__ void correct_orbit_body(
+    const od_dparams& p, const od_dstate* __restrict__ ds,
     const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
     const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
     const float4* __restrict__ list_old, const float4* __restrict__ list_new,
-    double* __restrict__ orbit_part, int nb) {
+    double* __restrict__ orbit_part, int nb, int blk, int nrec) {
   __shared__ double s_red[kBlk / 32];
-  const od_dparams& p = *dp;
   const int K = ds->nlist;
   const int tid = threadIdx.x;
-  if ((int)blockIdx.x < nb) {
-    const int i = blockIdx.x * kBlk + tid;
+  if (blk < nb) {
+    const int i = blk * kBlk + tid;
     const bool live = i < p.N;
     const float4 x = live ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     // orbit sums (opendust.py:977-1037): exp(-r)(x_p - x)(1/r^3 + 1/r^2), lambda units
@@ -670,7 +713,7 @@ __global__ void __launch_bounds__(kBlk) k_correct_orbit(
       double sy = block_sum_256(ty, s_red);
       double sz = block_sum_256(tz, s_red);
       if (tid == 0) {
-        double* o = orbit_part + ((size_t)blockIdx.x * p.P + g) * 3;
+        double* o = orbit_part + ((size_t)blk * p.P + g) * 3;
         o[0] = sx; o[1] = sy; o[2] = sz;
       }
     }
@@ -697,9 +740,8 @@ __global__ void __launch_bounds__(kBlk) k_correct_orbit(
   } else {
     // full ion–ion sums of the re-injected ions at their new positions
     __shared__ float s_h[3][kBlk], s_l[3][kBlk];
-    const int nrec = gridDim.x - nb;
     const bool cut = p.method == OD_FORCE_CUTOFF;
-    for (int k = blockIdx.x - nb; k < K; k += nrec) {
+    for (int k = blk - nb; k < K; k += nrec) {
       const int i = list[k];
       const float4 xi = list_new[k];
       float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
@@ -735,6 +777,16 @@ __global__ void __launch_bounds__(kBlk) k_correct_orbit(
       __syncthreads();
     }
   }
+}
+
+__global__ void __launch_bounds__(kBlk) k_correct_orbit(
+    const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+    const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
+    const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
+    const float4* __restrict__ list_old, const float4* __restrict__ list_new,
+    double* __restrict__ orbit_part, int nb) {
+  correct_orbit_body(*dp, ds, pos, fhi, flo, flags, list, list_old, list_new, orbit_part, nb,
+                     blockIdx.x, gridDim.x - nb);
 }
 
 // ============================================================== K6: FP64 host-tail on device
@@ -781,16 +833,14 @@ __device__ void out_domain_force(const od_dparams& p, double x, double y, double
   f[2] = fH;
 }
 
-__global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp,
-                                               od_dstate* __restrict__ ds,
-                                               const double* __restrict__ orbit_part, int nb,
-                                               double* __restrict__ s_q, double* __restrict__ s_orbit,
-                                               double* __restrict__ s_collect,
-                                               double* __restrict__ s_dust,
-                                               double* __restrict__ s_field, float* __restrict__ cq) {
+__device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __restrict__ ds,
+                                          const double* __restrict__ orbit_part, int nb,
+                                          double* __restrict__ s_q, double* __restrict__ s_orbit,
+                                          double* __restrict__ s_collect,
+                                          double* __restrict__ s_dust,
+                                          double* __restrict__ s_field, float* __restrict__ cq) {
   __shared__ double s_red[kBlk];
   __shared__ double S[OD_MAX_GRAINS * 3];
-  const od_dparams& p = *dp;
   const int tid = threadIdx.x;
   const int nc = p.P * 3;
   for (int c = 0; c < nc; c++) {
@@ -853,6 +903,16 @@ __global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp
   ds->step = step + 1;
 }
 
+__global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp,
+                                               od_dstate* __restrict__ ds,
+                                               const double* __restrict__ orbit_part, int nb,
+                                               double* __restrict__ s_q, double* __restrict__ s_orbit,
+                                               double* __restrict__ s_collect,
+                                               double* __restrict__ s_dust,
+                                               double* __restrict__ s_field, float* __restrict__ cq) {
+  tail_body(*dp, ds, orbit_part, nb, s_q, s_orbit, s_collect, s_dust, s_field, cq);
+}
+
 __global__ void k_set_charges(const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
                               float* __restrict__ cq, int P) {
   const int g = threadIdx.x;
@@ -912,16 +972,22 @@ int od_num_sms(int device) {
   return n;
 }
 
+// grid.x limit for timing probes of the autotuner (0 = the full grid)
+static thread_local int g_gridx_limit = 0;
+static inline unsigned gx_of(int full) {
+  return (unsigned)((g_gridx_limit > 0 && g_gridx_limit < full) ? g_gridx_limit : full);
+}
+
 template <int NT, int IPT, int V>
 static void launch_pairs_t(const od_pair_plan& pl, const float4* pos, int Npad, float4* ph,
                            float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
-  dim3 grid(Npad / (NT * IPT), pl.jsplit);
+  dim3 grid(gx_of(Npad / (NT * IPT)), pl.jsplit);
   k_pairs<NT, IPT, V><<<grid, NT, 0, s>>>(pos, Npad, pl.chunk, ph, plo, rho0, err);
 }
 template <int NT, int NEWTON>
 static void launch_pairs_x2(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
                             float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
-  dim3 grid(Npad / (NT * 2), pl.jsplit);
+  dim3 grid(gx_of(Npad / (NT * 2)), pl.jsplit);
   const float nr = 64.0f * rho0;  // Newton (2 steps) keeps 1/s within 2^-24 for r > 64 r0
   k_pairs_x2<NT, NEWTON><<<grid, NT, 0, s>>>(io.sx, io.sy, io.sz, Npad, pl.chunk, ph, plo, rho0,
                                              nr * nr, err);
@@ -946,6 +1012,15 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Np
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+cudaError_t od_launch_pairs_probe(const od_pair_plan& pl, const od_pair_io& io, int Npad,
+                                  int gridx_limit, float4* ph, float4* plo, float rho0,
+                                  uint32_t* err, cudaStream_t s) {
+  g_gridx_limit = gridx_limit;
+  cudaError_t e = od_launch_pairs(pl, io, Npad, ph, plo, rho0, err, s);
+  g_gridx_limit = 0;
+  return e;
 }
 
 cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,
@@ -1111,5 +1186,85 @@ cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, 
                                           rho0, nr * nr, v.err);
   k_static_finish<<<(n + kBlk - 1) / kBlk, kBlk, 0, s>>>(v.part_hi, v.part_lo, n, Npad, jsplit,
                                                         scale, force);
+  return cudaGetLastError();
+}
+
+// ============================================================== batched step
+// Many independent simulations advance together: every stage of the step is one launch for
+// the whole batch. Blocks of the ion-parallel stages look up (simulation, local block) in a
+// table; the all-pairs stage is one persistent launch whose blocks take work items
+// (simulation, 512-target block, source range) from a device counter, largest items first;
+// compaction/re-injection and the FP64 tail run one block per simulation. Each simulation
+// keeps its own buffers, source split and partial slabs, so its results are bitwise the
+// results of the same simulation stepped alone.
+namespace {
+
+__global__ void __launch_bounds__(kBlk) k_b_kick_drift(const od_simdesc* __restrict__ sims,
+                                                       const int2* __restrict__ blk) {
+  const int2 e = blk[blockIdx.x];
+  const od_simdesc& d = sims[e.x];
+  kick_drift_body(*d.dp, d.ds, d.b.pos, d.b.vel, d.b.fhi, d.b.flo, d.b.cq, d.b.sx, d.b.sy, d.b.sz,
+                  e.y * kBlk + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(256) k_b_pairs(const od_simdesc* __restrict__ sims,
+                                                 const int4* __restrict__ items, int nitems,
+                                                 unsigned int* __restrict__ next,
+                                                 uint32_t* __restrict__ err) {
+  __shared__ int s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= nitems) return;
+    const int4 w = items[it];
+    const od_simdesc& d = sims[w.x];
+    const bool ok = pairs_x2_body<256, 0>(d.b.sx, d.b.sy, d.b.sz, w.y, w.z, w.w,
+                                          (size_t)(w.z / d.chunk) * d.Npad, d.b.part_hi,
+                                          d.b.part_lo, d.rho0, d.newton_r2, err);
+    if (!ok) return;
+  }
+}
+
+__global__ void __launch_bounds__(kBlk) k_b_kick_flag(const od_simdesc* __restrict__ sims,
+                                                      const int2* __restrict__ blk) {
+  const int2 e = blk[blockIdx.x];
+  const od_simdesc& d = sims[e.x];
+  kick_flag_body(*d.dp, d.b.pos, d.b.vel, d.b.part_hi, d.b.part_lo, d.jsplit, d.b.fhi, d.b.flo,
+                 d.b.flags, d.b.cq, e.y * kBlk + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(kCT) k_b_collect_inject(const od_simdesc* __restrict__ sims) {
+  const od_simdesc& d = sims[blockIdx.x];
+  collect_inject_body(*d.dp, d.ds, d.b.pos, d.b.vel, d.b.flags, d.b.list, d.b.list_bits,
+                      d.b.list_old, d.b.list_new, d.b.list_v);
+}
+
+__global__ void __launch_bounds__(kBlk) k_b_correct_orbit(const od_simdesc* __restrict__ sims,
+                                                          const int2* __restrict__ blk) {
+  const int2 e = blk[blockIdx.x];
+  const od_simdesc& d = sims[e.x];
+  correct_orbit_body(*d.dp, d.ds, d.b.pos, d.b.fhi, d.b.flo, d.b.flags, d.b.list, d.b.list_old,
+                     d.b.list_new, d.b.orbit_part, d.nb, e.y, d.nrec);
+}
+
+__global__ void __launch_bounds__(kBlk) k_b_tail(const od_simdesc* __restrict__ sims) {
+  const od_simdesc& d = sims[blockIdx.x];
+  tail_body(*d.dp, d.ds, d.b.orbit_part, d.nb, d.b.s_q, d.b.s_orbit, d.b.s_collect, d.b.s_dust,
+            d.b.s_field, d.b.cq);
+}
+
+}  // namespace
+
+cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s) {
+  k_b_kick_drift<<<v.nblk_ion, kBlk, 0, s>>>(v.sims, v.blk_ion);
+  cudaError_t e = cudaMemsetAsync(v.next, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  k_b_pairs<<<v.pair_grid, 256, 0, s>>>(v.sims, v.items, v.nitems, v.next, v.err);
+  k_b_kick_flag<<<v.nblk_ion, kBlk, 0, s>>>(v.sims, v.blk_ion);
+  k_b_collect_inject<<<v.nsims, kCT, 0, s>>>(v.sims);
+  k_b_correct_orbit<<<v.nblk_corr, kBlk, 0, s>>>(v.sims, v.blk_corr);
+  k_b_tail<<<v.nsims, kBlk, 0, s>>>(v.sims);
   return cudaGetLastError();
 }

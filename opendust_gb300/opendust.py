@@ -171,9 +171,10 @@ def parse_device_index(deviceIndex) -> int:
 def build_simulation(plasma, sim, dustParticles, distributionType, *, cutOff=False,
                      cutoff_distance=None, switch_distance=None, collisions=None,
                      mean_free_path=None, seed=0, avg_start=None, sim_id=0, trap=None,
-                     device=0, n_steps=None):
+                     device=0, n_steps=None, injection=None):
     """od_config for one simulation plus the host-side setup products.
 
+    injection: precomputed (tables, probs) of setup_host.injection_setup, or None.
     trap: None -> Monte-Carlo grid on the GPU (od_trap_potential) + host least squares;
           an array of 15 coefficients -> used as alpha;
           a callable (Rh, Hh, n_r, n_h, n_points, seed) -> potential grid.
@@ -183,7 +184,9 @@ def build_simulation(plasma, sim, dustParticles, distributionType, *, cutOff=Fal
     if distributionType not in ("Maxwellian", "fieldDriven"):
         raise ValueError("distributionType must be 'Maxwellian' or 'fieldDriven'")
     dist = _lib.OD_DIST_MAXWELLIAN if distributionType == "Maxwellian" else _lib.OD_DIST_FIELD_DRIVEN
-    tables, probs = sh.injection_setup(plasma.v_fl, plasma.v_T, sim.R, sim.H, distributionType)
+    if injection is None:
+        injection = sh.injection_setup(plasma.v_fl, plasma.v_T, sim.R, sim.H, distributionType)
+    tables, probs = injection
     Rh, Hh, n_r, n_h, n_points = sh.trap_grid(sim.R, sim.H, plasma.r_D_e)
     trap_seed = (int(seed) * 0x9E3779B97F4A7C15 + 0x51) & 0xFFFFFFFFFFFFFFFF
     if trap is None:

@@ -166,3 +166,18 @@ def test_time_averages(gpu_lib):
     print(f"time averages: q rel {dq:.3e}, orbit rel {do:.3e}")
     assert dq < 0.01
     assert do < 0.01
+
+
+def test_autotune_picks_a_correct_plan(gpu_lib):
+    holder, pos, vel, plasma, *_ = case(N=2**16, n=4, seed=41)
+    with _lib.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        rate = eng.autotune(use_cache=False)
+        plan = eng.pair_plan()
+        f = eng.force_snapshot(pos)
+        eng.step(2)
+    print(f"autotuned plan {plan}, {rate:.3e} pairs/s")
+    assert rate > 1e11
+    idx = np.arange(0, 2**16, 64)
+    ref = oracle.force_targets(holder, pos, idx, round32=True)
+    assert rel_err_per_ion(f[idx], ref).max() <= 1e-5
