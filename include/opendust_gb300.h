@@ -84,7 +84,11 @@ enum {
   OD_RNG_BOT_X = 9,      /* as TOP_X */
   OD_RNG_SIDE_X = 10,    /* w0 -> angle fraction, w1 -> axial fraction */
   OD_RNG_SIDE_V = 11,    /* gauss(w0,w1) -> (gy,gz), w2 -> u for side (and v_z) tables */
-  OD_RNG_TRAP = 13       /* trap-fit sample point p: counter (p,0,13,0); w0 radius^2, w1 angle, w2 axial */
+  OD_RNG_TRAP = 13,      /* trap-fit sample point p: counter (p,0,13,0); w0 radius^2, w1 angle, w2 axial */
+  OD_RNG_INIT_X = 14,    /* initial position of ion i, attempt a: counter (i,a,14,sim); w0 radius^2,
+                            w1 angle, w2 axial */
+  OD_RNG_INIT_V = 15     /* initial velocity of ion i: counter (i,0,15,sim): gauss(w0,w1) -> (gx,gy),
+                            gauss(w2,w3).cos -> gz; counter (i,1,15,sim) w0 -> u for the v_z table */
 };
 
 #define OD_MAX_GRAINS 16
@@ -160,6 +164,15 @@ const char* od_last_error(const od_handle* h);
 /* Replaces context.setPositions / setVelocities (opendust.py:1043-1044) and the
  * restart-file read (opendust.py:452-466). pos [m], vel [m/s], both n x 3 row-major. */
 od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n);
+
+/* Samples the initial ion state on the device (replaces the host loops of opendust.py:373-451):
+ * positions uniform in the cylinder and outside every grain (rejection, inclusive grain
+ * surface as in the reference), velocities N(0, v_T) across and N(v_fl, v_T) along the axis
+ * (Maxwellian), or, for field-driven plasmas, v_z from the piecewise-linear inverse CDF given by
+ * nodes vz_v [m/s] / vz_cdf (vz_n >= 2; the table of opendust.py:405-448). Random numbers:
+ * streams OD_RNG_INIT_X / OD_RNG_INIT_V with the configuration's seed. Then computes the
+ * ion–ion sums like od_set_state. */
+od_status od_init_state(od_handle* h, const double* vz_v, const double* vz_cdf, int32_t vz_n);
 
 /* Replaces context.getState(...).getPositions/getVelocities (opendust.py:1074-1078, :1102-1105). */
 od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n);

@@ -123,6 +123,7 @@ def load(path: str | None = None):
         "od_last_error": (c_char_p, [H]),
         "od_set_state": (c_int32, [H, _DP, _DP, c_int64]),
         "od_get_state": (c_int32, [H, _DP, _DP, c_int64]),
+        "od_init_state": (c_int32, [H, _DP, _DP, c_int32]),
         "od_step": (c_int32, [H, c_int64]),
         "od_step_index": (c_int64, [H]),
         "od_get_series": (c_int32, [H, c_int64, c_int64, _DP, _DP, _DP, _DP, _DP]),
@@ -299,6 +300,15 @@ class Engine:
         pos = np.ascontiguousarray(pos, dtype=np.float64)
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         check(self._lib.od_set_state(self.h, _dptr(pos), _dptr(vel), pos.shape[0]), self.h)
+
+    def init_state(self, vz_table=None):
+        """Sample the initial state on the device; vz_table = (v [m/s], cdf) for field-driven."""
+        if vz_table is None:
+            check(self._lib.od_init_state(self.h, None, None, 0), self.h)
+        else:
+            v = np.ascontiguousarray(vz_table[0], dtype=np.float64)
+            x = np.ascontiguousarray(vz_table[1], dtype=np.float64)
+            check(self._lib.od_init_state(self.h, _dptr(v), _dptr(x), len(v)), self.h)
 
     def get_state(self):
         pos = np.empty((self.n, 3))

@@ -447,6 +447,39 @@ extern "C" od_status od_set_state(od_handle* h, const double* pos, const double*
   return check_device_err(h);
 }
 
+extern "C" od_status od_init_state(od_handle* h, const double* vz_v, const double* vz_cdf,
+                                   int32_t vz_n) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (vz_n != 0 && (vz_n < 2 || !vz_v || !vz_cdf))
+    return fail(h, OD_ERR_INVALID, "the v_z table needs at least 2 nodes");
+  if (h->cfg.distribution == OD_DIST_FIELD_DRIVEN && vz_n < 2)
+    return fail(h, OD_ERR_INVALID, "field-driven initial states need the v_z table");
+  OD_CK(h, cudaSetDevice(h->device));
+  float* d_v = nullptr;
+  double* d_x = nullptr;
+  if (vz_n >= 2) {
+    std::vector<float> v(vz_n);
+    for (int k = 0; k < vz_n; k++) v[k] = (float)(vz_v[k] / h->hp.vunit);
+    OD_CK(h, cudaMalloc(&d_v, sizeof(float) * vz_n));
+    OD_CK(h, cudaMalloc(&d_x, sizeof(double) * vz_n));
+    OD_CK(h, cudaMemcpy(d_v, v.data(), sizeof(float) * vz_n, cudaMemcpyHostToDevice));
+    OD_CK(h, cudaMemcpy(d_x, vz_cdf, sizeof(double) * vz_n, cudaMemcpyHostToDevice));
+  }
+  cudaError_t e = od_launch_init_state(h->dp, h->N, h->b.pos, h->b.vel, d_v, d_x, vz_n,
+                                       &h->ds->err, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (d_v) cudaFree(d_v);
+  if (d_x) cudaFree(d_x);
+  if (e != cudaSuccess) return cuda_fail(h, e, "od_init_state");
+  od_status st = refresh_forces(h);
+  if (st != OD_OK) return st;
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->state_set = true;
+  st = check_device_err(h);
+  if (st == OD_ERR_STATE) return fail(h, OD_ERR_STATE, "no position outside the grains was found");
+  return st;
+}
+
 extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");

@@ -94,6 +94,9 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Np
 cudaError_t od_launch_pairs_probe(const od_pair_plan& pl, const od_pair_io& io, int Npad,
                                   int gridx_limit, float4* part_hi, float4* part_lo, float rho0,
                                   uint32_t* err, cudaStream_t s);
+cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* pos, float4* vel,
+                                 const float* vz_v, const double* vz_cdf, int vz_n, uint32_t* err,
+                                 cudaStream_t s);
 cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,
                                  cudaStream_t s);
 cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const float4* part_hi,

@@ -963,7 +963,60 @@ __global__ void __launch_bounds__(kBlk) k_trap(double Rh, double Hh, int n_r, in
   if (node < nn) part[(size_t)blockIdx.y * nn + node] = acc;
 }
 
+// ============================================================== initial state on the device
+// opendust.py:373-451: rejection sampling of uniform positions in the cylinder outside every
+// grain, Maxwellian (or tabulated field-driven v_z) velocities; Philox streams INIT_X / INIT_V.
+__global__ void __launch_bounds__(kBlk) k_init_state(const od_dparams* __restrict__ dp,
+                                                     float4* __restrict__ pos,
+                                                     float4* __restrict__ vel,
+                                                     const float* __restrict__ vz_v,
+                                                     const double* __restrict__ vz_cdf, int vz_n,
+                                                     uint32_t* __restrict__ err) {
+  const od_dparams& p = *dp;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.N) return;
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool ok = false;
+  for (uint32_t a = 0; a < 256 && !ok; a++) {
+    const od_u4 w = od_draw(p, (uint32_t)i, a, OD_RNG_INIT_X);
+    const float r = p.Rh * sqrtf(od_u01(w.x));
+    float s, c;
+    sincospif(2.0f * od_u01(w.y), &s, &c);
+    x = make_float4(r * c, r * s, p.Hh * od_u01(w.z) - p.Hh_half, 0.f);
+    ok = true;
+    for (int g = 0; g < p.P; g++) {
+      const float dx = (x.x - p.gxh[g]) - p.gxl[g], dy = (x.y - p.gyh[g]) - p.gyl[g],
+                  dz = (x.z - p.gzh[g]) - p.gzl[g];
+      if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= p.gr2f[g]) ok = false;
+    }
+  }
+  if (!ok) atomicOr(err, OD_DERR_LIST);
+  const od_u4 w = od_draw(p, (uint32_t)i, 0u, OD_RNG_INIT_V);
+  float gx, gy, gz, dummy;
+  od_gauss2(w.x, w.y, gx, gy);
+  od_gauss2(w.z, w.w, gz, dummy);
+  float vz;
+  if (vz_n >= 2) {
+    const float u = od_u01(od_draw(p, (uint32_t)i, 1u, OD_RNG_INIT_V).x);
+    int k = 1;
+    while (k < vz_n - 1 && (double)u > vz_cdf[k]) k++;
+    const float x0 = (float)vz_cdf[k - 1], x1 = (float)vz_cdf[k];
+    vz = vz_v[k - 1] + (u - x0) * (vz_v[k] - vz_v[k - 1]) / fmaxf(x1 - x0, 1e-30f);
+  } else {
+    vz = fmaf(p.vT, gz, p.vfl);
+  }
+  pos[i] = x;
+  vel[i] = make_float4(p.vT * gx, p.vT * gy, vz, 0.f);
+}
+
 }  // namespace
+
+cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* pos, float4* vel,
+                                 const float* vz_v, const double* vz_cdf, int vz_n, uint32_t* err,
+                                 cudaStream_t s) {
+  k_init_state<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, pos, vel, vz_v, vz_cdf, vz_n, err);
+  return cudaGetLastError();
+}
 
 // ============================================================== launch wrappers
 int od_num_sms(int device) {

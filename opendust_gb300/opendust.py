@@ -290,9 +290,11 @@ class OpenDust:
 
     def simulate(self, deviceIndex="0", cutOff=False, toRestartFileName="", *, seed=0,
                  collisions=None, mean_free_path=None, cutoff_distance=None,
-                 switch_distance=None, avg_start=None, quiet=False):
+                 switch_distance=None, avg_start=None, quiet=False, init="device"):
         """Run n steps on one GPU (opendust.py:362-1383). Returns (q, forces): q has shape
-        (n, P); forces is a dict of (n, P, 3) arrays "orbit", "collect", "dust", "field"."""
+        (n, P); forces is a dict of (n, P, 3) arrays "orbit", "collect", "dust", "field".
+        init: "device" samples the initial ions on the GPU (od_init_state), "host" with numpy
+        (setup_host.initial_state); a restart file overrides both."""
         plasma = self.plasmaParametersInSIUnits
         sim = self.simulationParametersInSIUnits
         out = self.outputParameters
@@ -303,15 +305,21 @@ class OpenDust:
             collisions=collisions, mean_free_path=mean_free_path, seed=seed,
             avg_start=avg_start, device=device)
         self.alphaTrap = info["alpha"]
-        if toRestartFileName == "":
+        pos = vel = None
+        if toRestartFileName != "":
+            pos, vel = sh.read_restart(toRestartFileName, self.N)
+        elif init == "host":
             grains = [(g.x, g.y, g.z, g.r) for g in self._inputParticles]
             pos, vel = sh.initial_state(self.N, sim.R, sim.H, grains, plasma.v_fl, plasma.v_T,
                                         self.distributionType, seed)
-        else:
-            pos, vel = sh.read_restart(toRestartFileName, self.N)
         eng = _lib.Engine(holder, device)
         try:
-            eng.set_state(pos, vel)
+            if pos is not None:
+                eng.set_state(pos, vel)
+            elif self.distributionType == "fieldDriven":
+                eng.init_state(sh.field_driven_vz_table(plasma.v_fl, plasma.v_T))
+            else:
+                eng.init_state()
             self._run_loop(eng, out, plasma, quiet)
             ser = eng.series(0, self.n)
             self.averages, _ = eng.averages()

@@ -166,8 +166,8 @@ def fit_trap(pot: np.ndarray, Rh: float, Hh: float, n_superions: int) -> np.ndar
     return -np.linalg.lstsq(A, pot.flatten(), rcond=None)[0] * n_superions
 
 
-def field_driven_vz(v_fl: float, v_T: float, u: np.ndarray) -> np.ndarray:
-    """Initial field-driven v_z by inverse CDF (opendust.py:405-448); speeds in m/s."""
+def field_driven_vz_table(v_fl: float, v_T: float):
+    """Nodes (v [m/s], CDF) of the initial field-driven v_z distribution (opendust.py:405-433)."""
     v_max = abs(v_fl) * 8 + 5 * v_T
     v_min = -4 * v_T
     n_v = int((v_max - v_min) / (0.2 * v_T))
@@ -175,6 +175,12 @@ def field_driven_vz(v_fl: float, v_T: float, u: np.ndarray) -> np.ndarray:
     f = _flux_field(v_fl, v_T, weight_v=False)
     F_max = integrate.quad(f, v_min, v_max)[0]
     xi = np.array([integrate.quad(f, v_min, x)[0] / F_max for x in v])
+    return v, xi
+
+
+def field_driven_vz(v_fl: float, v_T: float, u: np.ndarray) -> np.ndarray:
+    """Initial field-driven v_z by inverse CDF (opendust.py:405-448); speeds in m/s."""
+    v, xi = field_driven_vz_table(v_fl, v_T)
     return interp1d(xi, v)(u)
 
 
