@@ -198,7 +198,10 @@ od_status od_set_graph(od_handle* h, int32_t enable);
 /* Work decomposition of the all-pairs force kernel (OpenMM picks its own nonbonded
  * kernel configuration; this exposes ours). variant 0: shared-memory broadcast of each
  * source, 1: warp-shuffle broadcast, 2: packed f32x2 pair arithmetic on SoA tiles (two
- * targets per thread), 3: as 2 with Newton reciprocals for half of the targets.
+ * targets per thread), 3: as 2 with Newton reciprocals for half of the targets (tile redone on
+ * the SFU when a pair is too close), 4: as 3 with a warp-vote SFU fallback per pair,
+ * 5: packed with one target per thread (targets_per_thread 1), 6: as 5 with every other source
+ * pair on the Newton path of variant 4.
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);

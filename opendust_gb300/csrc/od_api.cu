@@ -212,11 +212,12 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->n_steps = c->n_steps; p->avg_start = c->avg_start;
 }
 
-// Default all-pairs plan: packed f32x2 arithmetic on SoA tiles (fastest variant measured on
-// GB300 from 2^16 to 2^20 ions), with enough source chunks for several waves on every SM.
+// Default all-pairs plan: packed f32x2 arithmetic on SoA tiles with one target per thread
+// (variant 5, the fastest measured on GB300 from 2^16 to 2^20 ions), with enough source chunks
+// for several waves on every SM.
 static od_pair_plan default_plan(int Npad, int sms) {
   od_pair_plan pl{};
-  pl.nt = 256; pl.ipt = 2; pl.variant = 2;
+  pl.nt = 256; pl.ipt = 1; pl.variant = 5;
   const int nbx = Npad / (pl.nt * pl.ipt);
   const int target = std::max(1, sms * 8 * 4);
   int js = std::max(1, (target + nbx - 1) / nbx);
@@ -250,7 +251,7 @@ static void free_all(od_handle* h) {
                   h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
                   h->b.sx, h->b.sy, h->b.sz, h->cut.cell_of, h->cut.count, h->cut.fill,
                   h->cut.start, h->cut.chunk_prefix, h->cut.perm, h->cut.ox, h->cut.oy, h->cut.oz,
-                  h->cut.stencil, h->d_pairs};
+                  h->cut.stencil, h->d_pairs, h->cut.chunk_prefix2};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -353,6 +354,8 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
     OD_CKC(dalloc(&h->cut.fill, nc));
     OD_CKC(dalloc(&h->cut.start, nc + 1));
     OD_CKC(dalloc(&h->cut.chunk_prefix, nc + 1));
+    OD_CKC(dalloc(&h->cut.chunk_prefix2, nc + 1));
+    h->cut.packed = true;
     OD_CKC(dalloc(&h->cut.perm, h->cut.cap));
     OD_CKC(dalloc(&h->cut.ox, h->cut.cap));
     OD_CKC(dalloc(&h->cut.oy, h->cut.cap));
@@ -626,7 +629,8 @@ static bool plan_supported(int nt, int ipt, int variant) {
   const int key = nt * 100 + ipt * 10 + variant;
   switch (key) {
     case 12810: case 12820: case 25610: case 25620: case 12811: case 25611: case 25621:
-    case 12822: case 25622: case 12823: case 25623:
+    case 12822: case 25622: case 12823: case 25623: case 12824: case 25624:
+    case 12815: case 25615: case 12816: case 25616:
       return true;
     default:
       return false;
@@ -636,6 +640,14 @@ static bool plan_supported(int nt, int ipt, int variant) {
 extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                                       int32_t variant, int32_t jsplit) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (h->has_cut) {
+    // cutoff method: variant 0 selects the scalar pair kernel, 2 the packed one
+    if (variant != 0 && variant != 2) return fail(h, OD_ERR_INVALID, "cutoff variants are 0 and 2");
+    h->cut.packed = variant == 2;
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+    if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+    return OD_OK;
+  }
   if (!plan_supported(threads, targets_per_thread, variant))
     return fail(h, OD_ERR_INVALID, "unsupported (threads, targets_per_thread, variant)");
   if (h->Npad % (threads * targets_per_thread) != 0)
@@ -685,7 +697,8 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
   }
   OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
   const int shapes[][3] = {{256, 1, 0}, {128, 1, 0}, {256, 1, 1}, {128, 2, 2}, {256, 2, 2},
-                           {128, 2, 3}, {256, 2, 3}};
+                           {128, 2, 3}, {256, 2, 3}, {128, 2, 4}, {256, 2, 4},
+                           {128, 1, 5}, {256, 1, 5}, {128, 1, 6}, {256, 1, 6}};
   const int sms = od_num_sms(h->device);
   cudaEvent_t e0, e1;
   OD_CK(h, cudaEventCreate(&e0));
@@ -1043,8 +1056,8 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
   od_handle* h = nullptr;
   od_status st = od_create(cfg, b->device, &h);
   if (st != OD_OK) return bfail(b, st, g_err);
-  if (h->plan.variant != 2 || h->plan.nt != 256 || h->plan.ipt != 2) {
-    st = od_set_pair_plan(h, 256, 2, 2, 0);
+  if (h->plan.variant != 5 || h->plan.nt != 256 || h->plan.ipt != 1) {
+    st = od_set_pair_plan(h, 256, 1, 5, 0);
     if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
   }
   st = od_set_state(h, pos, vel, cfg->n_ions);
@@ -1112,7 +1125,7 @@ static od_status batch_rebuild(od_batch* b) {
     sims.push_back(d);
     for (int lb = 0; lb < d.nb; lb++) blk_ion.push_back(make_int2(m, lb));
     for (int lb = 0; lb < d.nb + d.nrec; lb++) blk_corr.push_back(make_int2(m, lb));
-    for (int ib = 0; ib < d.Npad / 512; ib++)
+    for (int ib = 0; ib < d.Npad / 256; ib++)
       for (int js = 0; js < d.jsplit; js++) {
         const int j0 = js * d.chunk, j1 = std::min(j0 + d.chunk, d.Npad);
         if (j1 > j0) items.push_back({make_int4(m, ib, j0, j1), (long long)(j1 - j0)});

@@ -108,6 +108,34 @@ __device__ __forceinline__ float od_ex2(float x) {
 }
 #define OD_NLOG2E (-1.4426950408889634f)
 
+// ------------------------------------------------------------------ packed f32x2 arithmetic
+// Blackwell executes two FP32 lanes per instruction with the f32x2 forms of add/sub/mul/fma.
+typedef unsigned long long od_u64;
+__device__ __forceinline__ od_u64 p2(float lo, float hi) {
+  od_u64 r; asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi)); return r;
+}
+__device__ __forceinline__ float2 up2(od_u64 v) {
+  float2 r; asm("mov.b64 {%0,%1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v)); return r;
+}
+__device__ __forceinline__ od_u64 fma2(od_u64 a, od_u64 b, od_u64 c) {
+  od_u64 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d;
+}
+__device__ __forceinline__ od_u64 add2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+__device__ __forceinline__ od_u64 sub2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+__device__ __forceinline__ od_u64 mul2(od_u64 a, od_u64 b) {
+  od_u64 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
+}
+
+
+__device__ __forceinline__ float sum2(od_u64 v) {
+  const float2 f = up2(v);
+  return f.x + f.y;
+}
+
 // ------------------------------------------------------------------ two-float sums
 // Knuth TwoSum: hi + lo == a + b exactly.
 __device__ __forceinline__ void od_two_sum(float a, float b, float& s, float& e) {

@@ -250,6 +250,179 @@ __global__ void __launch_bounds__(kTgt) k_pairs_cut(od_cellgeom g, const int32_t
   }
 }
 
+// ------------------------------------------------------------------ packed variant
+// Two targets per thread, two sources per packed f32x2 operation (as the all-pairs kernel).
+// With switching, (1 - x) is clamped at 0, which makes S and S' vanish beyond r_c, so pairs
+// outside the cutoff contribute exactly 0 without a separate mask.
+constexpr int kTgt2 = 256;  // targets per block (128 threads x 2)
+
+struct cut_pk {
+  od_u64 eps, rho, nl2e, one, three, six, invw, nrsw, m30w;
+  float rc2;
+};
+
+template <bool SWITCH, bool COUNT>
+__device__ __forceinline__ void pair2_cut(const cut_pk& k, od_u64 X, od_u64 Y, od_u64 Z, od_u64 QX,
+                                          od_u64 QY, od_u64 QZ, od_u64& AX, od_u64& AY, od_u64& AZ,
+                                          unsigned int& cnt) {
+  const od_u64 DX = sub2(X, QX), DY = sub2(Y, QY), DZ = sub2(Z, QZ);
+  od_u64 R2 = fma2(DX, DX, k.eps);
+  R2 = fma2(DY, DY, R2);
+  R2 = fma2(DZ, DZ, R2);
+  const float2 r2 = up2(R2);
+  const od_u64 RI = p2(od_rsqrt(r2.x), od_rsqrt(r2.y));
+  const od_u64 R = mul2(R2, RI);
+  const float2 s = up2(add2(R, k.rho));
+  const od_u64 SI = p2(od_rcp(s.x), od_rcp(s.y));
+  const float2 ea = up2(mul2(R, k.nl2e));
+  const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
+  od_u64 F = mul2(EX, fma2(SI, SI, SI));
+  od_u64 C;
+  if (SWITCH) {
+    const float2 xx = up2(fma2(R, k.invw, k.nrsw));
+    const od_u64 X2 = p2(fmaxf(xx.x, 0.f), fmaxf(xx.y, 0.f));
+    const float2 om = up2(sub2(k.one, X2));
+    const od_u64 OM = p2(fmaxf(om.x, 0.f), fmaxf(om.y, 0.f));
+    const od_u64 S = mul2(mul2(OM, OM), mul2(OM, fma2(X2, fma2(k.six, X2, k.three), k.one)));
+    const od_u64 Q = mul2(X2, OM);
+    const od_u64 DS = mul2(mul2(Q, Q), k.m30w);
+    F = sub2(mul2(F, S), mul2(mul2(EX, SI), DS));
+    C = mul2(F, RI);
+  } else {
+    const float2 c = up2(mul2(F, RI));
+    C = p2(r2.x < k.rc2 ? c.x : 0.f, r2.y < k.rc2 ? c.y : 0.f);
+  }
+  if (COUNT) cnt += (r2.x < k.rc2) + (r2.y < k.rc2);
+  AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
+}
+
+template <bool SWITCH, bool COUNT>
+__global__ void __launch_bounds__(128) k_pairs_cut_x2(od_cellgeom g, const int32_t* __restrict__ count,
+                                                      const int32_t* __restrict__ start,
+                                                      const int32_t* __restrict__ chunk_prefix,
+                                                      const int32_t* __restrict__ perm,
+                                                      const float* __restrict__ ox,
+                                                      const float* __restrict__ oy,
+                                                      const float* __restrict__ oz,
+                                                      const int4* __restrict__ stencil, int nstencil,
+                                                      float4* __restrict__ part_hi,
+                                                      float4* __restrict__ part_lo, float rho0,
+                                                      float rc2, float rs, float inv_w,
+                                                      unsigned long long* __restrict__ pair_count) {
+  __shared__ __align__(16) float tx[OD_TJ], ty[OD_TJ], tz[OD_TJ];
+  const int b = blockIdx.x;
+  const int total = chunk_prefix[g.ncells];
+  if (b >= total) return;
+  int lo = 0, hi = g.ncells - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunk_prefix[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const int cell = lo;
+  const int chunk = b - chunk_prefix[cell];
+  const int n_cell = count[cell];
+  const int t0 = chunk * kTgt2 + threadIdx.x, t1 = t0 + kTgt2 / 2;
+  const bool live0 = t0 < n_cell, live1 = t1 < n_cell;
+  const int slot0 = start[cell] + (live0 ? t0 : 0), slot1 = start[cell] + (live1 ? t1 : 0);
+  const float ax0 = ox[slot0], ay0 = oy[slot0], az0 = oz[slot0];
+  const float ax1 = ox[slot1], ay1 = oy[slot1], az1 = oz[slot1];
+  const int cx = cell % g.gx, cy = (cell / g.gx) % g.gy, cz = cell / (g.gx * g.gy);
+  cut_pk k;
+  k.eps = p2(1e-30f, 1e-30f); k.rho = p2(rho0, rho0); k.nl2e = p2(OD_NLOG2E, OD_NLOG2E);
+  k.one = p2(1.f, 1.f); k.three = p2(3.f, 3.f); k.six = p2(6.f, 6.f);
+  k.invw = p2(inv_w, inv_w); k.nrsw = p2(-rs * inv_w, -rs * inv_w);
+  k.m30w = p2(-30.f * inv_w, -30.f * inv_w); k.rc2 = rc2;
+  float h0x = 0.f, h0y = 0.f, h0z = 0.f, l0x = 0.f, l0y = 0.f, l0z = 0.f;
+  float h1x = 0.f, h1y = 0.f, h1z = 0.f, l1x = 0.f, l1y = 0.f, l1z = 0.f;
+  unsigned int c0 = 0, c1 = 0;
+  for (int st = 0; st < nstencil; st++) {
+    const int4 d = stencil[st];
+    const int sx = cx + d.x, sy = cy + d.y, sz = cz + d.z;
+    if (sx < 0 || sy < 0 || sz < 0 || sx >= g.gx || sy >= g.gy || sz >= g.gz) continue;
+    const int sc = (sz * g.gy + sy) * g.gx + sx;
+    const int s0 = start[sc], s1 = start[sc + 1];
+    if (s1 == s0) continue;
+    const float fx = (float)(-d.x) * g.c, fy = (float)(-d.y) * g.c, fz = (float)(-d.z) * g.c;
+    const float px0 = ax0 + fx, py0 = ay0 + fy, pz0 = az0 + fz;
+    const float px1 = ax1 + fx, py1 = ay1 + fy, pz1 = az1 + fz;
+    const od_u64 X0 = p2(px0, px0), Y0 = p2(py0, py0), Z0 = p2(pz0, pz0);
+    const od_u64 X1 = p2(px1, px1), Y1 = p2(py1, py1), Z1 = p2(pz1, pz1);
+    for (int j0 = s0; j0 < s1; j0 += OD_TJ) {
+      const int nt = min(OD_TJ, s1 - j0);  // a multiple of 8 (segments are 8-padded)
+      __syncthreads();
+      for (int q = threadIdx.x; q < nt; q += kTgt2 / 2) {
+        tx[q] = ox[j0 + q]; ty[q] = oy[j0 + q]; tz[q] = oz[j0 + q];
+      }
+      __syncthreads();
+      od_u64 A0x = 0, A0y = 0, A0z = 0, A1x = 0, A1y = 0, A1z = 0;
+#pragma unroll 2
+      for (int j = 0; j < nt; j += 4) {
+        const ulonglong2 qx = *reinterpret_cast<const ulonglong2*>(&tx[j]);
+        const ulonglong2 qy = *reinterpret_cast<const ulonglong2*>(&ty[j]);
+        const ulonglong2 qz = *reinterpret_cast<const ulonglong2*>(&tz[j]);
+        pair2_cut<SWITCH, COUNT>(k, X0, Y0, Z0, qx.x, qy.x, qz.x, A0x, A0y, A0z, c0);
+        pair2_cut<SWITCH, COUNT>(k, X0, Y0, Z0, qx.y, qy.y, qz.y, A0x, A0y, A0z, c0);
+        pair2_cut<SWITCH, COUNT>(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z, c1);
+        pair2_cut<SWITCH, COUNT>(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z, c1);
+      }
+      od_acc2(h0x, l0x, sum2(A0x)); od_acc2(h0y, l0y, sum2(A0y)); od_acc2(h0z, l0z, sum2(A0z));
+      od_acc2(h1x, l1x, sum2(A1x)); od_acc2(h1y, l1y, sum2(A1y)); od_acc2(h1z, l1z, sum2(A1z));
+    }
+  }
+  if (live0) {
+    const int i = perm[slot0];
+    part_hi[i] = make_float4(h0x, h0y, h0z, 0.f);
+    part_lo[i] = make_float4(l0x, l0y, l0z, 0.f);
+  }
+  if (live1) {
+    const int i = perm[slot1];
+    part_hi[i] = make_float4(h1x, h1y, h1z, 0.f);
+    part_lo[i] = make_float4(l1x, l1y, l1z, 0.f);
+  }
+  if (COUNT) {
+    unsigned int v = (live0 ? c0 - 1u : 0u) + (live1 ? c1 - 1u : 0u);  // self pairs excluded
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(pair_count, (unsigned long long)v);
+  }
+}
+
+__global__ void k_chunks2(int ncells, const int32_t* __restrict__ count,
+                          int32_t* __restrict__ chunk_prefix2) {
+  // exclusive prefix of ceil(count / kTgt2), one 1024-thread block
+  __shared__ int s_w[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (ncells + 1023) / 1024;
+  const int c0 = min(tid * per, ncells), c1 = min(c0 + per, ncells);
+  int a = 0;
+  for (int c = c0; c < c1; c++) a += (count[c] + kTgt2 - 1) / kTgt2;
+  int ia = a;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, ia, o);
+    if (lane >= o) ia += y;
+  }
+  if (lane == 31) s_w[wid] = ia;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = s_w[lane];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    s_w[lane] = x - v;
+  }
+  __syncthreads();
+  int off = s_w[wid] + ia - a;
+  for (int c = c0; c < c1; c++) {
+    chunk_prefix2[c] = off;
+    off += (count[c] + kTgt2 - 1) / kTgt2;
+  }
+  if (tid == 1023) chunk_prefix2[ncells] = off;
+}
+
 }  // namespace
 
 cudaError_t od_launch_cutoff(const od_cutlist& L, const float4* pos, int n, int Npad,
@@ -261,9 +434,22 @@ cudaError_t od_launch_cutoff(const od_cutlist& L, const float4* pos, int n, int 
   k_cells_scan<<<1, 1024, 0, s>>>(g.ncells, L.count, L.start, L.chunk_prefix, err);
   k_cells_scatter<<<(n + kBlk - 1) / kBlk, kBlk, 0, s>>>(n, L.cell_of, L.start, L.fill, L.perm);
   k_cells_sort<<<g.ncells, kBlk, 0, s>>>(g, pos, L.count, L.start, L.perm, L.ox, L.oy, L.oz);
-  const int blocks = (n + kTgt - 1) / kTgt + g.ncells;
   const bool sw = rs < rc;
   const float inv_w = sw ? 1.0f / (rc - rs) : 0.0f;
+  if (L.packed) {
+    k_chunks2<<<1, 1024, 0, s>>>(g.ncells, L.count, L.chunk_prefix2);
+    const int blocks2 = (n + kTgt2 - 1) / kTgt2 + g.ncells;
+#define OD_CUT2(SW, CNT)                                                                        \
+  k_pairs_cut_x2<SW, CNT><<<blocks2, kTgt2 / 2, 0, s>>>(g, L.count, L.start, L.chunk_prefix2,   \
+                                                         L.perm, L.ox, L.oy, L.oz, L.stencil,   \
+                                                         L.nstencil, part_hi, part_lo, rho0,    \
+                                                         rc * rc, rs, inv_w, pair_count)
+    if (sw) { if (pair_count) OD_CUT2(true, true); else OD_CUT2(true, false); }
+    else { if (pair_count) OD_CUT2(false, true); else OD_CUT2(false, false); }
+#undef OD_CUT2
+    return cudaGetLastError();
+  }
+  const int blocks = (n + kTgt - 1) / kTgt + g.ncells;
   if (sw)
     k_pairs_cut<true><<<blocks, kTgt, 0, s>>>(g, L.count, L.start, L.chunk_prefix, L.perm, L.ox, L.oy,
                                               L.oz, L.stencil, L.nstencil, Npad, part_hi, part_lo,

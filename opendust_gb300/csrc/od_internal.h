@@ -50,7 +50,7 @@ struct od_batchview {
   int nsims;
   const int2* blk_ion;   // (member, local 256-ion block) for the ion-parallel stages
   int nblk_ion;
-  const int4* items;     // (member, 512-target block, j0, j1) all-pairs work items
+  const int4* items;     // (member, 256-target block, j0, j1) all-pairs work items
   int nitems;
   const int2* blk_corr;  // (member, local block in [0, nb + nrec)) for correction/orbit sums
   int nblk_corr;
@@ -73,6 +73,8 @@ struct od_cutlist {
   float *ox, *oy, *oz;   // sorted cell-relative offsets, 8-padded segments
   int4* stencil;         // source-cell offsets within the cutoff of a target cell
   int nstencil, cap;
+  int32_t* chunk_prefix2; // ncells+1: prefix of 256-target chunks (packed kernel)
+  bool packed;           // packed f32x2 kernel (default) or the scalar one
 };
 cudaError_t od_launch_cutoff(const od_cutlist& L, const float4* pos, int n, int Npad,
                              float4* part_hi, float4* part_lo, float rho0, float rc, float rs,

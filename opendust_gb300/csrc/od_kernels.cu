@@ -136,26 +136,6 @@ __global__ void __launch_bounds__(NT) k_pairs(const float4* __restrict__ pos, in
 // NEWTON = 1: target 1 takes 1/s from two packed Newton steps seeded with 1/r (error
 // (r0/r)^4); when any lane of the warp saw r^2 < newton_r2 in the tile, the tile is redone
 // for target 1 with the SFU reciprocal.
-typedef unsigned long long od_u64;
-__device__ __forceinline__ od_u64 p2(float lo, float hi) {
-  od_u64 r; asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(lo), "f"(hi)); return r;
-}
-__device__ __forceinline__ float2 up2(od_u64 v) {
-  float2 r; asm("mov.b64 {%0,%1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v)); return r;
-}
-__device__ __forceinline__ od_u64 fma2(od_u64 a, od_u64 b, od_u64 c) {
-  od_u64 d; asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c)); return d;
-}
-__device__ __forceinline__ od_u64 add2(od_u64 a, od_u64 b) {
-  od_u64 d; asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
-}
-__device__ __forceinline__ od_u64 sub2(od_u64 a, od_u64 b) {
-  od_u64 d; asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
-}
-__device__ __forceinline__ od_u64 mul2(od_u64 a, od_u64 b) {
-  od_u64 d; asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b)); return d;
-}
-
 struct od_pk {
   od_u64 eps, rho, nrho, nl2e, one;
 };
@@ -200,14 +180,38 @@ __device__ __forceinline__ void pair2_newton(const od_pk& k, od_u64 X, od_u64 Y,
   AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
 }
 
-__device__ __forceinline__ float sum2(od_u64 v) {
-  const float2 f = up2(v);
-  return f.x + f.y;
-}
 
 // One block's share of the packed all-pairs sums: targets iblk*2*NT .. +2*NT, sources
 // [j0, j1); partial sums written at part_*[slab_off + i]. Returns false after a wait timeout.
-template <int NT, int NEWTON>
+// Newton reciprocal with a warp-uniform fallback: when any lane of the warp has a pair closer
+// than sqrt(newton_r2) (where two Newton steps from 1/r are not accurate), the SFU reciprocal
+// replaces the Newton result for the whole warp.
+__device__ __forceinline__ void pair2_newton_vote(const od_pk& k, od_u64 X, od_u64 Y, od_u64 Z,
+                                                  od_u64 QX, od_u64 QY, od_u64 QZ, od_u64& AX,
+                                                  od_u64& AY, od_u64& AZ, float newton_r2) {
+  const od_u64 DX = sub2(X, QX), DY = sub2(Y, QY), DZ = sub2(Z, QZ);
+  od_u64 R2 = fma2(DX, DX, k.eps);
+  R2 = fma2(DY, DY, R2);
+  R2 = fma2(DZ, DZ, R2);
+  const float2 r2 = up2(R2);
+  const od_u64 RI = p2(od_rsqrt(r2.x), od_rsqrt(r2.y));
+  const od_u64 R = mul2(R2, RI);
+  const od_u64 NS = sub2(k.nrho, R);  // -(r + rho0)
+  od_u64 E = fma2(NS, RI, k.one);
+  od_u64 SI = fma2(RI, E, RI);
+  E = fma2(NS, SI, k.one);
+  SI = fma2(SI, E, SI);
+  if (__any_sync(0xffffffffu, fminf(r2.x, r2.y) < newton_r2)) {
+    const float2 ns = up2(NS);
+    SI = p2(od_rcp(-ns.x), od_rcp(-ns.y));
+  }
+  const float2 ea = up2(mul2(R, k.nl2e));
+  const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
+  const od_u64 C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
+  AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
+}
+
+template <int NT, int NEWTON, int TPT = 2>
 __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
                                               const float* __restrict__ sy,
                                               const float* __restrict__ sz, int iblk, int j0,
@@ -220,7 +224,7 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
   __shared__ __align__(128) float tz[2][OD_TJ];
   __shared__ __align__(8) uint64_t bar[2];
   const int tid = threadIdx.x;
-  const int i0 = iblk * (2 * NT) + tid, i1 = i0 + NT;
+  const int i0 = iblk * (TPT * NT) + tid, i1 = TPT == 2 ? i0 + NT : i0;
   const int ntiles = (j1 - j0) / OD_TJ;
   const od_u64 X0 = p2(sx[i0], sx[i0]), Y0 = p2(sy[i0], sy[i0]), Z0 = p2(sz[i0], sz[i0]);
   const od_u64 X1 = p2(sx[i1], sx[i1]), Y1 = p2(sy[i1], sy[i1]), Z1 = p2(sz[i1], sz[i1]);
@@ -263,8 +267,20 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
       const ulonglong2 qy = *reinterpret_cast<const ulonglong2*>(&ty[s][j]);
       const ulonglong2 qz = *reinterpret_cast<const ulonglong2*>(&tz[s][j]);
       pair2_sfu(k, X0, Y0, Z0, qx.x, qy.x, qz.x, A0x, A0y, A0z);
+      if (TPT == 1) {
+        // one target per thread: the second source pair of the load takes the Newton
+        // reciprocal (NEWTON == 2) or the SFU one
+        if (NEWTON == 2)
+          pair2_newton_vote(k, X0, Y0, Z0, qx.y, qy.y, qz.y, A0x, A0y, A0z, newton_r2);
+        else
+          pair2_sfu(k, X0, Y0, Z0, qx.y, qy.y, qz.y, A0x, A0y, A0z);
+        continue;
+      }
       pair2_sfu(k, X0, Y0, Z0, qx.y, qy.y, qz.y, A0x, A0y, A0z);
-      if (NEWTON) {
+      if (NEWTON == 2) {
+        pair2_newton_vote(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z, newton_r2);
+        pair2_newton_vote(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z, newton_r2);
+      } else if (NEWTON == 1) {
         pair2_newton(k, X1, Y1, Z1, qx.x, qy.x, qz.x, A1x, A1y, A1z, mr2);
         pair2_newton(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z, mr2);
       } else {
@@ -272,7 +288,7 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
         pair2_sfu(k, X1, Y1, Z1, qx.y, qy.y, qz.y, A1x, A1y, A1z);
       }
     }
-    if (NEWTON && __any_sync(0xffffffffu, mr2 < newton_r2)) {
+    if (TPT == 2 && NEWTON == 1 && __any_sync(0xffffffffu, mr2 < newton_r2)) {
       A1x = A1y = A1z = 0;
       for (int j = 0; j < OD_TJ; j += 4) {
         const ulonglong2 qx = *reinterpret_cast<const ulonglong2*>(&tx[s][j]);
@@ -283,7 +299,9 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
       }
     }
     od_acc2(h0x, l0x, sum2(A0x)); od_acc2(h0y, l0y, sum2(A0y)); od_acc2(h0z, l0z, sum2(A0z));
-    od_acc2(h1x, l1x, sum2(A1x)); od_acc2(h1y, l1y, sum2(A1y)); od_acc2(h1z, l1z, sum2(A1z));
+    if (TPT == 2) {
+      od_acc2(h1x, l1x, sum2(A1x)); od_acc2(h1y, l1y, sum2(A1y)); od_acc2(h1z, l1z, sum2(A1z));
+    }
     __syncthreads();
     if (tid == 0 && issued < ntiles) {
       const int jb = j0 + issued * OD_TJ;
@@ -304,15 +322,17 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
   const size_t off = slab_off;
   part_hi[off + i0] = make_float4(h0x, h0y, h0z, 0.f);
   part_lo[off + i0] = make_float4(l0x, l0y, l0z, 0.f);
-  part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
-  part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+  if (TPT == 2) {
+    part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
+    part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+  }
   // release the barriers so that the next call of this body (persistent loop) can init them
   __syncthreads();
   if (tid == 0) { od_mbar_inval(&bar[0]); od_mbar_inval(&bar[1]); }
   return true;
 }
 
-template <int NT, int NEWTON>
+template <int NT, int NEWTON, int TPT = 2>
 __global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
                                                  const float* __restrict__ sy,
                                                  const float* __restrict__ sz, int Npad, int chunk,
@@ -320,8 +340,8 @@ __global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
                                                  float4* __restrict__ part_lo, float rho0,
                                                  float newton_r2, uint32_t* __restrict__ err) {
   const int j0 = blockIdx.y * chunk;
-  pairs_x2_body<NT, NEWTON>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, Npad),
-                            (size_t)blockIdx.y * Npad, part_hi, part_lo, rho0, newton_r2, err);
+  pairs_x2_body<NT, NEWTON, TPT>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, Npad),
+                                 (size_t)blockIdx.y * Npad, part_hi, part_lo, rho0, newton_r2, err);
 }
 
 __global__ void k_aos_to_soa(const float4* __restrict__ pos, int Npad, float* __restrict__ sx,
@@ -1037,13 +1057,13 @@ static void launch_pairs_t(const od_pair_plan& pl, const float4* pos, int Npad, 
   dim3 grid(gx_of(Npad / (NT * IPT)), pl.jsplit);
   k_pairs<NT, IPT, V><<<grid, NT, 0, s>>>(pos, Npad, pl.chunk, ph, plo, rho0, err);
 }
-template <int NT, int NEWTON>
+template <int NT, int NEWTON, int TPT = 2>
 static void launch_pairs_x2(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
                             float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
-  dim3 grid(gx_of(Npad / (NT * 2)), pl.jsplit);
+  dim3 grid(gx_of(Npad / (NT * TPT)), pl.jsplit);
   const float nr = 64.0f * rho0;  // Newton (2 steps) keeps 1/s within 2^-24 for r > 64 r0
-  k_pairs_x2<NT, NEWTON><<<grid, NT, 0, s>>>(io.sx, io.sy, io.sz, Npad, pl.chunk, ph, plo, rho0,
-                                             nr * nr, err);
+  k_pairs_x2<NT, NEWTON, TPT><<<grid, NT, 0, s>>>(io.sx, io.sy, io.sz, Npad, pl.chunk, ph, plo,
+                                                  rho0, nr * nr, err);
 }
 
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
@@ -1062,6 +1082,12 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Np
     case 25622: launch_pairs_x2<256, 0>(pl, io, Npad, ph, plo, rho0, err, s); break;
     case 12823: launch_pairs_x2<128, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
     case 25623: launch_pairs_x2<256, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 12824: launch_pairs_x2<128, 2>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 25624: launch_pairs_x2<256, 2>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 12815: launch_pairs_x2<128, 0, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 25615: launch_pairs_x2<256, 0, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 12816: launch_pairs_x2<128, 2, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
+    case 25616: launch_pairs_x2<256, 2, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -1246,7 +1272,7 @@ cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, 
 // Many independent simulations advance together: every stage of the step is one launch for
 // the whole batch. Blocks of the ion-parallel stages look up (simulation, local block) in a
 // table; the all-pairs stage is one persistent launch whose blocks take work items
-// (simulation, 512-target block, source range) from a device counter, largest items first;
+// (simulation, 256-target block, source range) from a device counter, largest items first;
 // compaction/re-injection and the FP64 tail run one block per simulation. Each simulation
 // keeps its own buffers, source split and partial slabs, so its results are bitwise the
 // results of the same simulation stepped alone.
@@ -1273,7 +1299,7 @@ __global__ void __launch_bounds__(256) k_b_pairs(const od_simdesc* __restrict__ 
     if (it >= nitems) return;
     const int4 w = items[it];
     const od_simdesc& d = sims[w.x];
-    const bool ok = pairs_x2_body<256, 0>(d.b.sx, d.b.sy, d.b.sz, w.y, w.z, w.w,
+    const bool ok = pairs_x2_body<256, 0, 1>(d.b.sx, d.b.sy, d.b.sz, w.y, w.z, w.w,
                                           (size_t)(w.z / d.chunk) * d.Npad, d.b.part_hi,
                                           d.b.part_lo, d.rho0, d.newton_r2, err);
     if (!ok) return;

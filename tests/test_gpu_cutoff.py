@@ -22,25 +22,28 @@ def _cut_case(N, seed, **kw):
     return case(N=N, n=4, seed=seed, **kw)
 
 
-def test_cutoff_switching_snapshot(gpu_lib):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_cutoff_switching_snapshot(gpu_lib, variant):
     holder, pos, vel, plasma, sim, grains = _cut_case(4096, 21, cutOff=True)
     assert holder.cfg.force_method == _lib.OD_FORCE_CUTOFF
     pos = plant_close_pairs(pos, plasma.r_D_e, np.random.default_rng(3), n_pairs=32, dmin=2e-4)
     with _lib.Engine(holder) as eng:
+        eng.set_pair_plan(128, 1, variant)
         f = eng.force_snapshot(pos)
     ref = oracle.force_snapshot(holder, pos, round32=True)
     err = rel_err_per_ion(f, ref)
-    print(f"cutoff 3.2/3.0: per-ion rel err max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
+    print(f"variant {variant} cutoff 3.2/3.0: per-ion rel err max {err.max():.3e} p99 {np.quantile(err, 0.99):.3e}")
     assert err.max() <= 1e-5
 
 
-@pytest.mark.parametrize("N", [4096, 2**17])
-def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N):
+@pytest.mark.parametrize("N,variant", [(4096, 0), (4096, 2), (2**17, 2)])
+def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N, variant):
     spatial = pytest.importorskip("scipy.spatial")
     holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=22, builder=workloads.field_chain,
                                                  switch_distance=0.0)
     assert holder.cfg.switch_dist == 0.0
     with _lib.Engine(holder) as eng:
+        eng.set_pair_plan(128, 1, variant)
         f = eng.force_snapshot(pos)
         eng.set_state(pos, vel)
         eng.set_timing(True)
@@ -50,7 +53,7 @@ def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N):
     idx = np.arange(N) if N <= 4096 else np.sort(np.random.default_rng(0).choice(N, 2048, replace=False))
     ref = oracle.force_targets(holder, pos, idx, round32=True)
     err = rel_err_per_ion(f[idx], ref)
-    print(f"hard cutoff N={N}: max {err.max():.3e} p99.9 {np.quantile(err, 0.999):.3e}, pairs {pairs}")
+    print(f"variant {variant} hard cutoff N={N}: max {err.max():.3e} p99.9 {np.quantile(err, 0.999):.3e}, pairs {pairs}")
     assert np.quantile(err, 0.999) <= 1e-5
     assert err.max() <= 1e-3
     # directed pairs inside the cutoff at the step's drifted positions, within rounding

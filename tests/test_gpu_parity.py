@@ -18,7 +18,8 @@ from tests._util import case, plant_close_pairs, rel_err_per_ion
 pytestmark = pytest.mark.gpu
 
 
-PLANS = [(256, 1, 0), (128, 2, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3)]
+PLANS = [(256, 1, 0), (128, 2, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3),
+         (256, 2, 4), (256, 1, 5), (128, 1, 6), (256, 1, 6)]
 
 
 @pytest.mark.parametrize("plan", PLANS)
