@@ -36,7 +36,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = 25
-KERNELS_PER_STEP = 6
+KERNELS_PER_STEP = 6          # all pairs: kick/drift, pairs, kick/flag, collect, correct, tail
+KERNELS_PER_STEP_CUTOFF = 12  # + cell clear, count, scan, scatter, sort, chunk scan
 
 
 def parse():
@@ -324,7 +325,7 @@ def run_ours(args, dist: Dist):
                          "flops_per_pair": FLOPS_PER_PAIR, "pair_ms_avg": pair_avg_s * 1e3},
             "e2e": {"value": e2e_value, "unit": "ion-steps/s", "h2d_bytes_per_step": h2d // K_e2e,
                     "d2h_bytes_per_step": d2h // K_e2e},
-            "gpu_launches": KERNELS_PER_STEP * K,
+            "gpu_launches": (KERNELS_PER_STEP_CUTOFF if cutoff else KERNELS_PER_STEP) * K,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -264,7 +264,8 @@ od_status od_trap_potential(double R_over_lambda, double H_over_lambda, int32_t 
  * the same simulation stepped alone. Members use the all-pairs force method. */
 typedef struct od_batch od_batch;
 od_status od_batch_create(int32_t device, od_batch** out);
-/* Creates a member from cfg with initial state pos/vel (as od_create + od_set_state); *slot
+/* Creates a member from cfg with initial state pos/vel (as od_create + od_set_state), or, with
+ * pos = vel = NULL, a Maxwellian initial state sampled on the device (od_init_state); *slot
  * receives its slot index. May be called between steps (continuous batching). */
 od_status od_batch_add(od_batch* b, const od_config* cfg, const double* pos, const double* vel,
                        int32_t* slot);

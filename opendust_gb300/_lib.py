@@ -430,12 +430,18 @@ class Batch:
             msg = self._lib.od_batch_last_error(b)
             raise OpenDustError(st, msg.decode() if msg else "")
 
-    def add(self, holder: ConfigHolder, pos: np.ndarray, vel: np.ndarray) -> int:
-        pos = np.ascontiguousarray(pos, dtype=np.float64)
-        vel = np.ascontiguousarray(vel, dtype=np.float64)
+    def add(self, holder: ConfigHolder, pos: np.ndarray | None = None,
+            vel: np.ndarray | None = None) -> int:
+        """Add a member; without pos/vel its (Maxwellian) initial state is sampled on the device."""
         slot = c_int32()
-        self._check(self._lib.od_batch_add(self.b, holder.ptr(), _dptr(pos), _dptr(vel),
-                                           ctypes.byref(slot)), self.b)
+        if pos is None:
+            self._check(self._lib.od_batch_add(self.b, holder.ptr(), None, None, ctypes.byref(slot)),
+                        self.b)
+        else:
+            pos = np.ascontiguousarray(pos, dtype=np.float64)
+            vel = np.ascontiguousarray(vel, dtype=np.float64)
+            self._check(self._lib.od_batch_add(self.b, holder.ptr(), _dptr(pos), _dptr(vel),
+                                               ctypes.byref(slot)), self.b)
         self._holders[slot.value] = holder
         return slot.value
 

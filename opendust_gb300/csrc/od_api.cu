@@ -1050,7 +1050,7 @@ extern "C" od_status od_batch_create(int32_t device, od_batch** out) {
 
 extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const double* pos,
                                   const double* vel, int32_t* slot) {
-  if (!b || !cfg || !pos || !vel || !slot) return bfail(b, OD_ERR_INVALID, "NULL argument");
+  if (!b || !cfg || !slot || (!pos) != (!vel)) return bfail(b, OD_ERR_INVALID, "NULL argument");
   if (cfg->force_method != OD_FORCE_ALLPAIRS)
     return bfail(b, OD_ERR_UNSUPPORTED, "batch members use the all-pairs force method");
   od_handle* h = nullptr;
@@ -1060,7 +1060,7 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
     st = od_set_pair_plan(h, 256, 1, 5, 0);
     if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
   }
-  st = od_set_state(h, pos, vel, cfg->n_ions);
+  st = pos ? od_set_state(h, pos, vel, cfg->n_ions) : od_init_state(h, nullptr, nullptr, 0);
   if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
   int s = -1;
   for (size_t k = 0; k < b->members.size(); k++)

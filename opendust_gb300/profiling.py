@@ -1,0 +1,83 @@
+"""Small drivers for profiling one kernel of the step with ncu (or timing it with CUDA events).
+
+    python -m opendust_gb300.profiling pairs  --n 65536  --plan 256,1,5 --steps 2
+    python -m opendust_gb300.profiling cutoff --n 131072 --variant 2    --steps 2
+    python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576
+
+`pairs` steps the small_plain workload with the given all-pairs plan, `cutoff` the field_chain
+workload (cutoff 2 lambda over the cell list), both launching kernel by kernel (no CUDA graph) so
+that `ncu -k regex:<kernel>` sees individual launches. `sweep` times every all-pairs plan with
+CUDA events and prints pairs/s.
+"""
+from __future__ import annotations
+
+import argparse
+
+from . import _lib, build_simulation, setup_host, workloads
+
+PLANS = [(256, 1, 0), (128, 1, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3),
+         (128, 2, 4), (256, 2, 4), (128, 1, 5), (256, 1, 5), (128, 1, 6), (256, 1, 6)]
+
+
+def _plain(N, n):
+    plasma, sim, grains, dist, ext = workloads.small_plain(N=N, n=n)
+    holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, **ext)
+    return holder
+
+
+def run_pairs(N, plan, steps):
+    with _lib.Engine(_plain(N, steps + 4)) as eng:
+        eng.set_graph(False)
+        eng.set_pair_plan(*plan)
+        eng.init_state()
+        eng.step(steps)
+        print("ok", eng.pair_plan(), eng.series()["q"][-1])
+
+
+def run_cutoff(N, variant, steps):
+    plasma, sim, grains, dist, ext = workloads.field_chain(N=N, n=steps + 4)
+    holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, **ext)
+    with _lib.Engine(holder) as eng:
+        eng.set_graph(False)
+        eng.set_pair_plan(128, 1, variant)
+        eng.init_state(setup_host.field_driven_vz_table(plasma.v_fl, plasma.v_T))
+        eng.step(steps)
+        print("ok", eng.series()["q"][-1])
+
+
+def run_sweep(sizes):
+    for N in sizes:
+        with _lib.Engine(_plain(N, 200)) as eng:
+            eng.init_state()
+            steps = 2 if N >= 2**20 else (4 if N >= 2**18 else 20)
+            for plan in PLANS:
+                eng.set_pair_plan(*plan)
+                eng.step(1)
+                eng.set_timing(True)
+                eng.step(steps)
+                sm, ns, pm, pl = eng.timing()
+                eng.set_timing(False)
+                per = pm / pl * 1e-3
+                print(f"N={N} plan={plan} {eng.pair_plan()} pair {pm / pl:.3f} ms "
+                      f"{N * (N - 1) / per:.3e} pairs/s {N * (N - 1) * 25 / per / 1e12:.2f} TFLOP/s",
+                      flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["pairs", "cutoff", "sweep"])
+    ap.add_argument("--n", default="65536")
+    ap.add_argument("--plan", default="256,1,5")
+    ap.add_argument("--variant", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=2)
+    a = ap.parse_args()
+    if a.what == "pairs":
+        run_pairs(int(a.n), tuple(int(x) for x in a.plan.split(",")), a.steps)
+    elif a.what == "cutoff":
+        run_cutoff(int(a.n), a.variant, a.steps)
+    else:
+        run_sweep([int(x) for x in a.n.split(",")])
+
+
+if __name__ == "__main__":
+    main()

@@ -6,8 +6,9 @@ its answer is the time-averaged grain charge and forces over the second half of 
 ion state resident on the GPU as a member of one ``od_batch`` and steps all members together;
 between chunks of steps it admits arrived requests while the device-memory budget allows and
 retires members whose window is complete. The host part of a request's setup (injection
-tables, initial state) runs in a worker process pool, overlapping the GPU steps; the trap fit
-runs on the GPU when the request is admitted.
+tables; the initial state of field-driven requests) runs in a worker process pool, overlapping
+the GPU steps; the trap fit and Maxwellian initial states run on the GPU when the request is
+admitted.
 
 ``run_plain`` is the baseline: the same requests served one at a time through the plain
 single-simulation path, in arrival order.
@@ -45,8 +46,11 @@ class Request:
 
 
 def host_prepare(req: Request):
-    """CPU part of a request's setup (picklable): injection tables and the initial ion state."""
+    """CPU part of a request's setup (picklable): injection tables and, for field-driven
+    requests, the initial ion state (Maxwellian ones are sampled on the device)."""
     inj = setup_host.injection_setup(req.plasma.v_fl, req.plasma.v_T, req.sim.R, req.sim.H, req.dist)
+    if req.dist == "Maxwellian":
+        return inj, None, None
     pos, vel = setup_host.initial_state(req.sim.N, req.sim.R, req.sim.H,
                                         [(g.x, g.y, g.z, g.r) for g in req.grains],
                                         req.plasma.v_fl, req.plasma.v_T, req.dist, req.seed)
@@ -163,7 +167,10 @@ def run_plain(requests: list[Request], device: int = 0) -> dict:
             time.sleep(wait)
         holder, pos, vel = prepare(r, device)
         with _lib.Engine(holder, device) as eng:
-            eng.set_state(pos, vel)
+            if pos is None:
+                eng.init_state()
+            else:
+                eng.set_state(pos, vel)
             t1 = time.perf_counter()
             eng.step(r.window)
             gpu_ms += (time.perf_counter() - t1) * 1e3
