@@ -11,8 +11,11 @@ kick, flags, ordered compaction, re-injection, grain sums, FP64 tail).
              resident in HBM, L2 flushed (512 MB write) before every timed step.
   e2e        the same metric through the C ABI with host arrays: od_set_state (host->device),
              od_step, od_get_series + od_get_state (device->host), wall clock.
-  roofline   the all-pairs force kernel: N(N-1) pair interactions x 25 FP32 flops per launch
-             over its CUDA-event duration, against the FP32 FMA peak measured on the same GPU.
+  roofline   the all-pairs force evaluation: N(N-1) directed pair interactions x 25 FP32 flops
+             per launch over its CUDA-event duration, against the FP32 FMA peak measured on the
+             same GPU. The default kernel from 2^15 ions (variant 7) evaluates each unordered
+             pair once and applies it to both ions, so it does about half those flops: its
+             fraction can exceed what a directed-pair kernel could reach.
   cpu_baseline  the CPU oracle (FP64 C restatement of the reference step, OpenMP over all host
              cores) on a bounded sample: the reference's two ion–ion evaluations per step for T
              target ions against all N sources plus one linear pass over all N ions.
@@ -37,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = 25
 KERNELS_PER_STEP = 6          # all pairs: kick/drift, pairs, kick/flag, collect, correct, tail
+                              # (+ the tile-pair row sums with variant 7)
 KERNELS_PER_STEP_CUTOFF = 12  # + cell clear, count, scan, scatter, sort, chunk scan
 
 
@@ -225,14 +229,16 @@ def run_reference(args, dist: Dist):
     return 0
 
 
-def load_traffic(n_ions: int):
-    """DRAM bytes per all-pairs launch from the committed ncu capture of the same size."""
+def load_traffic(n_ions: int, variant: int):
+    """DRAM bytes per all-pairs force evaluation from the committed ncu capture of the same size
+    and kernel variant."""
     path = os.path.join(ROOT, "profiles", "allpairs_traffic.json")
     try:
         d = json.load(open(path))
     except (OSError, ValueError):
         return None
-    return d.get("dram_bytes_per_launch") if d.get("n_ions") == n_ions else None
+    ok = d.get("n_ions") == n_ions and d.get("variant") == variant
+    return d.get("dram_bytes_per_launch") if ok else None
 
 
 def run_ours(args, dist: Dist):
@@ -255,6 +261,7 @@ def run_ours(args, dist: Dist):
     peak = _lib.fp32_peak_tflops(device)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
     eng = _lib.Engine(holder, device)
+    plan = eng.pair_plan()
     eng.set_state(pos, vel)
     eng.step(W)  # warm-up (graph replay path)
     eng.set_timing(True)
@@ -279,7 +286,16 @@ def run_ours(args, dist: Dist):
     cutoff = cut_pairs > 0
     pairs_per_launch = cut_pairs / pair_launches if cutoff else N * (N - 1)
     achieved = pairs_per_launch * FLOPS_PER_PAIR / pair_avg_s / 1e12
-    traffic = load_traffic(N)
+    n3 = not cutoff and plan["variant"] == 7
+    traffic = None if cutoff else load_traffic(N, plan["variant"])
+    if cutoff:
+        kernel = "cell-list build + k_pairs_cut (pairs inside the cutoff)"
+    elif n3:
+        kernel = (f"k_pairs_n3 + k_n3_reduce (each unordered pair once, {plan['jsplit']}-ion tiles; "
+                  "credited with the N(N-1) directed pair terms it replaces)")
+    else:
+        kernel = f"k_pairs_x2 variant {plan['variant']} (all-pairs ion-ion)"
+    launches = KERNELS_PER_STEP_CUTOFF if cutoff else KERNELS_PER_STEP + (1 if n3 else 0)
 
     # e2e through the C ABI with host buffers (the calls simulate() makes)
     eng.close()
@@ -318,14 +334,12 @@ def run_ours(args, dist: Dist):
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
             "pair_interactions_per_s": (pairs_per_launch * K * dist.world / (t_max * 1e-3)),
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None if cutoff else traffic,
-                         "kernel": ("cell-list build + k_pairs_cut (pairs inside the cutoff)" if cutoff
-                                    else "k_pairs_x2 (all-pairs ion-ion)"),
+                         "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                          "peak_source": "FP32 FMA probe measured on this GPU in this run",
                          "flops_per_pair": FLOPS_PER_PAIR, "pair_ms_avg": pair_avg_s * 1e3},
             "e2e": {"value": e2e_value, "unit": "ion-steps/s", "h2d_bytes_per_step": h2d // K_e2e,
                     "d2h_bytes_per_step": d2h // K_e2e},
-            "gpu_launches": (KERNELS_PER_STEP_CUTOFF if cutoff else KERNELS_PER_STEP) * K,
+            "gpu_launches": launches * K,
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -201,7 +201,10 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * targets per thread), 3: as 2 with Newton reciprocals for half of the targets (tile redone on
  * the SFU when a pair is too close), 4: as 3 with a warp-vote SFU fallback per pair,
  * 5: packed with one target per thread (targets_per_thread 1), 6: as 5 with every other source
- * pair on the Newton path of variant 4.
+ * pair on the Newton path of variant 4, 7: each unordered pair evaluated once and applied to
+ * both ions (threads 256, targets_per_thread = ions per lane, 2 or 4; jsplit = ions per tile,
+ * 1024, 2048 or 4096, <= 0 for the default; needs 24 bytes of device memory per ion and tile,
+ * OD_ERR_OOM when that does not fit).
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);
@@ -210,7 +213,7 @@ od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_th
  * cached for this (device, padded size) in the process is reused. *best_pairs_per_s receives
  * the measured rate (0 when cached). All-pairs method only. */
 od_status od_autotune(od_handle* h, int32_t use_cache, double* best_pairs_per_s);
-/* plan5 = {threads, targets_per_thread, variant, jsplit, chunk} */
+/* plan5 = {threads, targets_per_thread, variant, jsplit (variant 7: ions per tile), chunk} */
 od_status od_get_pair_plan(const od_handle* h, int32_t* plan5);
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured by a short probe
  * kernel: the denominator of the all-pairs kernel's roofline. */
@@ -280,7 +283,9 @@ od_status od_batch_destroy(od_batch* b);
 const char* od_batch_last_error(const od_batch* b);
 /* Free and total device memory (admission control of a request server). */
 od_status od_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
-/* Device bytes a simulation with this configuration allocates (admission control). */
+/* Device bytes a simulation created by od_create with this configuration allocates, including
+ * the tile-pair matrix of the default all-pairs plan (variant 7 from 2^15 ions; batch members
+ * do not allocate it) (admission control). */
 od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes);
 
 /* Ion–ion forces for callers that cannot allocate device memory (no counterpart in the

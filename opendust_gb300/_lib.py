@@ -355,6 +355,7 @@ class Engine:
         return sm.value, st.value, pm.value, pl.value
 
     def set_pair_plan(self, threads: int, targets_per_thread: int, variant: int, jsplit: int = 0):
+        """All-pairs work decomposition; for variant 7 `jsplit` is the tile size in ions."""
         check(self._lib.od_set_pair_plan(self.h, threads, targets_per_thread, variant, jsplit), self.h)
 
     def autotune(self, use_cache: bool = True) -> float:

@@ -215,6 +215,13 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
 // Default all-pairs plan: packed f32x2 arithmetic on SoA tiles with one target per thread
 // (variant 5, the fastest measured on GB300 from 2^16 to 2^20 ions), with enough source chunks
 // for several waves on every SM.
+// From 2^15 padded ions the default is variant 7 (each unordered pair once, 4 ions per lane)
+// when its tile-pair matrix fits OD_N3_BUDGET (about a ninth of a GB300's memory: 2048-ion tiles
+// up to 2^20 ions, 4096-ion tiles up to 2^21); od_create falls back to the plan below otherwise.
+static constexpr size_t OD_N3_BUDGET = (size_t)32 << 30;
+static bool uses_n3_default(int Npad) { return Npad >= 32768; }
+static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile);
+
 static od_pair_plan default_plan(int Npad, int sms) {
   od_pair_plan pl{};
   pl.nt = 256; pl.ipt = 1; pl.variant = 5;
@@ -251,7 +258,7 @@ static void free_all(od_handle* h) {
                   h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
                   h->b.sx, h->b.sy, h->b.sz, h->cut.cell_of, h->cut.count, h->cut.fill,
                   h->cut.start, h->cut.chunk_prefix, h->cut.perm, h->cut.ox, h->cut.oy, h->cut.oz,
-                  h->cut.stencil, h->d_pairs, h->cut.chunk_prefix2};
+                  h->cut.stencil, h->d_pairs, h->cut.chunk_prefix2, h->b.n3};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -265,7 +272,17 @@ static od_status alloc_scratch_for_plan(od_handle* h) {
   return OD_OK;
 }
 
+static od_status create_handle(const od_config* cfg, int32_t device, bool n3_default,
+                               od_handle** out);
+
 extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle** out) {
+  return create_handle(cfg, device, true, out);
+}
+
+// n3_default = false: keep the directed-pair default plan (batch members, which the batched
+// all-pairs kernel steps with their own plan), so that no tile-pair matrix is allocated.
+static od_status create_handle(const od_config* cfg, int32_t device, bool n3_default,
+                               od_handle** out) {
   if (!out) return fail(nullptr, OD_ERR_INVALID, "out is NULL");
   *out = nullptr;
   od_status st = validate(cfg);
@@ -320,6 +337,12 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
   OD_CKC(dalloc(&h->b.sy, Np));
   OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
+  if (n3_default && cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default(h->Npad) &&
+      set_plan_n3(h, 4, 0) != OD_OK) {
+    // the tile-pair matrix did not fit: stay on the directed-pair default
+    cudaGetLastError();
+    h->err.clear();
+  }
   if (cfg->force_method == OD_FORCE_CUTOFF) {
     // Cells of side c = a power of two not above rc/4 (halved while the mean occupancy exceeds
     // ~800 ions), on a grid whose origin is a multiple of c: cell origins and the shifts between
@@ -427,7 +450,7 @@ static od_status refresh_forces(od_handle* h) {
   const float rho0 = h->hp.rho0;
   OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
   (void)rho0;
-  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->b.pos, h->b.sx, h->b.sy, h->b.sz}, h->N,
+  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->b.pos, h->b.sx, h->b.sy, h->b.sz, h->b.n3}, h->N,
                            h->Npad, h->b.part_hi, h->b.part_lo, &h->ds->err, h->stream));
   OD_CK(h, od_launch_reduce(h->dp, h->Npad, force_jsplit(h), h->b.part_hi, h->b.part_lo, h->b.fhi,
                             h->b.flo, h->stream));
@@ -631,10 +654,52 @@ static bool plan_supported(int nt, int ipt, int variant) {
     case 12810: case 12820: case 25610: case 25620: case 12811: case 25611: case 25621:
     case 12822: case 25622: case 12823: case 25623: case 12824: case 25624:
     case 12815: case 25615: case 12816: case 25616:
+    case 25627: case 25647:  // each unordered pair once, 2 or 4 ions per lane
       return true;
     default:
       return false;
   }
+}
+
+static void drop_graph(od_handle* h) {
+  if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+}
+
+static void free_n3(od_handle* h) {
+  if (h->b.n3) { cudaFree(h->b.n3); h->b.n3 = nullptr; }
+  h->b.n3_len = 0;
+}
+
+// Variant 7: `tile` ions per tile (1024, 2048, 4096; 0 = the default for this ion count); its
+// tile-pair matrix holds 24 bytes per ion and tile (6.4 GB at 2^20 ions with 4096-ion tiles).
+static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile) {
+  if (!plan_supported(256, ions_per_lane, 7))
+    return fail(h, OD_ERR_INVALID, "variant 7 takes 2 or 4 ions per lane");
+  if (tile <= 0) {
+    tile = od_n3_tile(h->Npad, OD_N3_BUDGET);
+    if (tile == 0) return fail(h, OD_ERR_OOM, "variant 7 needs more than its memory budget here");
+  }
+  if (tile != 1024 && tile != 2048 && tile != 4096)
+    return fail(h, OD_ERR_INVALID, "variant 7 tiles hold 1024, 2048 or 4096 ions");
+  OD_CK(h, cudaSetDevice(h->device));
+  od_pair_plan pl{};
+  pl.nt = 256; pl.ipt = ions_per_lane; pl.variant = 7; pl.tile = tile;
+  pl.jsplit = 1; pl.chunk = h->Npad;
+  OD_CK(h, od_n3_prepare(pl));
+  const size_t need = od_n3_floats(h->Npad, tile);
+  if (h->b.n3_len < need) {
+    free_n3(h);
+    if (cudaMalloc((void**)&h->b.n3, sizeof(float) * need) != cudaSuccess) {
+      cudaGetLastError();
+      h->b.n3 = nullptr;
+      return fail(h, OD_ERR_OOM, "no device memory for the variant-7 tile-pair sums");
+    }
+    h->b.n3_len = need;
+  }
+  h->plan = pl;  // one partial slab: part_hi/part_lo always hold at least one
+  drop_graph(h);
+  return OD_OK;
 }
 
 extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
@@ -650,8 +715,10 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
   }
   if (!plan_supported(threads, targets_per_thread, variant))
     return fail(h, OD_ERR_INVALID, "unsupported (threads, targets_per_thread, variant)");
+  if (variant == 7) return set_plan_n3(h, targets_per_thread, jsplit);
   if (h->Npad % (threads * targets_per_thread) != 0)
     return fail(h, OD_ERR_INVALID, "block does not divide the padded ion count");
+  free_n3(h);
   od_pair_plan pl{};
   pl.nt = threads; pl.ipt = targets_per_thread; pl.variant = variant;
   if (jsplit <= 0) {
@@ -692,13 +759,14 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
     if (it != g_tuned.end()) {
       const od_pair_plan& p = it->second;
       if (best_pairs_per_s) *best_pairs_per_s = 0;
-      return od_set_pair_plan(h, p.nt, p.ipt, p.variant, p.jsplit);
+      return od_set_pair_plan(h, p.nt, p.ipt, p.variant, p.variant == 7 ? p.tile : p.jsplit);
     }
   }
   OD_CK(h, od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
   const int shapes[][3] = {{256, 1, 0}, {128, 1, 0}, {256, 1, 1}, {128, 2, 2}, {256, 2, 2},
                            {128, 2, 3}, {256, 2, 3}, {128, 2, 4}, {256, 2, 4},
-                           {128, 1, 5}, {256, 1, 5}, {128, 1, 6}, {256, 1, 6}};
+                           {128, 1, 5}, {256, 1, 5}, {128, 1, 6}, {256, 1, 6},
+                           {256, 2, 7}, {256, 4, 7}};
   const int sms = od_num_sms(h->device);
   cudaEvent_t e0, e1;
   OD_CK(h, cudaEventCreate(&e0));
@@ -706,6 +774,28 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
   double best = -1;
   od_pair_plan best_plan = h->plan;
   for (const auto& sh : shapes) {
+    if (sh[2] == 7) {
+      // each unordered pair once: timed over a full launch with the default tile, and only
+      // when its tile-pair matrix fits (the pair rate counts directed pairs, as for the others)
+      if (h->Npad < 8192 || od_set_pair_plan(h, sh[0], sh[1], 7, 0) != OD_OK) {
+        cudaGetLastError();
+        continue;
+      }
+      const od_pair_io io{h->b.pos, h->b.sx, h->b.sy, h->b.sz, h->b.n3};
+      OD_CK(h, od_launch_pairs(h->plan, io, h->Npad, h->b.part_hi, h->b.part_lo, h->hp.rho0,
+                               &h->ds->err, h->stream));
+      OD_CK(h, cudaEventRecord(e0, h->stream));
+      for (int r = 0; r < 2; r++)
+        OD_CK(h, od_launch_pairs(h->plan, io, h->Npad, h->b.part_hi, h->b.part_lo, h->hp.rho0,
+                                 &h->ds->err, h->stream));
+      OD_CK(h, cudaEventRecord(e1, h->stream));
+      OD_CK(h, cudaEventSynchronize(e1));
+      float ms = 0;
+      OD_CK(h, cudaEventElapsedTime(&ms, e0, e1));
+      const double rate = 2.0 * (double)h->Npad * h->Npad / (ms * 1e-3);
+      if (rate > best) { best = rate; best_plan = h->plan; }
+      continue;
+    }
     const int nbx = h->Npad / (sh[0] * sh[1]);
     const int js0 = std::max(1, (sms * 8 * 4 + nbx - 1) / nbx);
     for (int mult = 0; mult < 3; mult++) {
@@ -714,7 +804,7 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
       const od_pair_plan& pl = h->plan;
       // enough target blocks for ~8 waves of the source split, at most the full grid
       const int limit = std::min(nbx, std::max(1, (sms * 32 + pl.jsplit - 1) / pl.jsplit));
-      const od_pair_io io{h->b.pos, h->b.sx, h->b.sy, h->b.sz};
+      const od_pair_io io{h->b.pos, h->b.sx, h->b.sy, h->b.sz, h->b.n3};
       OD_CK(h, od_launch_pairs_probe(pl, io, h->Npad, limit, h->b.part_hi, h->b.part_lo, h->hp.rho0,
                                      &h->ds->err, h->stream));
       OD_CK(h, cudaEventRecord(e0, h->stream));
@@ -732,7 +822,8 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  od_status st = od_set_pair_plan(h, best_plan.nt, best_plan.ipt, best_plan.variant, best_plan.jsplit);
+  od_status st = od_set_pair_plan(h, best_plan.nt, best_plan.ipt, best_plan.variant,
+                                  best_plan.variant == 7 ? best_plan.tile : best_plan.jsplit);
   if (st != OD_OK) return st;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -747,7 +838,7 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
 extern "C" od_status od_get_pair_plan(const od_handle* h, int32_t* plan5) {
   if (!h || !plan5) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
   plan5[0] = h->plan.nt; plan5[1] = h->plan.ipt; plan5[2] = h->plan.variant;
-  plan5[3] = h->plan.jsplit; plan5[4] = h->plan.chunk;
+  plan5[3] = h->plan.variant == 7 ? h->plan.tile : h->plan.jsplit; plan5[4] = h->plan.chunk;
   return OD_OK;
 }
 
@@ -824,7 +915,7 @@ extern "C" od_status od_force_snapshot(od_handle* h, const double* pos, int64_t 
   if (st != OD_OK) return st;
   // the snapshot borrows the SoA source buffers; od_step rewrites them before its next use
   OD_CK(h, od_launch_aos_to_soa(h->snap_pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
-  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->snap_pos, h->b.sx, h->b.sy, h->b.sz},
+  OD_CK(h, od_launch_force(force_ctx(h, false), od_pair_io{h->snap_pos, h->b.sx, h->b.sy, h->b.sz, h->b.n3},
                            (int)n, h->Npad, h->b.part_hi, h->b.part_lo, &h->ds->err, h->stream));
   OD_CK(h, od_launch_reduce(h->dp, h->Npad, force_jsplit(h), h->b.part_hi, h->b.part_lo, h->snap_hi,
                             h->snap_lo, h->stream));
@@ -1054,7 +1145,7 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
   if (cfg->force_method != OD_FORCE_ALLPAIRS)
     return bfail(b, OD_ERR_UNSUPPORTED, "batch members use the all-pairs force method");
   od_handle* h = nullptr;
-  od_status st = od_create(cfg, b->device, &h);
+  od_status st = create_handle(cfg, b->device, false, &h);
   if (st != OD_OK) return bfail(b, st, g_err);
   if (h->plan.variant != 5 || h->plan.nt != 256 || h->plan.ipt != 1) {
     st = od_set_pair_plan(h, 256, 1, 5, 0);
@@ -1229,6 +1320,10 @@ extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes
   const od_pair_plan pl = default_plan((int)Np, 152);
   const int64_t P = std::max(cfg->n_grains, 1);
   int64_t b = 0;
+  if (cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default((int)Np)) {
+    const int tile = od_n3_tile((int)Np, OD_N3_BUDGET);
+    if (tile) b += (int64_t)(sizeof(float) * od_n3_floats((int)Np, tile));  // tile-pair sums
+  }
   b += Np * 16 * 4;                 // pos, vel, fhi, flo
   b += Np * 12;                     // SoA copy
   b += (int64_t)pl.jsplit * Np * 32;  // partial slabs

@@ -11,13 +11,16 @@ struct od_pair_plan {
   int jsplit;  // source chunks (grid.y); partial slabs written per ion
   int chunk;   // sources per chunk (multiple of OD_TJ)
   int variant; // 0: shared-memory broadcast, 1: warp-shuffle broadcast, 2: packed f32x2 with
-               // SoA tiles (ipt 2), 3: as 2 with Newton reciprocals for half of the targets
+               // SoA tiles (ipt 2), 3: as 2 with Newton reciprocals for half of the targets,
+               // 4-6: further packed forms, 7: each unordered pair once (od_n3.cu)
+  int tile;    // variant 7: ions per tile (1024, 2048 or 4096); ipt = ions per lane (2 or 4)
 };
 
 // Position views the all-pairs kernels read: float4 AoS, and SoA slices for variants 2-3.
 struct od_pair_io {
   const float4* pos;
   const float *sx, *sy, *sz;
+  float* n3 = nullptr;  // variant 7: tile-pair partial sums [nT][nT][6][tile]
 };
 
 // Device buffers of one simulation.
@@ -32,9 +35,20 @@ struct od_dbufs {
   double *s_q, *s_orbit, *s_collect, *s_dust, *s_field;  // result series
   float* cq;                            // [P] A_id * q_param, FP32 copy for the ion kernels
   float *sx, *sy, *sz;                  // [Npad] SoA copy of positions (all-pairs sources)
+  float* n3;                            // variant 7 tile-pair partial sums (or NULL)
+  size_t n3_len;                        // floats allocated at n3
 };
 
 int od_num_sms(int device);
+
+// Variant 7 (od_n3.cu): default tile for a padded ion count whose partial-sum matrix fits the
+// byte budget (0: none fits), floats of that matrix, and the launch (pair kernel + fixed-order
+// row sums into slab 0 of ph/pl).
+int od_n3_tile(int Npad, size_t budget_bytes);
+size_t od_n3_floats(int Npad, int tile);
+cudaError_t od_n3_prepare(const od_pair_plan& pl);  // shared-memory opt-in, current device
+cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
+                               float4* pl_lo, float rho0, cudaStream_t s);
 
 // One member of a batch, as the batched kernels see it.
 struct od_simdesc {

@@ -1068,6 +1068,7 @@ static void launch_pairs_x2(const od_pair_plan& pl, const od_pair_io& io, int Np
 
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
                             float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
+  if (pl.variant == 7) return od_launch_pairs_n3(pl, io, Npad, ph, plo, rho0, s);
   const int key = pl.nt * 100 + pl.ipt * 10 + pl.variant;
   const float4* pos = io.pos;
   switch (key) {
@@ -1135,7 +1136,7 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
     return cudaGetLastError();
   }
   if (part == 1)
-    return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz}, N, Npad, b.part_hi, b.part_lo,
+    return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz, b.n3}, N, Npad, b.part_hi, b.part_lo,
                            &ds->err, s);
   const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
   k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,

@@ -290,11 +290,14 @@ class OpenDust:
 
     def simulate(self, deviceIndex="0", cutOff=False, toRestartFileName="", *, seed=0,
                  collisions=None, mean_free_path=None, cutoff_distance=None,
-                 switch_distance=None, avg_start=None, quiet=False, init="device"):
+                 switch_distance=None, avg_start=None, quiet=False, init="device",
+                 pair_plan=None):
         """Run n steps on one GPU (opendust.py:362-1383). Returns (q, forces): q has shape
         (n, P); forces is a dict of (n, P, 3) arrays "orbit", "collect", "dust", "field".
         init: "device" samples the initial ions on the GPU (od_init_state), "host" with numpy
-        (setup_host.initial_state); a restart file overrides both."""
+        (setup_host.initial_state); a restart file overrides both. pair_plan: all-pairs work
+        decomposition (threads, ions per thread, variant[, jsplit or tile]) passed to
+        od_set_pair_plan; None keeps the library's default for this ion count."""
         plasma = self.plasmaParametersInSIUnits
         sim = self.simulationParametersInSIUnits
         out = self.outputParameters
@@ -314,6 +317,8 @@ class OpenDust:
                                         self.distributionType, seed)
         eng = _lib.Engine(holder, device)
         try:
+            if pair_plan is not None:
+                eng.set_pair_plan(*pair_plan)
             if pos is not None:
                 eng.set_state(pos, vel)
             elif self.distributionType == "fieldDriven":

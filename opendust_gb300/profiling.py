@@ -2,7 +2,7 @@
 
     python -m opendust_gb300.profiling pairs  --n 65536  --plan 256,1,5 --steps 2
     python -m opendust_gb300.profiling cutoff --n 131072 --variant 2    --steps 2
-    python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576
+    python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576 [--plans '256,1,5;256,4,7']
 
 `pairs` steps the small_plain workload with the given all-pairs plan, `cutoff` the field_chain
 workload (cutoff 2 lambda over the cell list), both launching kernel by kernel (no CUDA graph) so
@@ -16,7 +16,8 @@ import argparse
 from . import _lib, build_simulation, setup_host, workloads
 
 PLANS = [(256, 1, 0), (128, 1, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3),
-         (128, 2, 4), (256, 2, 4), (128, 1, 5), (256, 1, 5), (128, 1, 6), (256, 1, 6)]
+         (128, 2, 4), (256, 2, 4), (128, 1, 5), (256, 1, 5), (128, 1, 6), (256, 1, 6),
+         (256, 2, 7), (256, 4, 7)]
 
 
 def _plain(N, n):
@@ -45,12 +46,13 @@ def run_cutoff(N, variant, steps):
         print("ok", eng.series()["q"][-1])
 
 
-def run_sweep(sizes):
+def run_sweep(sizes, plans=None):
+    plans = plans or PLANS
     for N in sizes:
-        with _lib.Engine(_plain(N, 200)) as eng:
+        with _lib.Engine(_plain(N, 22 * len(plans) + 8)) as eng:
             eng.init_state()
             steps = 2 if N >= 2**20 else (4 if N >= 2**18 else 20)
-            for plan in PLANS:
+            for plan in plans:
                 eng.set_pair_plan(*plan)
                 eng.step(1)
                 eng.set_timing(True)
@@ -70,13 +72,15 @@ def main():
     ap.add_argument("--plan", default="256,1,5")
     ap.add_argument("--variant", type=int, default=2)
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--plans", default="", help="sweep only these plans, e.g. '256,1,5;256,4,7'")
     a = ap.parse_args()
     if a.what == "pairs":
         run_pairs(int(a.n), tuple(int(x) for x in a.plan.split(",")), a.steps)
     elif a.what == "cutoff":
         run_cutoff(int(a.n), a.variant, a.steps)
     else:
-        run_sweep([int(x) for x in a.n.split(",")])
+        plans = [tuple(int(x) for x in p.split(",")) for p in a.plans.split(";") if p]
+        run_sweep([int(x) for x in a.n.split(",")], plans)
 
 
 if __name__ == "__main__":
