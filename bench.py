@@ -9,8 +9,9 @@ kick, flags, ordered compaction, re-injection, grain sums, FP64 tail).
 
   value      ion-steps/s from CUDA events on the library's stream over K timed steps, inputs
              resident in HBM, L2 flushed (512 MB write) before every timed step.
-  e2e        the same metric through the C ABI with host arrays: od_set_state (host->device),
-             od_step, od_get_series + od_get_state (device->host), wall clock.
+  e2e        the same metric through the C ABI with host arrays: od_set_state (host->device,
+             including the initial force evaluation), then per step od_step and od_get_series of
+             that step (device->host), then od_get_state (device->host); wall clock.
   roofline   the all-pairs force evaluation: N(N-1) directed pair interactions x 25 FP32 flops
              per launch over its CUDA-event duration, against the FP32 FMA peak measured on the
              same GPU. The default kernel from 2^15 ions (variant 7) evaluates each unordered
@@ -303,8 +304,11 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     t0 = time.perf_counter()
     eng.set_state(pos, vel)
-    eng.step(K_e2e)
-    ser = eng.series(0, K_e2e)
+    rows = []
+    for i in range(K_e2e):  # each step's grain results read back as the reference does per step
+        eng.step(1)
+        rows.append(eng.series(i, 1))
+    ser = {k: np.concatenate([r[k] for r in rows]) for k in rows[0]}
     p_out, v_out = eng.get_state()
     t1 = time.perf_counter()
     e2e_t = dist.reduce(t1 - t0, "max")
