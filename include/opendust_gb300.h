@@ -202,9 +202,10 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * the SFU when a pair is too close), 4: as 3 with a warp-vote SFU fallback per pair,
  * 5: packed with one target per thread (targets_per_thread 1), 6: as 5 with every other source
  * pair on the Newton path of variant 4, 7: each unordered pair evaluated once and applied to
- * both ions (threads 256, targets_per_thread = ions per lane, 2 or 4; jsplit = ions per tile,
- * 1024, 2048 or 4096, <= 0 for the default; needs 24 bytes of device memory per ion and tile,
- * OD_ERR_OOM when that does not fit).
+ * both ions (threads 256; targets_per_thread = target ions per lane: 2 or 4 with as many source
+ * ions, 8 with two; jsplit = ions per tile, 1024, 2048 or 4096 (not 1024 with 8), <= 0 for the
+ * default; needs 24 bytes of device memory per ion and tile, OD_ERR_OOM when that does not
+ * fit). From 2^15 ions od_create selects variant 7 when its memory fits 32 GiB.
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);

@@ -215,9 +215,10 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
 // Default all-pairs plan: packed f32x2 arithmetic on SoA tiles with one target per thread
 // (variant 5, the fastest measured on GB300 from 2^16 to 2^20 ions), with enough source chunks
 // for several waves on every SM.
-// From 2^15 padded ions the default is variant 7 (each unordered pair once, 4 ions per lane)
-// when its tile-pair matrix fits OD_N3_BUDGET (about a ninth of a GB300's memory: 2048-ion tiles
-// up to 2^20 ions, 4096-ion tiles up to 2^21); od_create falls back to the plan below otherwise.
+// From 2^15 padded ions the default is variant 7 (each unordered pair once: 4 x 4 ions per lane
+// with 1024-ion tiles up to 2^17 ions, then 8 x 2 with 2048-ion tiles) when its tile-pair matrix
+// fits OD_N3_BUDGET (about a ninth of a GB300's memory: 2048-ion tiles up to 2^20 ions, 4096-ion
+// tiles up to 2^21); od_create falls back to the plan below otherwise.
 static constexpr size_t OD_N3_BUDGET = (size_t)32 << 30;
 static bool uses_n3_default(int Npad) { return Npad >= 32768; }
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile);
@@ -337,8 +338,10 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
   OD_CKC(dalloc(&h->b.sy, Np));
   OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
-  if (n3_default && cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default(h->Npad) &&
-      set_plan_n3(h, 4, 0) != OD_OK) {
+  int n3_ipt = 0, n3_tile = 0;
+  if (n3_default && cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default(h->Npad))
+    n3_tile = od_n3_default(h->Npad, OD_N3_BUDGET, &n3_ipt);
+  if (n3_tile && set_plan_n3(h, n3_ipt, n3_tile) != OD_OK) {
     // the tile-pair matrix did not fit: stay on the directed-pair default
     cudaGetLastError();
     h->err.clear();
@@ -654,7 +657,7 @@ static bool plan_supported(int nt, int ipt, int variant) {
     case 12810: case 12820: case 25610: case 25620: case 12811: case 25611: case 25621:
     case 12822: case 25622: case 12823: case 25623: case 12824: case 25624:
     case 12815: case 25615: case 12816: case 25616:
-    case 25627: case 25647:  // each unordered pair once, 2 or 4 ions per lane
+    case 25627: case 25647: case 25687:  // each unordered pair once
       return true;
     default:
       return false;
@@ -671,17 +674,23 @@ static void free_n3(od_handle* h) {
   h->b.n3_len = 0;
 }
 
-// Variant 7: `tile` ions per tile (1024, 2048, 4096; 0 = the default for this ion count); its
-// tile-pair matrix holds 24 bytes per ion and tile (6.4 GB at 2^20 ions with 4096-ion tiles).
+// Variant 7: `ions_per_lane` targets per lane (2 or 4 with as many sources, 8 with two sources),
+// `tile` ions per tile (1024, 2048, 4096; <= 0: the smallest supported tile whose matrix fits
+// OD_N3_BUDGET, 1024 only up to 2^17 ions). The tile-pair matrix holds 24 bytes per ion and tile
+// (12.9 GB at 2^20 ions with 2048-ion tiles).
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile) {
   if (!plan_supported(256, ions_per_lane, 7))
-    return fail(h, OD_ERR_INVALID, "variant 7 takes 2 or 4 ions per lane");
+    return fail(h, OD_ERR_INVALID, "variant 7 takes 2, 4 or 8 targets per lane");
   if (tile <= 0) {
-    tile = od_n3_tile(h->Npad, OD_N3_BUDGET);
-    if (tile == 0) return fail(h, OD_ERR_OOM, "variant 7 needs more than its memory budget here");
+    for (int T = h->Npad <= (1 << 17) ? 1024 : 2048; T <= 4096 && tile <= 0; T <<= 1)
+      if (od_n3_supported(ions_per_lane, T) &&
+          sizeof(float) * od_n3_floats(h->Npad, T) <= OD_N3_BUDGET)
+        tile = T;
+    if (tile <= 0) return fail(h, OD_ERR_OOM, "variant 7 needs more than its memory budget here");
   }
-  if (tile != 1024 && tile != 2048 && tile != 4096)
-    return fail(h, OD_ERR_INVALID, "variant 7 tiles hold 1024, 2048 or 4096 ions");
+  if (!od_n3_supported(ions_per_lane, tile))
+    return fail(h, OD_ERR_INVALID,
+                "variant 7 tiles hold 1024, 2048 or 4096 ions (2048 or 4096 with 8 per lane)");
   OD_CK(h, cudaSetDevice(h->device));
   od_pair_plan pl{};
   pl.nt = 256; pl.ipt = ions_per_lane; pl.variant = 7; pl.tile = tile;
@@ -766,7 +775,7 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
   const int shapes[][3] = {{256, 1, 0}, {128, 1, 0}, {256, 1, 1}, {128, 2, 2}, {256, 2, 2},
                            {128, 2, 3}, {256, 2, 3}, {128, 2, 4}, {256, 2, 4},
                            {128, 1, 5}, {256, 1, 5}, {128, 1, 6}, {256, 1, 6},
-                           {256, 2, 7}, {256, 4, 7}};
+                           {256, 2, 7}, {256, 4, 7}, {256, 8, 7}};
   const int sms = od_num_sms(h->device);
   cudaEvent_t e0, e1;
   OD_CK(h, cudaEventCreate(&e0));
@@ -1321,7 +1330,8 @@ extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes
   const int64_t P = std::max(cfg->n_grains, 1);
   int64_t b = 0;
   if (cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default((int)Np)) {
-    const int tile = od_n3_tile((int)Np, OD_N3_BUDGET);
+    int ipt = 0;
+    const int tile = od_n3_default((int)Np, OD_N3_BUDGET, &ipt);
     if (tile) b += (int64_t)(sizeof(float) * od_n3_floats((int)Np, tile));  // tile-pair sums
   }
   b += Np * 16 * 4;                 // pos, vel, fhi, flo

@@ -13,7 +13,8 @@ struct od_pair_plan {
   int variant; // 0: shared-memory broadcast, 1: warp-shuffle broadcast, 2: packed f32x2 with
                // SoA tiles (ipt 2), 3: as 2 with Newton reciprocals for half of the targets,
                // 4-6: further packed forms, 7: each unordered pair once (od_n3.cu)
-  int tile;    // variant 7: ions per tile (1024, 2048 or 4096); ipt = ions per lane (2 or 4)
+  int tile;    // variant 7: ions per tile (1024, 2048 or 4096); ipt = targets per lane (2, 4:
+               // as many sources; 8: two sources)
 };
 
 // Position views the all-pairs kernels read: float4 AoS, and SoA slices for variants 2-3.
@@ -41,10 +42,12 @@ struct od_dbufs {
 
 int od_num_sms(int device);
 
-// Variant 7 (od_n3.cu): default tile for a padded ion count whose partial-sum matrix fits the
-// byte budget (0: none fits), floats of that matrix, and the launch (pair kernel + fixed-order
-// row sums into slab 0 of ph/pl).
-int od_n3_tile(int Npad, size_t budget_bytes);
+// Variant 7 (od_n3.cu): whether (ions per lane, tile) has a kernel; the default (ions per lane,
+// tile) for a padded ion count whose tile-pair matrix fits the byte budget (returns the tile, 0
+// when none fits); floats of that matrix; and the launch (pair kernel + fixed-order row sums
+// into slab 0 of ph/pl).
+bool od_n3_supported(int ipt, int tile);
+int od_n3_default(int Npad, size_t budget_bytes, int* ipt);
 size_t od_n3_floats(int Npad, int tile);
 cudaError_t od_n3_prepare(const od_pair_plan& pl);  // shared-memory opt-in, current device
 cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,

@@ -7,20 +7,21 @@
 // (the reference's OpenMM CUDA nonbonded kernel also applies each pair force to both atoms).
 //
 // Decomposition
-//   * Ions are split into groups of G = 32·M (one warp: lane l owns the ions l + 32k, k < M)
-//     and tiles of T = PA·8·G ions (8 warps, PA passes).
-//   * One block per tile pair (a, b), a <= b. Warp w, pass p, holds target group
-//     ga = w + 8p of tile a in registers and sweeps the source groups of tile b in a staggered
-//     order (gb = (s + w·PA) mod groups-per-tile at step s), so that at every step the eight
-//     warps touch eight different source groups and a __syncthreads() between steps makes the
-//     shared-memory updates race-free.
+//   * A warp owns a target group of GT = 32·MT ions (lane l holds ions l + 32k, k < MT) and
+//     visits source groups of GS = 32·MS ions. Tiles hold T = PA·8·GT ions (8 warps, PA passes).
+//   * One block per tile pair (a, b), a <= b. Warp w, pass p, holds target group ga = w + 8p of
+//     tile a in registers and sweeps the source groups of tile b in a staggered order (group
+//     s + w·NBS/8 at step s), so that at every step the eight warps touch eight different
+//     source groups and a __syncthreads() between steps makes the shared-memory updates
+//     race-free.
 //   * Inside a group pair the sources rotate around the warp: at each of the 32 lane steps every
-//     lane evaluates its M targets against the M sources it holds (packed f32x2, two sources per
-//     operation), then passes its sources — positions and their FP32 reaction sums — to the
+//     lane evaluates its MT targets against the MS sources it holds (packed f32x2, two sources
+//     per operation), then passes the sources — positions and their FP32 reaction sums — to the
 //     previous lane. After 32 steps every source is back in its own lane with the sum of the
-//     M·32 target reactions on it.
-//   * Diagonal tiles (a == b) evaluate a group against itself as directed pairs (no reaction,
-//     self pair included: it contributes exactly 0) and skip groups below the diagonal.
+//     GT target reactions on it.
+//   * Diagonal tiles (a == b) evaluate the source groups inside a warp's own target group as
+//     directed pairs (no reaction; the self pair contributes exactly 0) and skip source groups
+//     below it.
 //   * Per target group the per-step FP32 sums are folded into two-float accumulators; reaction
 //     sums are folded into a two-float shared-memory slice of tile b.
 //   * Output: a dense matrix S[t][y] of two-float partial sums for the ions of tile t from the
@@ -63,22 +64,22 @@ __device__ __forceinline__ od_u64 shfl64(od_u64 v, int src) {
   return __shfl_sync(0xffffffffu, v, src);
 }
 
-// One group pair: 32 lane steps of M x M pair terms per lane with rotating sources.
-template <int M, bool REACT>
-__device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[M],
-                                         const od_u64 (&Y)[M], const od_u64 (&Z)[M],
-                                         od_u64 (&QX)[M / 2], od_u64 (&QY)[M / 2],
-                                         od_u64 (&QZ)[M / 2], od_u64 (&AX)[M], od_u64 (&AY)[M],
-                                         od_u64 (&AZ)[M], od_u64 (&RX)[M / 2],
-                                         od_u64 (&RY)[M / 2], od_u64 (&RZ)[M / 2], int src) {
+// One group pair: 32 lane steps of MT x MS pair terms per lane with rotating sources. Each
+// source pack moves on as soon as its terms are done, so that its shuffles overlap the next
+// pack's arithmetic.
+template <int MT, int MS, bool REACT>
+__device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[MT],
+                                         const od_u64 (&Y)[MT], const od_u64 (&Z)[MT],
+                                         od_u64 (&QX)[MS / 2], od_u64 (&QY)[MS / 2],
+                                         od_u64 (&QZ)[MS / 2], od_u64 (&AX)[MT], od_u64 (&AY)[MT],
+                                         od_u64 (&AZ)[MT], od_u64 (&RX)[MS / 2],
+                                         od_u64 (&RY)[MS / 2], od_u64 (&RZ)[MS / 2], int src) {
 #pragma unroll 1
   for (int st = 0; st < 32; st++) {
-    // each source pack moves on as soon as its terms are done, so that its shuffles overlap
-    // the next pack's arithmetic
 #pragma unroll
-    for (int q = 0; q < M / 2; q++) {
+    for (int q = 0; q < MS / 2; q++) {
 #pragma unroll
-      for (int kt = 0; kt < M; kt++)
+      for (int kt = 0; kt < MT; kt++)
         n3_pair<REACT>(k, X[kt], Y[kt], Z[kt], QX[q], QY[q], QZ[q], AX[kt], AY[kt], AZ[kt],
                        RX[q], RY[q], RZ[q]);
       QX[q] = shfl64(QX[q], src); QY[q] = shfl64(QY[q], src); QZ[q] = shfl64(QZ[q], src);
@@ -95,29 +96,32 @@ __device__ __forceinline__ void acc2x2(float& hi, float& lo, float h, float l) {
   lo = __fadd_rn(lo, l);
 }
 
-// Register and shared-memory budget per instantiation. With 4 ions per lane the target sums
-// live in shared memory for tiles up to 2048 ions, so that 80 registers per thread give three
-// blocks (24 warps) per SM; the 4096-ion tile keeps them in registers (two blocks per SM, the
-// shared-memory limit). Measured on GB300 at 2^20 ions: 2.91e12 pair terms/s against 2.73e12
-// for the two-block form.
-template <int M, int PA>
+// Register and shared-memory budget per instantiation (MT targets and MS sources per lane,
+// PA passes). The two-float target sums live in shared memory where registers are scarce:
+// 4 x 4 with tiles up to 2048 ions (80 registers, three blocks per SM) and 8 x 2 (128 registers,
+// two blocks per SM). Measured on GB300 at 2^20 ions, pair terms/s: 8 x 2 with 2048-ion tiles
+// 2.99e12, 4 x 4 with 2048-ion tiles 2.91e12 (two blocks per SM with the sums in registers:
+// 2.73e12), 4 x 2 2.89e12, 2 x 2 2.22e12.
+template <int MT, int MS, int PA>
 struct n3_traits {
-  static constexpr int T = PA * kWarps * 32 * M;
-  static constexpr bool HL_SMEM = M == 4 && T <= 2048;
-  static constexpr int MIN_BLOCKS = T <= 2048 ? 3 : 2;
-  static constexpr size_t SMEM = sizeof(float) * (6 * T + (HL_SMEM ? 6 * kWarps * 32 * M : 0));
+  static constexpr int GT = 32 * MT, GS = 32 * MS;  // target and source group sizes
+  static constexpr int T = PA * kWarps * GT;        // ions per tile
+  static constexpr int NBT = T / GT;                // target groups per tile
+  static constexpr int NBS = T / GS;                // source groups per tile (a power of two)
+  static constexpr bool HL_SMEM = (MT == 4 && T <= 2048) || MT == 8;
+  static constexpr int MIN_BLOCKS = MT == 8 ? 2 : (T <= 2048 ? 3 : 2);
+  static constexpr size_t SMEM = sizeof(float) * (6 * T + (HL_SMEM ? 6 * kWarps * GT : 0));
 };
 
-template <int M, int PA>
-__global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
+template <int MT, int MS, int PA>
+__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
     k_pairs_n3(const float* __restrict__ sx, const float* __restrict__ sy,
-               const float* __restrict__ sz, int ngroups, int nT, float* __restrict__ S,
+               const float* __restrict__ sz, int Npad, int nT, float* __restrict__ S,
                float rho0) {
-  constexpr int G = 32 * M;
-  constexpr int NBT = PA * kWarps;  // groups per tile (a power of two)
-  constexpr int T = NBT * G;        // ions per tile
-  constexpr bool HLS = n3_traits<M, PA>::HL_SMEM;
-  // [6][T]: hi x, y, z, lo x, y, z of tile b's ions; then (HLS) per warp [6][G] target sums
+  using TR = n3_traits<MT, MS, PA>;
+  constexpr int GT = TR::GT, GS = TR::GS, T = TR::T, NBT = TR::NBT, NBS = TR::NBS;
+  constexpr bool HLS = TR::HL_SMEM;
+  // [6][T]: hi x, y, z, lo x, y, z of tile b's ions; then (HLS) per warp [6][GT] target sums
   extern __shared__ float sm[];
   // tile pair (a, b), a <= b, from the block index (b-major upper triangle)
   const int kb = blockIdx.x;
@@ -127,6 +131,7 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
   const int a = kb - b * (b + 1) / 2;
   const bool diag = a == b;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
+  const int ngt = Npad / GT, ngs = Npad / GS;
   for (int e = tid; e < 6 * T; e += kWarps * 32) sm[e] = 0.f;
   __syncthreads();
   n3_consts k;
@@ -136,44 +141,47 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
   for (int p = 0; p < PA; p++) {
     const int ga = w + kWarps * p;
     const int GA = a * NBT + ga;
-    const bool ta_ok = GA < ngroups;
-    od_u64 X[M], Y[M], Z[M];
+    const bool ta_ok = GA < ngt;
+    od_u64 X[MT], Y[MT], Z[MT];
     // two-float target sums: registers, or this warp's shared-memory slice (lane-private words)
-    float hreg[HLS ? 1 : 6 * M];
-    float* const hsm = sm + 6 * T + w * 6 * G + lane;
-#define N3_H(c, kt) (HLS ? hsm[(c) * G + 32 * (kt)] : hreg[(c) * M + (kt)])
+    float hreg[HLS ? 1 : 6 * MT];
+    float* const hsm = sm + 6 * T + w * 6 * GT + lane;
+#define N3_H(c, kt) (HLS ? hsm[(c) * GT + 32 * (kt)] : hreg[(c) * MT + (kt)])
 #pragma unroll
-    for (int kt = 0; kt < M; kt++) {
-      const int i = (ta_ok ? GA : 0) * G + lane + 32 * kt;
+    for (int kt = 0; kt < MT; kt++) {
+      const int i = (ta_ok ? GA : 0) * GT + lane + 32 * kt;
       const float x = sx[i], y = sy[i], z = sz[i];
       X[kt] = p2(x, x); Y[kt] = p2(y, y); Z[kt] = p2(z, z);
 #pragma unroll
       for (int c = 0; c < 6; c++) N3_H(c, kt) = 0.f;
     }
-    for (int s = 0; s < NBT; s++) {
-      const int gb = (s + w * PA) & (NBT - 1);
-      const int GB = b * NBT + gb;
-      int mode = 0;  // 0: skip, 1: directed (the group against itself), 2: each pair once
-      if (ta_ok && GB < ngroups) mode = (!diag || gb > ga) ? 2 : (gb == ga ? 1 : 0);
+    for (int s = 0; s < NBS; s++) {
+      const int gb = (s + w * (NBS / kWarps)) & (NBS - 1);
+      const int GB = b * NBS + gb;
+      int mode = 0;  // 0: skip, 1: directed (sources inside the target group), 2: each pair once
+      if (ta_ok && GB < ngs) {
+        const int s0 = gb * GS, t0 = ga * GT;  // tile-local first ions (GS divides GT)
+        mode = (!diag || s0 >= t0 + GT) ? 2 : (s0 >= t0 ? 1 : 0);
+      }
       if (mode != 0) {
-        od_u64 QX[M / 2], QY[M / 2], QZ[M / 2], RX[M / 2], RY[M / 2], RZ[M / 2];
-        od_u64 AX[M], AY[M], AZ[M];
+        od_u64 QX[MS / 2], QY[MS / 2], QZ[MS / 2], RX[MS / 2], RY[MS / 2], RZ[MS / 2];
+        od_u64 AX[MT], AY[MT], AZ[MT];
 #pragma unroll
-        for (int q = 0; q < M / 2; q++) {
-          const int j = GB * G + lane + 64 * q;
+        for (int q = 0; q < MS / 2; q++) {
+          const int j = GB * GS + lane + 64 * q;
           QX[q] = p2(sx[j], sx[j + 32]);
           QY[q] = p2(sy[j], sy[j + 32]);
           QZ[q] = p2(sz[j], sz[j + 32]);
           RX[q] = RY[q] = RZ[q] = 0ull;
         }
 #pragma unroll
-        for (int kt = 0; kt < M; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
+        for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
         if (mode == 2)
-          n3_group<M, true>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
+          n3_group<MT, MS, true>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
         else
-          n3_group<M, false>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
+          n3_group<MT, MS, false>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
 #pragma unroll
-        for (int kt = 0; kt < M; kt++) {
+        for (int kt = 0; kt < MT; kt++) {
           od_acc2(N3_H(0, kt), N3_H(3, kt), sum2(AX[kt]));
           od_acc2(N3_H(1, kt), N3_H(4, kt), sum2(AY[kt]));
           od_acc2(N3_H(2, kt), N3_H(5, kt), sum2(AZ[kt]));
@@ -181,9 +189,9 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
         if (mode == 2) {
           // the force on the sources is minus the accumulated terms
 #pragma unroll
-          for (int q = 0; q < M / 2; q++) {
+          for (int q = 0; q < MS / 2; q++) {
             const float2 rx = up2(RX[q]), ry = up2(RY[q]), rz = up2(RZ[q]);
-            const int e0 = gb * G + lane + 64 * q, e1 = e0 + 32;
+            const int e0 = gb * GS + lane + 64 * q, e1 = e0 + 32;
             od_acc2(sm[e0], sm[3 * T + e0], -rx.x);
             od_acc2(sm[T + e0], sm[4 * T + e0], -ry.x);
             od_acc2(sm[2 * T + e0], sm[5 * T + e0], -rz.x);
@@ -199,8 +207,8 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
       if (diag) {
         // tile a is tile b: add the target sums to the same slice
 #pragma unroll
-        for (int kt = 0; kt < M; kt++) {
-          const int e = ga * G + lane + 32 * kt;
+        for (int kt = 0; kt < MT; kt++) {
+          const int e = ga * GT + lane + 32 * kt;
           acc2x2(sm[e], sm[3 * T + e], N3_H(0, kt), N3_H(3, kt));
           acc2x2(sm[T + e], sm[4 * T + e], N3_H(1, kt), N3_H(4, kt));
           acc2x2(sm[2 * T + e], sm[5 * T + e], N3_H(2, kt), N3_H(5, kt));
@@ -208,8 +216,8 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<M, PA>::MIN_BLOCKS))
       } else {
         float* o = S + ((size_t)a * nT + b) * (6 * (size_t)T);
 #pragma unroll
-        for (int kt = 0; kt < M; kt++) {
-          const int e = ga * G + lane + 32 * kt;
+        for (int kt = 0; kt < MT; kt++) {
+          const int e = ga * GT + lane + 32 * kt;
 #pragma unroll
           for (int c = 0; c < 6; c++) o[c * T + e] = N3_H(c, kt);
         }
@@ -257,47 +265,67 @@ __global__ void k_n3_reduce(const float* __restrict__ S, int nT, int T, int Npad
   pl[i] = make_float4(lx, ly, lz, 0.f);
 }
 
-template <int M, int PA>
+template <int MT, int MS, int PA>
 cudaError_t launch_n3(const od_pair_io& io, int Npad, float* S, float4* ph, float4* pl,
                       float rho0, cudaStream_t s) {
-  constexpr int T = PA * kWarps * 32 * M;
-  const int ngroups = Npad / (32 * M);
-  const int nT = (Npad + T - 1) / T;
-  const size_t smem = n3_traits<M, PA>::SMEM;
+  using TR = n3_traits<MT, MS, PA>;
+  const int nT = (Npad + TR::T - 1) / TR::T;
   const long long nblk = (long long)nT * (nT + 1) / 2;
-  k_pairs_n3<M, PA><<<(unsigned)nblk, kWarps * 32, smem, s>>>(io.sx, io.sy, io.sz, ngroups, nT,
-                                                              S, rho0);
-  k_n3_reduce<<<(Npad + 255) / 256, 256, 0, s>>>(S, nT, T, Npad, ph, pl);
+  k_pairs_n3<MT, MS, PA><<<(unsigned)nblk, kWarps * 32, TR::SMEM, s>>>(io.sx, io.sy, io.sz, Npad,
+                                                                      nT, S, rho0);
+  k_n3_reduce<<<(Npad + 255) / 256, 256, 0, s>>>(S, nT, TR::T, Npad, ph, pl);
   return cudaGetLastError();
 }
 
-template <int M, int PA>
+template <int MT, int MS, int PA>
 cudaError_t prepare_n3() {
-  return cudaFuncSetAttribute(k_pairs_n3<M, PA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)n3_traits<M, PA>::SMEM);
+  return cudaFuncSetAttribute(k_pairs_n3<MT, MS, PA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)n3_traits<MT, MS, PA>::SMEM);
 }
 
 }  // namespace
 
+// (plan ipt, tile) -> instantiation: ipt 2 and 4 take as many sources as targets per lane,
+// ipt 8 takes 8 targets and 2 sources per lane.
+#define OD_N3_CASES(CALL)                                                  \
+  case 21024: return CALL(2, 2, 2); case 22048: return CALL(2, 2, 4);      \
+  case 24096: return CALL(2, 2, 8); case 41024: return CALL(4, 4, 1);      \
+  case 42048: return CALL(4, 4, 2); case 44096: return CALL(4, 4, 4);      \
+  case 82048: return CALL(8, 2, 1); case 84096: return CALL(8, 2, 2);
+
+bool od_n3_supported(int ipt, int tile) {
+#define OD_N3_YES(a, b, c) true
+  switch (ipt * 10000 + tile) { OD_N3_CASES(OD_N3_YES) }
+#undef OD_N3_YES
+  return false;
+}
+
 cudaError_t od_n3_prepare(const od_pair_plan& pl) {
-  const int key = pl.ipt * 10000 + pl.tile;
-  switch (key) {
-    case 21024: return prepare_n3<2, 2>();
-    case 22048: return prepare_n3<2, 4>();
-    case 24096: return prepare_n3<2, 8>();
-    case 41024: return prepare_n3<4, 1>();
-    case 42048: return prepare_n3<4, 2>();
-    case 44096: return prepare_n3<4, 4>();
-  }
+#define OD_N3_PREP(a, b, c) prepare_n3<a, b, c>()
+  switch (pl.ipt * 10000 + pl.tile) { OD_N3_CASES(OD_N3_PREP) }
+#undef OD_N3_PREP
   return cudaErrorInvalidValue;
 }
 
-int od_n3_tile(int Npad, size_t budget_bytes) {
-  // 1024-ion tiles up to 2^17 ions (enough blocks for several waves), then 2048 (the fastest
-  // measured), then 4096, whichever first keeps the tile-pair matrix within the budget
-  const int first = Npad <= (1 << 17) ? 1024 : 2048;
-  for (int T = first; T <= 4096; T <<= 1)
-    if (sizeof(float) * od_n3_floats(Npad, T) <= budget_bytes) return T;
+cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
+                               float4* plo, float rho0, cudaStream_t s) {
+  if (!io.n3) return cudaErrorInvalidValue;
+#define OD_N3_LAUNCH(a, b, c) launch_n3<a, b, c>(io, Npad, io.n3, ph, plo, rho0, s)
+  switch (pl.ipt * 10000 + pl.tile) { OD_N3_CASES(OD_N3_LAUNCH) }
+#undef OD_N3_LAUNCH
+  return cudaErrorInvalidValue;
+}
+
+int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
+  // 4 x 4 with 1024-ion tiles up to 2^17 ions (2.87e12 pair terms/s at 2^17 against 2.85e12
+  // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.94e12 at 2^18, 2.99e12 at 2^20), then 4 x 4
+  // with 4096-ion tiles: the first whose tile-pair matrix fits the budget
+  const int cand[3][2] = {{4, 1024}, {8, 2048}, {4, 4096}};
+  for (int c = Npad <= (1 << 17) ? 0 : 1; c < 3; c++)
+    if (sizeof(float) * od_n3_floats(Npad, cand[c][1]) <= budget_bytes) {
+      *ipt = cand[c][0];
+      return cand[c][1];
+    }
   return 0;
 }
 
@@ -305,24 +333,4 @@ size_t od_n3_floats(int Npad, int T) {
   if (T <= 0) return 0;
   const size_t nT = (size_t)((Npad + T - 1) / T);
   return nT * nT * 6 * (size_t)T;
-}
-
-cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
-                               float4* plo, float rho0, cudaStream_t s) {
-  if (!io.n3) return cudaErrorInvalidValue;
-  // ipt selects the ions per lane (M); the tile fixes the passes per block
-  if (pl.ipt == 2) {
-    switch (pl.tile) {
-      case 1024: return launch_n3<2, 2>(io, Npad, io.n3, ph, plo, rho0, s);
-      case 2048: return launch_n3<2, 4>(io, Npad, io.n3, ph, plo, rho0, s);
-      case 4096: return launch_n3<2, 8>(io, Npad, io.n3, ph, plo, rho0, s);
-    }
-  } else if (pl.ipt == 4) {
-    switch (pl.tile) {
-      case 1024: return launch_n3<4, 1>(io, Npad, io.n3, ph, plo, rho0, s);
-      case 2048: return launch_n3<4, 2>(io, Npad, io.n3, ph, plo, rho0, s);
-      case 4096: return launch_n3<4, 4>(io, Npad, io.n3, ph, plo, rho0, s);
-    }
-  }
-  return cudaErrorInvalidValue;
 }
