@@ -372,11 +372,15 @@ def run_sweep(args, dist: Dist):
         members.append((holder, pos, vel, sim.N))
     t_setup = time.perf_counter() - t_setup
     ion_steps = sum(m[3] for m in members) * K
-    # plain path, back to back
+    # plain path, back to back, each simulation with its own default all-pairs plan
     plain_s = 0.0
-    plain_series = []
-    for holder, pos, vel, _ in members:
+    plain_series, same_plan = [], []
+    for holder, pos, vel, n in members:
         with _lib.Engine(holder) as eng:
+            pl = eng.pair_plan()
+            bp = _lib.batch_pair_plan(n)
+            same_plan.append((pl["threads"], pl["targets_per_thread"], pl["variant"]) == bp[:3] and
+                             (bp[2] != 7 or pl["jsplit"] == bp[3]))
             eng.set_state(pos, vel)
             eng.step(args.warmup)
             t0 = time.perf_counter()
@@ -391,8 +395,17 @@ def run_sweep(args, dist: Dist):
         batch.step(K)
         batch_s = time.perf_counter() - t0
         batch_dev_ms = batch.last_step_ms()
-        same = all(all(np.array_equal(batch.member(s).series(0, K + args.warmup)[q], ps[q]) for q in ps)
-                   for s, ps in zip(slots, plain_series))
+        # members whose batch plan is their plain default must match bitwise; the others (below
+        # 2^15 ions the batch takes the each-pair-once kernel, the plain path the directed one)
+        # differ by rounding: report the largest relative difference of the grain charge
+        same, qdiff = True, 0.0
+        for s, ps, sp in zip(slots, plain_series, same_plan):
+            bs = batch.member(s).series(0, K + args.warmup)
+            if sp:
+                same = same and all(np.array_equal(bs[q], ps[q]) for q in ps)
+            else:
+                qdiff = max(qdiff, float(np.max(np.abs(bs["q"] - ps["q"]) /
+                                                np.maximum(np.abs(ps["q"]), 1e-30))))
     per_sim_window_s = lambda sec: sec / K * window / S
     line = {"metric": "sweep sims/hour", "value": 3600.0 / per_sim_window_s(batch_s),
             "unit": "simulations/hour (5000-step windows, 64 seeded members)",
@@ -400,7 +413,9 @@ def run_sweep(args, dist: Dist):
             "steps": K, "warmup": args.warmup, "batched_step_ms": batch_s / K * 1e3,
             "batched_device_step_ms": batch_dev_ms / K, "plain_step_ms_sum": plain_s / K * 1e3,
             "ion_steps_per_s_batched": ion_steps / batch_s, "ion_steps_per_s_plain": ion_steps / plain_s,
-            "results_equal_bitwise": bool(same), "force_error_vs_plain": 0.0 if same else None,
+            "results_equal_bitwise": bool(same),
+            "bitwise_members": f"{sum(same_plan)} of {S} (same plan in both arms)",
+            "q_rel_diff_other_members": qdiff,
             "host_setup_s": t_setup, "n_ions": [int(m[3]) for m in members],
             "config": {"workload": "sweep: 64 members, N log-uniform 2^14-2^18, Mach 0.1-2, grain radius "
                                    "1-20 um log-uniform, 1-4 grains, mfp collisions with p=0.5"}}

@@ -149,6 +149,7 @@ def load(path: str | None = None):
         "od_batch_size": (c_int32, [c_void_p]),
         "od_batch_step": (c_int32, [c_void_p, c_int64]),
         "od_batch_last_step_ms": (c_int32, [c_void_p, _DP]),
+        "od_batch_pair_plan": (c_int32, [c_int64, POINTER(c_int32)]),
         "od_batch_destroy": (c_int32, [c_void_p]),
         "od_batch_last_error": (c_char_p, [c_void_p]),
         "od_config_device_bytes": (c_int32, [POINTER(od_config), POINTER(c_int64)]),
@@ -484,6 +485,14 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def batch_pair_plan(n_ions: int) -> tuple:
+    """(threads, targets per thread, variant, jsplit or tile) a batch member of n_ions steps
+    with; Engine.set_pair_plan(*plan) makes a single simulation bitwise equal to it."""
+    a = (c_int32 * 5)()
+    check(load().od_batch_pair_plan(int(n_ions), a), None)
+    return tuple(a[:4])
 
 
 def fp32_peak_tflops(device: int = 0) -> float:

@@ -1097,6 +1097,10 @@ struct od_batch {
   int4* d_items = nullptr;
   int2* d_blk_corr = nullptr;
   size_t c_sims = 0, c_blk_ion = 0, c_items = 0, c_blk_corr = 0;
+  int4* d_n3_items[2] = {nullptr, nullptr};
+  size_t c_n3_items[2] = {0, 0};
+  int2* d_n3_blk = nullptr;
+  size_t c_n3_blk = 0;
   unsigned int* d_next = nullptr;
   uint32_t* d_err = nullptr;
   od_batchview view{};
@@ -1156,7 +1160,12 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
   od_handle* h = nullptr;
   od_status st = create_handle(cfg, b->device, false, &h);
   if (st != OD_OK) return bfail(b, st, g_err);
-  if (h->plan.variant != 5 || h->plan.nt != 256 || h->plan.ipt != 1) {
+  // each unordered pair once when the member's tile-pair matrix fits, else the directed kernel
+  int ipt = 0;
+  const int tile = od_n3_batch_plan(h->Npad, OD_N3_BUDGET, &ipt);
+  st = tile ? set_plan_n3(h, ipt, tile) : OD_ERR_OOM;
+  if (st != OD_OK) {
+    cudaGetLastError();
     st = od_set_pair_plan(h, 256, 1, 5, 0);
     if (st != OD_OK) { std::string m = h->err; od_destroy(h); return bfail(b, st, m); }
   }
@@ -1212,6 +1221,8 @@ static od_status batch_rebuild(od_batch* b) {
   std::vector<int2> blk_ion, blk_corr;
   struct item { int4 w; long long work; };
   std::vector<item> items;
+  std::vector<int4> n3_items[2];
+  std::vector<int2> n3_blk;
   for (od_handle* h : b->members) {
     if (!h) continue;
     const int m = (int)sims.size();
@@ -1222,9 +1233,19 @@ static od_status batch_rebuild(od_batch* b) {
     d.rho0 = h->hp.rho0;
     const float nr = 64.0f * h->hp.rho0;
     d.newton_r2 = nr * nr;
+    d.n3_tile = h->plan.variant == 7 ? h->plan.tile : 0;
     sims.push_back(d);
     for (int lb = 0; lb < d.nb; lb++) blk_ion.push_back(make_int2(m, lb));
     for (int lb = 0; lb < d.nb + d.nrec; lb++) blk_corr.push_back(make_int2(m, lb));
+    if (d.n3_tile) {
+      // every tile pair of this member, in the table of its instantiation
+      const int nT = (d.Npad + d.n3_tile - 1) / d.n3_tile;
+      std::vector<int4>& t = n3_items[h->plan.ipt == 4 && d.n3_tile == 1024 ? 0 : 1];
+      for (int bb = 0; bb < nT; bb++)
+        for (int aa = 0; aa <= bb; aa++) t.push_back(make_int4(m, aa, bb, nT));
+      for (int lb = 0; lb < d.nb; lb++) n3_blk.push_back(make_int2(m, lb));
+      continue;
+    }
     for (int ib = 0; ib < d.Npad / 256; ib++)
       for (int js = 0; js < d.jsplit; js++) {
         const int j0 = js * d.chunk, j1 = std::min(j0 + d.chunk, d.Npad);
@@ -1239,6 +1260,10 @@ static od_status batch_rebuild(od_batch* b) {
   if ((st = upload_table(b, &b->d_blk_ion, &b->c_blk_ion, blk_ion)) != OD_OK) return st;
   if ((st = upload_table(b, &b->d_items, &b->c_items, w)) != OD_OK) return st;
   if ((st = upload_table(b, &b->d_blk_corr, &b->c_blk_corr, blk_corr)) != OD_OK) return st;
+  for (int k = 0; k < 2; k++)
+    if ((st = upload_table(b, &b->d_n3_items[k], &b->c_n3_items[k], n3_items[k])) != OD_OK)
+      return st;
+  if ((st = upload_table(b, &b->d_n3_blk, &b->c_n3_blk, n3_blk)) != OD_OK) return st;
   OD_BCK(b, cudaStreamSynchronize(b->stream));
   od_batchview& v = b->view;
   v.sims = b->d_sims; v.nsims = (int)sims.size();
@@ -1247,6 +1272,11 @@ static od_status batch_rebuild(od_batch* b) {
   v.blk_corr = b->d_blk_corr; v.nblk_corr = (int)blk_corr.size();
   v.pair_grid = od_num_sms(b->device) * 4;
   v.next = b->d_next; v.err = b->d_err;
+  for (int k = 0; k < 2; k++) {
+    v.n3_items[k] = b->d_n3_items[k];
+    v.n3_nitems[k] = (int)n3_items[k].size();
+  }
+  v.n3_blk = b->d_n3_blk; v.n3_nblk = (int)n3_blk.size();
   if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
   if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
   if (v.nsims > 0) {
@@ -1297,6 +1327,20 @@ extern "C" od_status od_batch_step(od_batch* b, int64_t nsteps) {
   return OD_OK;
 }
 
+extern "C" od_status od_batch_pair_plan(int64_t n_ions, int32_t* plan5) {
+  if (!plan5 || n_ions <= 0) return bfail(nullptr, OD_ERR_INVALID, "bad argument");
+  const int Npad = (int)(((n_ions + OD_PAD - 1) / OD_PAD) * OD_PAD);
+  int ipt = 0;
+  const int tile = od_n3_batch_plan(Npad, OD_N3_BUDGET, &ipt);
+  if (tile) {
+    plan5[0] = 256; plan5[1] = ipt; plan5[2] = 7; plan5[3] = tile; plan5[4] = Npad;
+  } else {
+    const od_pair_plan pl = default_plan(Npad, 152);
+    plan5[0] = pl.nt; plan5[1] = pl.ipt; plan5[2] = pl.variant; plan5[3] = 0; plan5[4] = 0;
+  }
+  return OD_OK;
+}
+
 extern "C" od_status od_batch_last_step_ms(const od_batch* b, double* ms) {
   if (!b || !ms) return OD_ERR_INVALID;
   *ms = b->last_ms;
@@ -1311,7 +1355,8 @@ extern "C" od_status od_batch_destroy(od_batch* b) {
     if (h) od_destroy(h);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  void* ptrs[] = {b->d_sims, b->d_blk_ion, b->d_items, b->d_blk_corr, b->d_next, b->d_err};
+  void* ptrs[] = {b->d_sims,         b->d_blk_ion,      b->d_items,  b->d_blk_corr, b->d_next,
+                  b->d_err,          b->d_n3_items[0], b->d_n3_items[1], b->d_n3_blk};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);

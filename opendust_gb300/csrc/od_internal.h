@@ -60,6 +60,7 @@ struct od_simdesc {
   od_dbufs b;
   int N, Npad, nb, jsplit, chunk, nrec;
   float rho0, newton_r2;
+  int n3_tile;  // variant-7 tile of this member (its tile-pair matrix is b.n3), 0 otherwise
 };
 // Device tables of one batch step.
 struct od_batchview {
@@ -74,8 +75,17 @@ struct od_batchview {
   int pair_grid;         // persistent blocks of the all-pairs stage
   unsigned int* next;    // work counter of the all-pairs stage
   uint32_t* err;
+  // members on variant 7: (member, tile a, tile b, tiles) per instantiation (0: 4 x 4 with
+  // 1024-ion tiles, 1: 8 x 2 with 2048-ion tiles), and (member, 256-ion block) row-sum blocks
+  const int4* n3_items[2];
+  int n3_nitems[2];
+  const int2* n3_blk;
+  int n3_nblk;
 };
 cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s);
+cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s);
+// Variant-7 plan of a batch member (ions per lane through ipt; returns the tile, 0: none fits).
+int od_n3_batch_plan(int Npad, size_t budget_bytes, int* ipt);
 
 // Uniform cell grid of the cutoff path (lambda units): cell (cx, cy, cz) spans
 // [lo + c*cx, lo + c*(cx+1)) per axis; ions outside the grid are clamped into border cells.

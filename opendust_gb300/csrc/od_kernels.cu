@@ -1339,9 +1339,13 @@ __global__ void __launch_bounds__(kBlk) k_b_tail(const od_simdesc* __restrict__ 
 
 cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s) {
   k_b_kick_drift<<<v.nblk_ion, kBlk, 0, s>>>(v.sims, v.blk_ion);
-  cudaError_t e = cudaMemsetAsync(v.next, 0, sizeof(unsigned int), s);
+  if (v.nitems > 0) {  // members on the directed-pair kernel
+    cudaError_t e = cudaMemsetAsync(v.next, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    k_b_pairs<<<v.pair_grid, 256, 0, s>>>(v.sims, v.items, v.nitems, v.next, v.err);
+  }
+  cudaError_t e = od_launch_batch_pairs_n3(v, s);
   if (e != cudaSuccess) return e;
-  k_b_pairs<<<v.pair_grid, 256, 0, s>>>(v.sims, v.items, v.nitems, v.next, v.err);
   k_b_kick_flag<<<v.nblk_ion, kBlk, 0, s>>>(v.sims, v.blk_ion);
   k_b_collect_inject<<<v.nsims, kCT, 0, s>>>(v.sims);
   k_b_correct_orbit<<<v.nblk_corr, kBlk, 0, s>>>(v.sims, v.blk_corr);

@@ -113,22 +113,18 @@ struct n3_traits {
   static constexpr size_t SMEM = sizeof(float) * (6 * T + (HL_SMEM ? 6 * kWarps * GT : 0));
 };
 
+// Tile pair (a, b), a <= b, of one simulation: one block. sm: dynamic shared memory of
+// n3_traits::SMEM bytes.
 template <int MT, int MS, int PA>
-__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
-    k_pairs_n3(const float* __restrict__ sx, const float* __restrict__ sy,
-               const float* __restrict__ sz, int Npad, int nT, float* __restrict__ S,
-               float rho0) {
+__device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
+                                             const float* __restrict__ sy,
+                                             const float* __restrict__ sz, int Npad, int nT,
+                                             float* __restrict__ S, float rho0, int a, int b,
+                                             float* sm) {
   using TR = n3_traits<MT, MS, PA>;
   constexpr int GT = TR::GT, GS = TR::GS, T = TR::T, NBT = TR::NBT, NBS = TR::NBS;
   constexpr bool HLS = TR::HL_SMEM;
-  // [6][T]: hi x, y, z, lo x, y, z of tile b's ions; then (HLS) per warp [6][GT] target sums
-  extern __shared__ float sm[];
-  // tile pair (a, b), a <= b, from the block index (b-major upper triangle)
-  const int kb = blockIdx.x;
-  int b = (int)((sqrtf(8.f * (float)kb + 1.f) - 1.f) * 0.5f);
-  while ((b + 1) * (b + 2) / 2 <= kb) b++;
-  while (b * (b + 1) / 2 > kb) b--;
-  const int a = kb - b * (b + 1) / 2;
+  // sm: [6][T] hi x, y, z, lo x, y, z of tile b's ions; then (HLS) per warp [6][GT] target sums
   const bool diag = a == b;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
   const int ngt = Npad / GT, ngs = Npad / GS;
@@ -230,11 +226,38 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   for (int e = tid; e < 6 * T; e += kWarps * 32) o[e] = sm[e];
 }
 
-// Row sums of S in a fixed order: slab 0 of (ph, pl) for every ion below Npad.
-__global__ void k_n3_reduce(const float* __restrict__ S, int nT, int T, int Npad,
-                            float4* __restrict__ ph, float4* __restrict__ pl) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= Npad) return;
+// (a, b) of the k-th pair of the b-major upper triangle
+__device__ __forceinline__ int2 tri_pair(int kb) {
+  int b = (int)((sqrtf(8.f * (float)kb + 1.f) - 1.f) * 0.5f);
+  while ((b + 1) * (b + 2) / 2 <= kb) b++;
+  while (b * (b + 1) / 2 > kb) b--;
+  return make_int2(kb - b * (b + 1) / 2, b);
+}
+
+template <int MT, int MS, int PA>
+__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
+    k_pairs_n3(const float* __restrict__ sx, const float* __restrict__ sy,
+               const float* __restrict__ sz, int Npad, int nT, float* __restrict__ S,
+               float rho0) {
+  extern __shared__ float sm[];
+  const int2 ab = tri_pair(blockIdx.x);
+  n3_tile_pair<MT, MS, PA>(sx, sy, sz, Npad, nT, S, rho0, ab.x, ab.y, sm);
+}
+
+// Batched form: block k takes work item k = (simulation, tile a, tile b) of a table that lists
+// every tile pair of every simulation using this instantiation.
+template <int MT, int MS, int PA>
+__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
+    k_b_pairs_n3(const od_simdesc* __restrict__ sims, const int4* __restrict__ items) {
+  extern __shared__ float sm[];
+  const int4 w = items[blockIdx.x];
+  const od_simdesc& d = sims[w.x];
+  n3_tile_pair<MT, MS, PA>(d.b.sx, d.b.sy, d.b.sz, d.Npad, w.w, d.b.n3, d.rho0, w.y, w.z, sm);
+}
+
+// Row sums of S in a fixed order: slab 0 of (ph, pl) for ion i < Npad.
+__device__ __forceinline__ void n3_row_sum(const float* __restrict__ S, int nT, int T, int i,
+                                           float4* __restrict__ ph, float4* __restrict__ pl) {
   const int t = i / T, e = i - t * T;
   float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
   const float* r = S + (size_t)t * nT * 6 * (size_t)T + e;
@@ -265,6 +288,20 @@ __global__ void k_n3_reduce(const float* __restrict__ S, int nT, int T, int Npad
   pl[i] = make_float4(lx, ly, lz, 0.f);
 }
 
+__global__ void k_n3_reduce(const float* __restrict__ S, int nT, int T, int Npad,
+                            float4* __restrict__ ph, float4* __restrict__ pl) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < Npad) n3_row_sum(S, nT, T, i, ph, pl);
+}
+
+// Batched row sums: block k covers 256 ions of the simulation in blk[k] (those using variant 7).
+__global__ void k_b_n3_reduce(const od_simdesc* __restrict__ sims, const int2* __restrict__ blk) {
+  const int2 e = blk[blockIdx.x];
+  const od_simdesc& d = sims[e.x];
+  n3_row_sum(d.b.n3, (d.Npad + d.n3_tile - 1) / d.n3_tile, d.n3_tile, e.y * 256 + threadIdx.x,
+             d.b.part_hi, d.b.part_lo);
+}
+
 template <int MT, int MS, int PA>
 cudaError_t launch_n3(const od_pair_io& io, int Npad, float* S, float4* ph, float4* pl,
                       float rho0, cudaStream_t s) {
@@ -279,8 +316,12 @@ cudaError_t launch_n3(const od_pair_io& io, int Npad, float* S, float4* ph, floa
 
 template <int MT, int MS, int PA>
 cudaError_t prepare_n3() {
-  return cudaFuncSetAttribute(k_pairs_n3<MT, MS, PA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)n3_traits<MT, MS, PA>::SMEM);
+  const int smem = (int)n3_traits<MT, MS, PA>::SMEM;
+  cudaError_t e = cudaFuncSetAttribute(k_pairs_n3<MT, MS, PA>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_b_pairs_n3<MT, MS, PA>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 }  // namespace
@@ -333,4 +374,26 @@ size_t od_n3_floats(int Npad, int T) {
   if (T <= 0) return 0;
   const size_t nT = (size_t)((Npad + T - 1) / T);
   return nT * nT * 6 * (size_t)T;
+}
+
+cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s) {
+  // the two instantiations batch members use (od_n3_batch_plan)
+  if (v.n3_nitems[0] > 0)
+    k_b_pairs_n3<4, 4, 1><<<v.n3_nitems[0], kWarps * 32, n3_traits<4, 4, 1>::SMEM, s>>>(
+        v.sims, v.n3_items[0]);
+  if (v.n3_nitems[1] > 0)
+    k_b_pairs_n3<8, 2, 1><<<v.n3_nitems[1], kWarps * 32, n3_traits<8, 2, 1>::SMEM, s>>>(
+        v.sims, v.n3_items[1]);
+  if (v.n3_nblk > 0) k_b_n3_reduce<<<v.n3_nblk, 256, 0, s>>>(v.sims, v.n3_blk);
+  return cudaGetLastError();
+}
+
+int od_n3_batch_plan(int Npad, size_t budget_bytes, int* ipt) {
+  // batch members: 4 x 4 with 1024-ion tiles up to 2^17 ions (also below 2^15, where the tile
+  // pairs of the other members fill the GPU), 8 x 2 with 2048-ion tiles above; 0 when the
+  // matrix does not fit (the member then takes the directed-pair kernel)
+  const int T = Npad <= (1 << 17) ? 1024 : 2048;
+  if (sizeof(float) * od_n3_floats(Npad, T) > budget_bytes) return 0;
+  *ipt = T == 1024 ? 4 : 8;
+  return T;
 }

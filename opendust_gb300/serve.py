@@ -156,8 +156,10 @@ class Server:
         return summarize(reqs, wall, gpu_ms)
 
 
-def run_plain(requests: list[Request], device: int = 0) -> dict:
-    """Baseline: the same requests, one at a time through the single-simulation path."""
+def run_plain(requests: list[Request], device: int = 0, batch_plan: bool = False) -> dict:
+    """Baseline: the same requests, one at a time through the single-simulation path (its
+    default all-pairs plan, or with batch_plan the plan the server's batch gives each request,
+    so that results are bitwise comparable)."""
     reqs = sorted(requests, key=lambda r: r.arrival)
     t0 = time.perf_counter()
     gpu_ms = 0.0
@@ -167,6 +169,8 @@ def run_plain(requests: list[Request], device: int = 0) -> dict:
             time.sleep(wait)
         holder, pos, vel = prepare(r, device)
         with _lib.Engine(holder, device) as eng:
+            if batch_plan:
+                eng.set_pair_plan(*_lib.batch_pair_plan(r.sim.N))
             if pos is None:
                 eng.init_state()
             else:

@@ -1,9 +1,10 @@
 """Batched simulations: results in a batch equal the same simulations stepped alone.
 
-Each batch member keeps its own buffers, source split and partial slabs, and the batched
-kernels run the same device code as the single-simulation kernels, so the comparison is
-bitwise (tolerance 0) — alone, in a fixed mix, and with members joining and leaving between
-steps (continuous batching).
+Each batch member keeps its own buffers and partial sums, and the batched kernels run the same
+device code as the single-simulation kernels with the member's all-pairs plan
+(_lib.batch_pair_plan), so the comparison with a single simulation given that plan is bitwise
+(tolerance 0) — alone, in a fixed mix, and with members joining and leaving between steps
+(continuous batching).
 """
 import numpy as np
 import pytest
@@ -27,6 +28,7 @@ def member(N, P, seed, collisions, n=24):
 
 def alone(holder, pos, vel, steps):
     with _lib.Engine(holder) as eng:
+        eng.set_pair_plan(*_lib.batch_pair_plan(eng.n))
         eng.set_state(pos, vel)
         eng.step(steps)
         s = eng.series(0, steps)
@@ -75,6 +77,7 @@ def test_batch_continuous_membership(gpu_lib):
         # the later member's first 8 steps equal its solo run
         s = m.series(0, 8)
     with _lib.Engine(c[0]) as eng:
+        eng.set_pair_plan(*_lib.batch_pair_plan(eng.n))
         eng.set_state(c[1], c[2])
         eng.step(8)
         s8 = eng.series(0, 8)

@@ -21,7 +21,7 @@ def test_server_results_equal_alone(gpu_lib):
     mixed = copy.deepcopy(reqs)
     stats = serve.Server(chunk=6).run(mixed)
     alone = copy.deepcopy(reqs)
-    base = serve.run_plain(alone)
+    base = serve.run_plain(alone, batch_plan=True)
     print(f"server: {stats}\nplain: {base}")
     for a, b in zip(sorted(mixed, key=lambda r: r.rid), sorted(alone, key=lambda r: r.rid)):
         for k in a.series:
