@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 1
+#define OD_ABI_VERSION 2
 
 typedef enum od_status {
   OD_OK = 0,
@@ -55,8 +55,17 @@ typedef enum od_status {
   OD_ERR_CAPACITY = 7      /* an output buffer given by the caller is too small */
 } od_status;
 
-/* distributionType (opendust.py:261, :302): "Maxwellian" / "fieldDriven" */
-enum { OD_DIST_MAXWELLIAN = 0, OD_DIST_FIELD_DRIVEN = 1 };
+/* distributionType (opendust.py:261, :302): "Maxwellian" / "fieldDriven"; MATTHEWS is the
+ * plasma model of the reference's chains/matthews.py fork (PlasmaParametersInSIUnitsMatthews,
+ * matthews.py:50-112): shifted-Maxwellian inflow through the top face only, per-DOF
+ * charge-exchange collisions, specular reflection at the side wall (matthews.py:653-682). */
+enum { OD_DIST_MAXWELLIAN = 0, OD_DIST_FIELD_DRIVEN = 1, OD_DIST_MATTHEWS = 2 };
+/* ion trap: the 14-term even polynomial alpha[] (opendust.py:499-577), the fork's radial
+ * polynomial with height-dependent coefficients alpha_k(h) tabulated on uniform knots and
+ * interpolated by natural cubic splines (OpenMM Continuous1DFunction, matthews.py:395-478), or
+ * none (simulate(considerTrap=False), matthews.py:505-514). */
+enum { OD_TRAP_POLY = 0, OD_TRAP_TABLE = 1, OD_TRAP_NONE = 2 };
+#define OD_MAX_TRAP 128
 /* chargeCalculationMethod (opendust.py:1120, :1153): "given" / "consistent" / "oml" */
 enum { OD_CHARGE_GIVEN = 0, OD_CHARGE_CONSISTENT = 1, OD_CHARGE_OML = 2 };
 /* ion–neutral collisions.
@@ -140,6 +149,25 @@ typedef struct od_config {
   const double* grain_r;
   const double* grain_q0;
   const int32_t* grain_method; /* OD_CHARGE_* */
+  /* external field order (matthews.py:481-495): 0 uniform E (fieldDriven and the fork's
+   * order 0); 2: E(z) = E + field_alpha z + field_beta z^2 for field_z1 <= z <= field_z7,
+   * E(field_z1) below and E(field_z7) above (the derivative of the fork's potential).
+   * Units V/m, V/m^2, V/m^3, m. Applies to MATTHEWS; fieldDriven uses order 0 with E. */
+  int32_t field_order;
+  int32_t trap_kind;        /* OD_TRAP_* */
+  double field_alpha, field_beta, field_z1, field_z7;
+  /* OD_TRAP_TABLE: trap_tab[k * trap_n + j] = alpha_k at h_j = -H/2 + j H/(trap_n - 1),
+   * k = 0..4 (coefficients of rho^0, rho^2, .., rho^8, rho = r/r_D_e, dimensionless as the
+   * fork's fit returns them); 4 <= trap_n <= OD_MAX_TRAP. Zero outside [-H/2, H/2]. */
+  int32_t trap_n;
+  const double* trap_tab;
+  /* per-grain factors of the host tail, or NULL: grain_field[p] is the field at grain p
+   * [V/m] so that forceExternalField_z = q_p * grain_field[p] (NULL: E for fieldDriven, 0
+   * otherwise); grain_out[3p..3p+2] is the out-of-domain trap force per unit grain charge
+   * [N/C] for OD_TRAP_TABLE (the fork evaluates it with quartic splines of the table,
+   * matthews.py:978-1007; NULL: zero). */
+  const double* grain_field;
+  const double* grain_out;
 } od_config;
 
 typedef struct od_handle od_handle;
@@ -173,6 +201,35 @@ od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64
  * streams OD_RNG_INIT_X / OD_RNG_INIT_V with the configuration's seed. Then computes the
  * ion–ion sums like od_set_state. */
 od_status od_init_state(od_handle* h, const double* vz_v, const double* vz_cdf, int32_t vz_n);
+
+/* Screened potential of the current ions at grid points: pot[j * n_r + i] =
+ * sum over ions of exp(-r)/(r + r_0) with r the distance from (gr[i], 0, gz[j]) in units of
+ * r_D_e (FP64, fixed summation order). Replaces the CuPy loop of the fork's trap fit
+ * (matthews.py:397-421), which evaluates this sum from the simulation's own ions. */
+od_status od_ion_potential_grid(od_handle* h, const double* gr, const double* gz, int32_t n_r,
+                                int32_t n_z, double* pot);
+
+/* Replaces the fork's trap force setup (matthews.py:423-478: the fitted or file-read table
+ * and its Continuous1DFunctions): switches the handle to OD_TRAP_TABLE with trap_tab / trap_n
+ * as in od_config (n = 0: OD_TRAP_NONE) and the per-grain out-of-domain factors grain_out
+ * [P][3] (N/C, may be NULL). Takes effect at the next step. */
+od_status od_set_trap_table(od_handle* h, const double* trap_tab, int32_t n,
+                            const double* grain_out);
+
+/* Moves the grains and sets their charges between windows, keeping the ions resident (the
+ * dust-dynamics driver of the reference, examples/DustDynamics/TwoParticles/launch.py:120-224,
+ * rebuilds the OpenDust object each iteration and passes the ions through a restart file).
+ * x, y, z [m], q [C] per grain; grain_field [P] and grain_out [P][3] as in od_config (NULL
+ * keeps the current factors). The ion–ion sums are unchanged; the grain forces on the ions
+ * follow at the next step. */
+od_status od_set_grains(od_handle* h, const double* x, const double* y, const double* z,
+                        const double* q, const double* grain_field, const double* grain_out);
+
+/* Starts a new result window: the next step writes series row 0 and restarts the time
+ * averages; the ion state, the grain charges and the random streams continue (the Philox
+ * step counter keeps counting across windows). No counterpart in the reference: it creates
+ * a new simulation per window (launch.py:120-145). */
+od_status od_begin_window(od_handle* h);
 
 /* Replaces context.getState(...).getPositions/getVelocities (opendust.py:1074-1078, :1102-1105). */
 od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n);

@@ -12,12 +12,14 @@ from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint64, c_vo
 
 import numpy as np
 
-OD_ABI_VERSION = 1
+OD_ABI_VERSION = 2
 OD_MAX_GRAINS = 16
 OD_MAX_TABLE = 256
 OD_NTAB = 4
 OD_TAB_TOP, OD_TAB_BOTTOM, OD_TAB_SIDE, OD_TAB_VZ = 0, 1, 2, 3
-OD_DIST_MAXWELLIAN, OD_DIST_FIELD_DRIVEN = 0, 1
+OD_DIST_MAXWELLIAN, OD_DIST_FIELD_DRIVEN, OD_DIST_MATTHEWS = 0, 1, 2
+OD_TRAP_POLY, OD_TRAP_TABLE, OD_TRAP_NONE = 0, 1, 2
+OD_MAX_TRAP = 128
 OD_CHARGE = {"given": 0, "consistent": 1, "oml": 2}
 OD_COLL_NONE, OD_COLL_PER_DOF, OD_COLL_MFP = 0, 1, 2
 OD_FORCE_ALLPAIRS, OD_FORCE_CUTOFF = 0, 1
@@ -88,6 +90,16 @@ class od_config(ctypes.Structure):
         ("grain_r", _DP),
         ("grain_q0", _DP),
         ("grain_method", POINTER(c_int32)),
+        ("field_order", c_int32),
+        ("trap_kind", c_int32),
+        ("field_alpha", c_double),
+        ("field_beta", c_double),
+        ("field_z1", c_double),
+        ("field_z7", c_double),
+        ("trap_n", c_int32),
+        ("trap_tab", _DP),
+        ("grain_field", _DP),
+        ("grain_out", _DP),
     ]
 
 
@@ -150,6 +162,10 @@ def load(path: str | None = None):
         "od_batch_step": (c_int32, [c_void_p, c_int64]),
         "od_batch_last_step_ms": (c_int32, [c_void_p, _DP]),
         "od_batch_pair_plan": (c_int32, [c_int64, POINTER(c_int32)]),
+        "od_ion_potential_grid": (c_int32, [H, _DP, _DP, c_int32, c_int32, _DP]),
+        "od_set_trap_table": (c_int32, [H, _DP, c_int32, _DP]),
+        "od_set_grains": (c_int32, [H, _DP, _DP, _DP, _DP, _DP, _DP]),
+        "od_begin_window": (c_int32, [H]),
         "od_batch_destroy": (c_int32, [c_void_p]),
         "od_batch_last_error": (c_char_p, [c_void_p]),
         "od_config_device_bytes": (c_int32, [POINTER(od_config), POINTER(c_int64)]),
@@ -214,8 +230,16 @@ def make_config(
     probs: tuple,
     tables: list,
     grains: dict,
+    field: dict | None = None,
+    trap_table: np.ndarray | None = None,
+    trap_none: bool = False,
+    grain_field=None,
+    grain_out=None,
 ) -> ConfigHolder:
-    """Fill an od_config from plain Python/numpy values (SI units)."""
+    """Fill an od_config from plain Python/numpy values (SI units). field: order-2 field of the
+    chains/matthews.py fork {"order", "alpha", "beta", "z1", "z7"}; trap_table: (5, n) alpha_k
+    at uniform heights over [-H/2, H/2] (OD_TRAP_TABLE); trap_none: no trap (OD_TRAP_NONE);
+    grain_field [P] (V/m) and grain_out [P, 3] (N/C): per-grain tail factors."""
     c = od_config()
     c.abi_version = OD_ABI_VERSION
     c.distribution = distribution
@@ -258,6 +282,29 @@ def make_config(
     c.grain_x, c.grain_y, c.grain_z = _dptr(garr["x"]), _dptr(garr["y"]), _dptr(garr["z"])
     c.grain_r, c.grain_q0 = _dptr(garr["r"]), _dptr(garr["q0"])
     c.grain_method = gm.ctypes.data_as(POINTER(c_int32))
+    if field:
+        c.field_order = int(field.get("order", 0))
+        c.field_alpha = float(field.get("alpha", 0.0))
+        c.field_beta = float(field.get("beta", 0.0))
+        c.field_z1 = float(field.get("z1", 0.0))
+        c.field_z7 = float(field.get("z7", 0.0))
+    c.trap_kind = OD_TRAP_NONE if trap_none else OD_TRAP_POLY
+    if trap_table is not None:
+        tt = np.ascontiguousarray(trap_table, dtype=np.float64)
+        if tt.ndim != 2 or tt.shape[0] != 5 or not 4 <= tt.shape[1] <= OD_MAX_TRAP:
+            raise ValueError("trap table must have shape (5, n), 4 <= n <= OD_MAX_TRAP")
+        keep.append(tt)
+        c.trap_kind = OD_TRAP_TABLE
+        c.trap_n = tt.shape[1]
+        c.trap_tab = _dptr(tt)
+    if grain_field is not None:
+        gf = np.ascontiguousarray(grain_field, dtype=np.float64)
+        keep.append(gf)
+        c.grain_field = _dptr(gf)
+    if grain_out is not None:
+        go = np.ascontiguousarray(grain_out, dtype=np.float64).reshape(-1)
+        keep.append(go)
+        c.grain_out = _dptr(go)
     return ConfigHolder(c, keep)
 
 
@@ -354,6 +401,39 @@ class Engine:
         check(self._lib.od_get_timing(self.h, ctypes.byref(sm), ctypes.byref(st), ctypes.byref(pm),
                                       ctypes.byref(pl)), self.h)
         return sm.value, st.value, pm.value, pl.value
+
+    def ion_potential_grid(self, gr, gz) -> np.ndarray:
+        """(len(gz), len(gr)) screened potential of the current ions at (gr[i], 0, gz[j]) in
+        units of r_D_e (the fork's trap-fit grid)."""
+        gr = np.ascontiguousarray(gr, dtype=np.float64)
+        gz = np.ascontiguousarray(gz, dtype=np.float64)
+        pot = np.empty((len(gz), len(gr)))
+        check(self._lib.od_ion_potential_grid(self.h, _dptr(gr), _dptr(gz), len(gr), len(gz),
+                                              _dptr(pot)), self.h)
+        return pot
+
+    def set_trap_table(self, table, grain_out=None):
+        """Tabulated trap (5, n) alpha_k(h) (None: no trap) and per-grain out-of-domain factors."""
+        if table is None:
+            check(self._lib.od_set_trap_table(self.h, None, 0, None), self.h)
+            return
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        go = None if grain_out is None else np.ascontiguousarray(grain_out, dtype=np.float64)
+        check(self._lib.od_set_trap_table(self.h, _dptr(t), t.shape[1],
+                                          None if go is None else _dptr(go)), self.h)
+
+    def set_grains(self, x, y, z, q, grain_field=None, grain_out=None):
+        """Move the grains and set their charges (SI); ions stay resident."""
+        arr = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, q)]
+        gf = None if grain_field is None else np.ascontiguousarray(grain_field, dtype=np.float64)
+        go = None if grain_out is None else np.ascontiguousarray(grain_out, dtype=np.float64)
+        check(self._lib.od_set_grains(self.h, *[_dptr(a) for a in arr],
+                                      None if gf is None else _dptr(gf),
+                                      None if go is None else _dptr(go)), self.h)
+
+    def begin_window(self):
+        """Restart the result series at row 0 (ion state and random streams continue)."""
+        check(self._lib.od_begin_window(self.h), self.h)
 
     def set_pair_plan(self, threads: int, targets_per_thread: int, variant: int, jsplit: int = 0):
         """All-pairs work decomposition; for variant 7 `jsplit` is the tile size in ions."""

@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <cstddef>
 #include <cstdlib>
 #include <mutex>
 #include <string>
@@ -107,8 +108,17 @@ static od_status validate(const od_config* c) {
   if (c->n_grains < 0 || c->n_grains > OD_MAX_GRAINS)
     return fail(nullptr, OD_ERR_INVALID, "n_grains must be in [0, 16]");
   if (c->n_steps < 1) return fail(nullptr, OD_ERR_INVALID, "n_steps must be >= 1");
-  if (c->distribution != OD_DIST_MAXWELLIAN && c->distribution != OD_DIST_FIELD_DRIVEN)
-    return fail(nullptr, OD_ERR_INVALID, "distribution must be Maxwellian or fieldDriven");
+  if (c->distribution < OD_DIST_MAXWELLIAN || c->distribution > OD_DIST_MATTHEWS)
+    return fail(nullptr, OD_ERR_INVALID, "distribution must be Maxwellian, fieldDriven or Matthews");
+  if (c->field_order != 0 && c->field_order != 2)
+    return fail(nullptr, OD_ERR_INVALID, "field_order must be 0 or 2");
+  if (c->field_order == 2 && !(c->field_z7 >= c->field_z1))
+    return fail(nullptr, OD_ERR_INVALID, "field order 2 needs field_z1 <= field_z7");
+  if (c->trap_kind < OD_TRAP_POLY || c->trap_kind > OD_TRAP_NONE)
+    return fail(nullptr, OD_ERR_INVALID, "unknown trap kind");
+  if (c->trap_kind == OD_TRAP_TABLE &&
+      (c->trap_n < 4 || c->trap_n > OD_MAX_TRAP || !c->trap_tab))
+    return fail(nullptr, OD_ERR_INVALID, "a trap table needs 4..OD_MAX_TRAP knots");
   if (c->collision_model < OD_COLL_NONE || c->collision_model > OD_COLL_MFP)
     return fail(nullptr, OD_ERR_INVALID, "unknown collision model");
   if (c->collision_model == OD_COLL_MFP && !(c->mfp > 0))
@@ -140,6 +150,43 @@ static od_status validate(const od_config* c) {
   return OD_OK;
 }
 
+// Natural cubic spline through y[0..n-1] on uniform knots of spacing d (second derivative zero
+// at both ends, as OpenMM's Continuous1DFunction): coef[j] = (c0, c1, c2, c3) of
+// y_j + c1 t + c2 t^2 + c3 t^3 on [h_j, h_j+1], t = h - h_j. Tridiagonal solve (Thomas) in FP64.
+static void natural_spline(const double* y, int n, double d, double (*coef)[4]) {
+  std::vector<double> M(n, 0.0), cp(n, 0.0), dp(n, 0.0);
+  // rows j = 1..n-2: M[j-1] + 4 M[j] + M[j+1] = 6 (y[j+1] - 2 y[j] + y[j-1]) / d^2
+  for (int j = 1; j < n - 1; j++) {
+    const double r = 6.0 * (y[j + 1] - 2.0 * y[j] + y[j - 1]) / (d * d);
+    const double den = 4.0 - (j > 1 ? cp[j - 1] : 0.0);
+    cp[j] = 1.0 / den;
+    dp[j] = (r - (j > 1 ? dp[j - 1] : 0.0)) / den;
+  }
+  for (int j = n - 2; j >= 1; j--) M[j] = dp[j] - cp[j] * (j < n - 2 ? M[j + 1] : 0.0);
+  for (int j = 0; j < n - 1; j++) {
+    coef[j][0] = y[j];
+    coef[j][1] = (y[j + 1] - y[j]) / d - d * (2.0 * M[j] + M[j + 1]) / 6.0;
+    coef[j][2] = M[j] / 2.0;
+    coef[j][3] = (M[j + 1] - M[j]) / (6.0 * d);
+  }
+}
+
+// Tabulated trap (OD_TRAP_TABLE): knots over [-Hh/2, Hh/2] (lambda), coefficients times -A_ii.
+static void fill_trap_table(od_dparams* p, const double* tab, int n, double Hh, double A_ii) {
+  p->trap_kind = n > 0 ? OD_TRAP_TABLE : OD_TRAP_NONE;
+  p->ttn = n;
+  if (n <= 0) return;
+  const double d = Hh / (n - 1);
+  p->th0 = (float)(-Hh / 2.0); p->th1 = (float)(Hh / 2.0);
+  p->tdh = (float)d; p->tinv_dh = (float)(1.0 / d);
+  std::vector<double> c((size_t)(n - 1) * 4);
+  for (int k = 0; k < 5; k++) {
+    natural_spline(tab + (size_t)k * n, n, d, reinterpret_cast<double(*)[4]>(c.data()));
+    for (int j = 0; j < n - 1; j++)
+      for (int m = 0; m < 4; m++) p->tcf[k][j][m] = (float)(-A_ii * c[(size_t)j * 4 + m]);
+  }
+}
+
 static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   memset(p, 0, sizeof(*p));
   const double pi = OD_PI_D;
@@ -160,7 +207,18 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->rho0 = (float)(c->r_0 / lam);
   const double Rh = c->R / lam, Hh = c->H / lam;
   p->Rh = (float)Rh; p->Hh = (float)Hh; p->Hh_half = (float)(Hh / 2.0);
-  p->a_field = c->distribution == OD_DIST_FIELD_DRIVEN ? (float)(c->E * q_s * dt * dt / (m_s * lam)) : 0.f;
+  const double sf = q_s * dt * dt / (m_s * lam);  // field [V/m] -> acceleration (lambda/d_t^2)
+  p->a_field = c->distribution != OD_DIST_MAXWELLIAN ? (float)(c->E * sf) : 0.f;
+  p->field_order = c->distribution == OD_DIST_MATTHEWS ? c->field_order : 0;
+  if (p->field_order == 2) {
+    p->fa0 = (float)(c->E * sf);
+    p->fa1 = (float)(c->field_alpha * lam * sf);
+    p->fa2 = (float)(c->field_beta * lam * lam * sf);
+    p->fz1 = (float)(c->field_z1 / lam);
+    p->fz7 = (float)(c->field_z7 / lam);
+  }
+  p->trap_kind = c->trap_kind;
+  if (c->trap_kind == OD_TRAP_TABLE) fill_trap_table(p, c->trap_tab, c->trap_n, Hh, A_ii);
   const double vunit = lam / dt;
   p->vT = (float)(c->v_T / vunit);
   p->vfl = (float)(c->v_fl / vunit);
@@ -184,6 +242,9 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
     p->gxs[g] = c->grain_x[g]; p->gys[g] = c->grain_y[g]; p->gzs[g] = c->grain_z[g];
     p->grs[g] = c->grain_r[g];
     p->gmethod[g] = c->grain_method[g];
+    p->gfield[g] = c->grain_field ? c->grain_field[g]
+                                  : (c->distribution == OD_DIST_FIELD_DRIVEN ? c->E : 0.0);
+    for (int d = 0; d < 3; d++) p->gout[g][d] = c->grain_out ? c->grain_out[3 * g + d] : 0.0;
   }
   p->Rh2 = Rh * Rh;
   p->Hh_half_d = Hh / 2.0;
@@ -507,6 +568,101 @@ extern "C" od_status od_init_state(od_handle* h, const double* vz_v, const doubl
   st = check_device_err(h);
   if (st == OD_ERR_STATE) return fail(h, OD_ERR_STATE, "no position outside the grains was found");
   return st;
+}
+
+extern "C" od_status od_ion_potential_grid(od_handle* h, const double* gr, const double* gz,
+                                           int32_t n_r, int32_t n_z, double* pot) {
+  if (!h || !gr || !gz || !pot) return fail(h, OD_ERR_INVALID, "NULL argument");
+  if (n_r < 1 || n_z < 1 || (int64_t)n_r * n_z > (1 << 20))
+    return fail(h, OD_ERR_INVALID, "grid must have 1..2^20 points");
+  if (!h->state_set) return fail(h, OD_ERR_STATE, "no ion state set");
+  OD_CK(h, cudaSetDevice(h->device));
+  const int npts = n_r * n_z;
+  std::vector<double> pts((size_t)2 * npts);
+  for (int j = 0; j < n_z; j++)
+    for (int i = 0; i < n_r; i++) {
+      pts[2 * ((size_t)j * n_r + i)] = gr[i];
+      pts[2 * ((size_t)j * n_r + i) + 1] = gz[j];
+    }
+  double *d_pts = nullptr, *d_out = nullptr;
+  OD_CK(h, cudaMalloc((void**)&d_pts, sizeof(double) * pts.size()));
+  cudaError_t e = cudaMalloc((void**)&d_out, sizeof(double) * npts);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_pts, pts.data(), sizeof(double) * pts.size(), cudaMemcpyHostToDevice,
+                        h->stream);
+  if (e == cudaSuccess)
+    e = od_launch_grid_potential(h->b.pos, h->N, d_pts, npts, h->cfg.r_0 / h->cfg.r_D_e, d_out,
+                                 h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(pot, d_out, sizeof(double) * npts, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(d_pts);
+  if (d_out) cudaFree(d_out);
+  if (e != cudaSuccess) return cuda_fail(h, e, "od_ion_potential_grid");
+  return OD_OK;
+}
+
+extern "C" od_status od_set_trap_table(od_handle* h, const double* trap_tab, int32_t n,
+                                       const double* grain_out) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (n != 0 && (n < 4 || n > OD_MAX_TRAP || !trap_tab))
+    return fail(h, OD_ERR_INVALID, "a trap table needs 4..OD_MAX_TRAP knots");
+  OD_CK(h, cudaSetDevice(h->device));
+  const double lam = h->cfg.r_D_e, dt = h->cfg.d_t;
+  const double k = 1.0 / (h->cfg.eps_0 * 4.0 * OD_PI_D);
+  const double q_s = fabs(h->cfg.e) * h->cfg.N_s, m_s = h->cfg.m_i * h->cfg.N_s;
+  const double A_ii = k * q_s * q_s * dt * dt / (m_s * lam * lam * lam);
+  fill_trap_table(&h->hp, trap_tab, n, h->cfg.H / lam, A_ii);
+  for (int g = 0; g < h->P; g++)
+    for (int d = 0; d < 3; d++) h->hp.gout[g][d] = grain_out ? grain_out[3 * g + d] : 0.0;
+  h->cfg.trap_kind = h->hp.trap_kind;
+  h->cfg.trap_n = n;
+  OD_CK(h, cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_set_grains(od_handle* h, const double* x, const double* y,
+                                   const double* z, const double* q, const double* grain_field,
+                                   const double* grain_out) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (h->P > 0 && (!x || !y || !z || !q)) return fail(h, OD_ERR_INVALID, "NULL argument");
+  OD_CK(h, cudaSetDevice(h->device));
+  const double lam = h->cfg.r_D_e;
+  od_dparams& p = h->hp;
+  for (int g = 0; g < h->P; g++) {
+    const double gx = x[g] / lam, gy = y[g] / lam, gz = z[g] / lam;
+    p.gx[g] = gx; p.gy[g] = gy; p.gz[g] = gz;
+    split2(gx, p.gxh[g], p.gxl[g]);
+    split2(gy, p.gyh[g], p.gyl[g]);
+    split2(gz, p.gzh[g], p.gzl[g]);
+    p.gxs[g] = x[g]; p.gys[g] = y[g]; p.gzs[g] = z[g];
+    if (grain_field) p.gfield[g] = grain_field[g];
+    if (grain_out)
+      for (int d = 0; d < 3; d++) p.gout[g][d] = grain_out[3 * g + d];
+  }
+  OD_CK(h, cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, cudaMemcpyAsync(reinterpret_cast<char*>(h->ds) + offsetof(od_dstate, q_param), q,
+                           sizeof(double) * h->P, cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, od_launch_set_charges(h->dp, h->ds, h->b.cq, h->P, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_begin_window(od_handle* h) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  OD_CK(h, cudaSetDevice(h->device));
+  od_dstate s;
+  OD_CK(h, cudaMemcpyAsync(&s, h->ds, sizeof(s), cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  s.rng_base += s.step;
+  s.step = 0;
+  memset(s.avg, 0, sizeof(s.avg));
+  s.n_avg = 0;
+  OD_CK(h, cudaMemcpyAsync(h->ds, &s, sizeof(s), cudaMemcpyHostToDevice, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->step = 0;
+  return OD_OK;
 }
 
 extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n) {

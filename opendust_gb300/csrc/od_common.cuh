@@ -50,11 +50,26 @@ struct od_dparams {
   double gxs[OD_MAX_GRAINS], gys[OD_MAX_GRAINS], gzs[OD_MAX_GRAINS], grs[OD_MAX_GRAINS];
   int32_t gmethod[OD_MAX_GRAINS];
   int64_t n_steps, avg_start;
+  // external field of order 2 (chains/matthews.py:481-495) in acceleration units:
+  // a_z = fa0 + fa1 zc + fa2 zc^2 with zc = z clamped to [fz1, fz7]
+  int32_t field_order, trap_kind;
+  float fa0, fa1, fa2, fz1, fz7;
+  // tabulated trap (OD_TRAP_TABLE): knots th0 + j*tdh, j < ttn, on [th0, th1] (lambda);
+  // tcf[k][j] = -A_ii times the natural-cubic-spline coefficients (c0..c3 in powers of h - h_j)
+  // of alpha_k on [h_j, h_j+1]
+  int32_t ttn;
+  float th0, th1, tdh, tinv_dh;
+  float tcf[5][OD_MAX_TRAP][4];
+  // FP64 tail factors: field at each grain [V/m] and out-of-domain trap force per unit
+  // charge [N/C] (OD_TRAP_TABLE)
+  double gfield[OD_MAX_GRAINS];
+  double gout[OD_MAX_GRAINS][3];
 };
 
 // Per-simulation FP64 accumulators and bookkeeping, resident in device memory.
 struct od_dstate {
-  int64_t step;                       // next step index
+  int64_t step;                       // next step index (series row) of the current window
+  int64_t rng_base;                   // Philox step counter of series row 0 (windows)
   uint32_t err;                       // OD_DERR_* bits
   int32_t nlist;                      // flagged ions this step
   double q_param[OD_MAX_GRAINS];      // charges the ion forces use (q at the previous step)
@@ -186,6 +201,10 @@ __device__ __forceinline__ float od_pair_c_cut(float r2, const od_dparams& p) {
 __device__ __forceinline__ float3 od_ext_accel(const od_dparams& p, const float* cq, float x,
                                                float y, float z) {
   float ax = 0.f, ay = 0.f, az = p.a_field;
+  if (p.field_order == 2) {  // chains/matthews.py:484-495, the field clamped outside [z1, z7]
+    const float zc = fminf(fmaxf(z, p.fz1), p.fz7);
+    az = fmaf(fmaf(p.fa2, zc, p.fa1), zc, p.fa0);
+  }
   for (int g = 0; g < p.P; g++) {
     float dx = (x - p.gxh[g]) - p.gxl[g];
     float dy = (y - p.gyh[g]) - p.gyl[g];
@@ -195,6 +214,29 @@ __device__ __forceinline__ float3 od_ext_accel(const od_dparams& p, const float*
     float c = cq[g] * ri * ri * ri;
     ax = fmaf(c, dx, ax); ay = fmaf(c, dy, ay); az = fmaf(c, dz, az);
   }
+  if (p.trap_kind == OD_TRAP_TABLE) {
+    // -A_ii grad [alpha_0(h) + alpha_1(h) u + .. + alpha_4(h) u^4], u = x^2 + y^2, h = z
+    // (chains/matthews.py:463-478); the tabulated functions are zero outside [-H/2, H/2]
+    if (z >= p.th0 && z <= p.th1) {
+      const int j = min((int)((z - p.th0) * p.tinv_dh), p.ttn - 2);
+      const float t = z - fmaf((float)j, p.tdh, p.th0);
+      const float u = fmaf(x, x, y * y);
+      float Pu = 0.f, Pz = 0.f;
+#pragma unroll
+      for (int k = 4; k >= 0; k--) {
+        const float* c = p.tcf[k][j];
+        const float a = fmaf(fmaf(fmaf(c[3], t, c[2]), t, c[1]), t, c[0]);
+        const float da = fmaf(fmaf(3.f * c[3], t, 2.f * c[2]), t, c[1]);
+        if (k > 0) Pu = fmaf(Pu, u, (float)k * a);
+        Pz = fmaf(Pz, u, da);
+      }
+      ax = fmaf(2.f * x, Pu, ax);
+      ay = fmaf(2.f * y, Pu, ay);
+      az += Pz;
+    }
+    return make_float3(ax, ay, az);
+  }
+  if (p.trap_kind == OD_TRAP_NONE) return make_float3(ax, ay, az);
   const float* t = p.trapc;
   float u = fmaf(x, x, y * y), w = z * z;
   // P_u and P_w of the 14-term even polynomial; t[k] = -2 A_ii alpha_k

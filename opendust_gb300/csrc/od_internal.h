@@ -83,6 +83,9 @@ struct od_batchview {
   int n3_nblk;
 };
 cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s);
+// pot[k] = sum over ions i < N of exp(-r)/(r + rho0), r = |(pts[2k], 0, pts[2k+1]) - x_i|
+cudaError_t od_launch_grid_potential(const float4* pos, int N, const double* pts, int npts,
+                                     double rho0, double* out, cudaStream_t s);
 cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s);
 // Variant-7 plan of a batch member (ions per lane through ipt; returns the tile, 0: none fits).
 int od_n3_batch_plan(int Npad, size_t budget_bytes, int* ipt);

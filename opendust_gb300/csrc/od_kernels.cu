@@ -419,7 +419,7 @@ __device__ __forceinline__ void kick_drift_body(const od_dparams& p, const od_ds
                                                 float* __restrict__ sz, int i) {
   if (i >= p.N) return;
   float4 x = pos[i], v = vel[i];
-  if (p.coll != OD_COLL_NONE) collide(p, (uint32_t)i, (uint32_t)ds->step, v);
+  if (p.coll != OD_COLL_NONE) collide(p, (uint32_t)i, (uint32_t)(ds->step + ds->rng_base), v);
   const float4 gh = fhi[i], gl = flo[i];
   float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
   a.x = fmaf(p.A_ii, gh.x + gl.x, a.x);
@@ -643,7 +643,32 @@ __device__ __forceinline__ void collect_inject_body(
     my = block_sum_1024(my); mz = block_sum_1024(mz);
     if (tid == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
   }
-  const uint32_t step = (uint32_t)ds->step;
+  const uint32_t step = (uint32_t)(ds->step + ds->rng_base);
+  if (p.dist == OD_DIST_MATTHEWS) {
+    // the fork (chains/matthews.py:653-682): ions past |z| = H/2 or inside a grain re-enter
+    // through the top face; ions past the side wall keep their position and have the radial
+    // velocity component reversed, with the normal taken before any re-injection
+    const int grains = (1 << p.P) - 1;
+    for (int k = tid; k < K; k += kCT) {
+      const int i = list[k];
+      const int bits = list_bits[k];
+      const float4 xo = list_old[k];
+      float4 x = xo, v = list_v[k];
+      if (bits & (grains | (1 << 29))) inject_one(p, (uint32_t)i, step, x, v);
+      if (bits & (1 << 30)) {
+        const float rr = sqrtf(fmaf(xo.x, xo.x, xo.y * xo.y));
+        const float nx = xo.x / rr, ny = xo.y / rr;
+        const float vn = fmaf(v.x, nx, v.y * ny);          // dot(v, n)
+        const float vt = fmaf(v.x, ny, -v.y * nx);         // dot(v, tau), tau = (y, -x)/rho
+        v.x = fmaf(-vn, nx, vt * ny);
+        v.y = fmaf(-vn, ny, -vt * nx);
+      }
+      pos[i] = x;
+      vel[i] = v;
+      list_new[k] = x;
+    }
+    return;
+  }
   for (int k = tid; k < K; k += kCT) {
     const int i = list[k];
     float4 x, v;
@@ -891,8 +916,10 @@ __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __rest
       const double kk = p.k * qn[g] * qn[j] / (r * r * r);
       fd[0] += kk * dx; fd[1] += kk * dy; fd[2] += kk * dz;
     }
-    double fo[3];
-    out_domain_force(p, p.gxs[g], p.gys[g], p.gzs[g], qn[g], fo);
+    double fo[3] = {0, 0, 0};
+    if (p.trap_kind == OD_TRAP_POLY) out_domain_force(p, p.gxs[g], p.gys[g], p.gzs[g], qn[g], fo);
+    else if (p.trap_kind == OD_TRAP_TABLE)
+      for (int d = 0; d < 3; d++) fo[d] = qn[g] * p.gout[g][d];
     const double so = qn[g] * p.k * p.q_s / (p.lam * p.lam);
     const double sc = p.vunit * p.m_s / p.dt;
     double vals[13];
@@ -901,7 +928,7 @@ __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __rest
       vals[1 + d] = S[g * 3 + d] * so + fo[d];
       vals[4 + d] = ds->M[g][d] * sc;
       vals[7 + d] = fd[d];
-      vals[10 + d] = (d == 2 && p.dist == OD_DIST_FIELD_DRIVEN) ? qn[g] * p.E : 0.0;
+      vals[10 + d] = d == 2 ? qn[g] * p.gfield[g] : 0.0;
     }
     const size_t r = (size_t)step * P + g;
     s_q[r] = vals[0];
@@ -1336,6 +1363,37 @@ __global__ void __launch_bounds__(kBlk) k_b_tail(const od_simdesc* __restrict__ 
 }
 
 }  // namespace
+
+// Screened potential of the ions at grid points (the fork's trap fit, chains/matthews.py:
+// 397-421): one block per point, FP64 terms in a fixed order (per-thread strided sums, then a
+// fixed tree).
+__global__ void __launch_bounds__(kBlk) k_grid_potential(const float4* __restrict__ pos, int N,
+                                                         const double* __restrict__ pts,
+                                                         double rho0, double* __restrict__ out) {
+  __shared__ double red[kBlk];
+  const double gx = pts[2 * blockIdx.x], gz = pts[2 * blockIdx.x + 1];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < N; i += kBlk) {
+    const float4 x = pos[i];
+    const double dx = gx - x.x, dy = -(double)x.y, dz = gz - x.z;
+    const double r = sqrt(dx * dx + dy * dy + dz * dz);
+    acc += exp(-r) / (r + rho0);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kBlk / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+cudaError_t od_launch_grid_potential(const float4* pos, int N, const double* pts, int npts,
+                                     double rho0, double* out, cudaStream_t s) {
+  if (npts <= 0) return cudaSuccess;
+  k_grid_potential<<<npts, kBlk, 0, s>>>(pos, N, pts, rho0, out);
+  return cudaGetLastError();
+}
 
 cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s) {
   k_b_kick_drift<<<v.nblk_ion, kBlk, 0, s>>>(v.sims, v.blk_ion);

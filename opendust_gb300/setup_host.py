@@ -228,3 +228,77 @@ def write_restart(path: str, pos: np.ndarray, vel: np.ndarray):
     with open(path, "w") as f:
         for p, v in zip(pos * 1e9, vel / NMPS):
             f.write("{}\t{}\t{}\t{}\t{}\t{}\n".format(p[0], p[1], p[2], v[0], v[1], v[2]))
+
+
+# ----------------------------------------------------------------- chains/matthews.py fork
+def matthews_trap_grid(R: float, H: float, r_D_e: float):
+    """Grid of the fork's trap fit in units of r_D_e (chains/matthews.py:398-405): int(10 R)
+    radii on [0, R] and int(10 H) heights on [-H/2, H/2]."""
+    Rh, Hh = R / r_D_e, H / r_D_e
+    return np.linspace(0.0, Rh, int(Rh * 10)), np.linspace(-Hh / 2.0, Hh / 2.0, int(Hh * 10))
+
+
+def fit_trap_table(pot: np.ndarray, grid_R: np.ndarray, N: int) -> np.ndarray:
+    """Per-height least squares of the fork (chains/matthews.py:420-440): pot[j, i] is the
+    summed screened potential of the N ions at (grid_R[i], 0, h_j); returns alpha (5, n_h),
+    alpha[k, j] the coefficient of rho^(2k) at height h_j (rho in units of r_D_e)."""
+    potential = np.asarray(pot, dtype=np.float64) / float(N)
+    A = np.vstack([np.ones(len(grid_R)), grid_R ** 2, grid_R ** 4, grid_R ** 6, grid_R ** 8]).T
+    alpha = np.zeros((5, potential.shape[0]))
+    for j in range(potential.shape[0]):
+        alpha[:, j] = -np.linalg.lstsq(A, potential[j], rcond=None)[0] * N
+    return alpha
+
+
+def read_trap_table(path: str) -> np.ndarray:
+    """Trap file of the fork (chains/matthews.py:441-453): one height per line, the five
+    coefficients tab-separated. Returns (5, n)."""
+    return np.loadtxt(path, delimiter="\t", ndmin=2)[:, :5].T.copy()
+
+
+def write_trap_table(path: str, alpha: np.ndarray):
+    """Same format (chains/matthews.py:827-833)."""
+    with open(path, "w") as f:
+        for j in range(alpha.shape[1]):
+            f.write("{}\t{}\t{}\t{}\t{}\n".format(*(alpha[k][j] for k in range(5))))
+
+
+def trap_table_out_factor(alpha: np.ndarray, H: float, r_D_e: float, eps_0: float, q_s: float,
+                          grains_xyz) -> np.ndarray:
+    """Out-of-domain trap force on each grain per unit grain charge [N/C] for the tabulated
+    trap (chains/matthews.py:975-1013): quartic interpolating splines of the alpha_k(h) rows
+    (scipy UnivariateSpline k=4, s=0, as the fork) and their derivatives at the grain height.
+    Returns (P, 3)."""
+    from scipy.interpolate import UnivariateSpline
+
+    hs = np.linspace(-H / r_D_e / 2.0, H / r_D_e / 2.0, alpha.shape[1])
+    spl = [UnivariateSpline(hs, alpha[k], k=4, s=0) for k in range(5)]
+    der = [s.derivative() for s in spl]
+    k = 1.0 / (eps_0 * 4.0 * np.pi)
+    L = r_D_e
+    out = np.zeros((len(grains_xyz), 3))
+    for p, (x, y, z) in enumerate(grains_xyz):
+        r = np.sqrt(x ** 2 + y ** 2)
+        h = z / L
+        fR = (-2 * float(spl[1](h)) * r) / L ** 2
+        fR += (-4 * float(spl[2](h)) * r ** 3) / L ** 4
+        fR += (-6 * float(spl[3](h)) * r ** 5) / L ** 6
+        fR += (-8 * float(spl[4](h)) * r ** 7) / L ** 8
+        fR *= k * q_s / L
+        fH = (-float(der[0](h))) / L
+        fH += (-float(der[1](h)) * r ** 2) / L ** 2 / L
+        fH += (-float(der[2](h)) * r ** 4) / L ** 4 / L
+        fH += (-float(der[3](h)) * r ** 6) / L ** 6 / L
+        fH += (-float(der[4](h)) * r ** 8) / L ** 8 / L
+        fH *= k * q_s / L
+        out[p] = (0.0, 0.0, fH) if r == 0 else (fR * x / r, fR * y / r, fH)
+    return out
+
+
+def matthews_field_at(order: int, Phi: dict, z: float) -> float:
+    """Field along z at a grain [V/m] as the fork's tail uses it (chains/matthews.py:1086-1095):
+    E_0 for order 0, E_0 + alpha z + beta z^2 (not clamped) for order 2."""
+    E0 = Phi["E_0"][0]
+    if order == 2:
+        return E0 + Phi["alpha"][0] * z + Phi["beta"][0] * z ** 2
+    return E0

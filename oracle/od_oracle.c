@@ -84,7 +84,38 @@ typedef struct {
   int tn[OD_NTAB];
   double tv[OD_NTAB][OD_MAX_TABLE], txi[OD_NTAB][OD_MAX_TABLE], tsl[OD_NTAB][OD_MAX_TABLE];
   double p_t, p_s, p_b;
+  /* chains/matthews.py fork: field of order 2 (acceleration units, z in lambda), tabulated
+   * trap (natural cubic splines of alpha_k(h), h in lambda), per-grain tail factors */
+  int field_order, trap_kind, ttn;
+  double fa0, fa1, fa2, fz1, fz7;
+  double th0, tdh;
+  double tcf[5][OD_MAX_TRAP][4];
+  double gfield[OD_MAX_GRAINS], gout[OD_MAX_GRAINS][3];
 } odo_par;
+
+/* Natural cubic spline (zero second derivative at both ends: OpenMM's Continuous1DFunction)
+ * through y[0..n-1] on knots of spacing d. Second derivatives from the tridiagonal system
+ * M[j-1] + 4 M[j] + M[j+1] = 6 (y[j+1] - 2 y[j] + y[j-1]) / d^2, solved by Gaussian elimination
+ * without pivoting; coef[j] = (y_j, slope, M_j / 2, (M_j+1 - M_j) / (6 d)) in powers of h - h_j. */
+static void spline_natural(const double* y, int n, double d, double (*coef)[4]) {
+  double M[OD_MAX_TRAP] = {0}, diag[OD_MAX_TRAP], rhs[OD_MAX_TRAP];
+  for (int j = 1; j < n - 1; j++) {
+    diag[j] = 4.0;
+    rhs[j] = 6.0 * (y[j + 1] - 2.0 * y[j] + y[j - 1]) / (d * d);
+  }
+  for (int j = 2; j < n - 1; j++) {
+    double m = 1.0 / diag[j - 1];
+    diag[j] -= m;
+    rhs[j] -= m * rhs[j - 1];
+  }
+  for (int j = n - 2; j >= 1; j--) M[j] = (rhs[j] - (j < n - 2 ? M[j + 1] : 0.0)) / diag[j];
+  for (int j = 0; j < n - 1; j++) {
+    coef[j][0] = y[j];
+    coef[j][1] = (y[j + 1] - y[j]) / d - d * (2.0 * M[j] + M[j + 1]) / 6.0;
+    coef[j][2] = M[j] / 2.0;
+    coef[j][3] = (M[j + 1] - M[j]) / (6.0 * d);
+  }
+}
 
 static int make_par(const od_config* c, odo_par* p) {
   if (!c || c->abi_version != OD_ABI_VERSION) return 1;
@@ -102,8 +133,24 @@ static int make_par(const od_config* c, odo_par* p) {
   p->rho0 = c->r_0 / c->r_D_e;
   p->Rh = c->R / c->r_D_e; p->Hh = c->H / c->r_D_e;
   p->Rh2 = p->Rh * p->Rh; p->Hh_half = p->Hh / 2.0;
-  p->a_field = (c->distribution == OD_DIST_FIELD_DRIVEN)
-                   ? c->E * p->q_s * c->d_t * c->d_t / (p->m_s * c->r_D_e) : 0.0;
+  double sf = p->q_s * c->d_t * c->d_t / (p->m_s * c->r_D_e); /* V/m -> lambda/d_t^2 */
+  p->a_field = (c->distribution != OD_DIST_MAXWELLIAN) ? c->E * sf : 0.0;
+  p->field_order = c->distribution == OD_DIST_MATTHEWS ? c->field_order : 0;
+  if (p->field_order == 2) { /* chains/matthews.py:484-495 */
+    p->fa0 = c->E * sf;
+    p->fa1 = c->field_alpha * c->r_D_e * sf;
+    p->fa2 = c->field_beta * c->r_D_e * c->r_D_e * sf;
+    p->fz1 = c->field_z1 / c->r_D_e;
+    p->fz7 = c->field_z7 / c->r_D_e;
+  }
+  p->trap_kind = c->trap_kind;
+  if (c->trap_kind == OD_TRAP_TABLE) { /* chains/matthews.py:463-478 */
+    if (c->trap_n < 4 || c->trap_n > OD_MAX_TRAP || !c->trap_tab) return 1;
+    p->ttn = c->trap_n;
+    p->th0 = -c->H / c->r_D_e / 2.0;
+    p->tdh = c->H / c->r_D_e / (c->trap_n - 1);
+    for (int k = 0; k < 5; k++) spline_natural(c->trap_tab + (size_t)k * c->trap_n, c->trap_n, p->tdh, p->tcf[k]);
+  }
   p->vT = c->v_T / p->vunit; p->vfl = c->v_fl / p->vunit;
   p->p_coll = c->d_t * c->w_c;
   if (c->collision_model == OD_COLL_MFP) {
@@ -119,6 +166,9 @@ static int make_par(const od_config* c, odo_par* p) {
     p->gz[g] = c->grain_z[g] / c->r_D_e;
     double r = c->grain_r[g] / c->r_D_e;
     p->gr2[g] = r * r;
+    p->gfield[g] = c->grain_field ? c->grain_field[g]
+                                  : (c->distribution == OD_DIST_FIELD_DRIVEN ? c->E : 0.0);
+    for (int d = 0; d < 3; d++) p->gout[g][d] = c->grain_out ? c->grain_out[3 * g + d] : 0.0;
   }
   for (int t = 0; t < OD_NTAB; t++) {
     p->tn[t] = c->tab_n[t];
@@ -184,6 +234,36 @@ static void trap_accel(const double* al, double A, double x, double y, double z,
   a[2] = -A * 2 * z * Pw;
 }
 
+/* tabulated trap (chains/matthews.py:463-478): -A grad [alpha_0(h) + alpha_1(h) u + .. +
+ * alpha_4(h) u^4], u = x^2 + y^2, h = z; zero outside [-H/2, H/2] */
+static void trap_table_accel(const odo_par* p, double x, double y, double z, double* a) {
+  a[0] = a[1] = a[2] = 0.0;
+  double h1 = p->th0 + p->tdh * (p->ttn - 1);
+  if (z < p->th0 || z > h1) return;
+  int j = (int)floor((z - p->th0) / p->tdh);
+  if (j > p->ttn - 2) j = p->ttn - 2;
+  double t = z - (p->th0 + j * p->tdh), u = x * x + y * y;
+  double Pu = 0.0, Pz = 0.0, un = 1.0, um = 1.0; /* dP/du = sum_k k alpha_k u^(k-1), dP/dh */
+  for (int k = 0; k <= 4; k++) {
+    const double* c = p->tcf[k][j];
+    double al = c[0] + c[1] * t + c[2] * t * t + c[3] * t * t * t;
+    double dal = c[1] + 2.0 * c[2] * t + 3.0 * c[3] * t * t;
+    Pz += dal * un; /* un = u^k */
+    if (k > 0) { Pu += k * al * um; um *= u; } /* um = u^(k-1) */
+    un *= u;
+  }
+  a[0] = -p->A_ii * 2.0 * x * Pu;
+  a[1] = -p->A_ii * 2.0 * y * Pu;
+  a[2] = -p->A_ii * Pz;
+}
+
+/* field along z: uniform, or of order 2 with z clamped to [z1, z7] (chains/matthews.py:484-495) */
+static double field_accel(const odo_par* p, double z) {
+  if (p->field_order != 2) return p->a_field;
+  double zc = z < p->fz1 ? p->fz1 : (z > p->fz7 ? p->fz7 : z);
+  return p->fa0 + p->fa1 * zc + p->fa2 * zc * zc;
+}
+
 /* total acceleration: ion–ion + grains (opendust.py:350-352) + trap + field (opendust.py:580-585) */
 static void accel_total(const odo_par* p, const double* alpha, int64_t n, const double* x,
                         const double* qp, double* a) {
@@ -198,11 +278,12 @@ static void accel_total(const odo_par* p, const double* alpha, int64_t n, const 
       double c = p->A_id * qp[g] / (r2 * sqrt(r2));
       ax += c * dx; ay += c * dy; az += c * dz;
     }
-    double t[3];
-    trap_accel(alpha, p->A_ii, xi, yi, zi, t);
+    double t[3] = {0, 0, 0};
+    if (p->trap_kind == OD_TRAP_POLY) trap_accel(alpha, p->A_ii, xi, yi, zi, t);
+    else if (p->trap_kind == OD_TRAP_TABLE) trap_table_accel(p, xi, yi, zi, t);
     a[3 * i] = ax + t[0];
     a[3 * i + 1] = ay + t[1];
-    a[3 * i + 2] = az + t[2] + p->a_field;
+    a[3 * i + 2] = az + t[2] + field_accel(p, zi);
   }
 }
 
@@ -452,9 +533,10 @@ int odo_inject(const od_config* c, int64_t ion, int64_t step, double* x, double*
  * pos [m] / vel [m/s] (n x 3) are updated in place; q_param[P] holds the charges the forces
  * use (q at the previous step) and is updated; per-step outputs (row i = step first_step+i):
  * q_out[P], f_orbit/f_collect/f_dust/f_field[P*3], n_inj (ions re-injected), dN[P].
- * round32 != 0 rounds the initial state to float first (the device representation). */
+ * round32 != 0 rounds the initial state to float first (the device representation).
+ * rng_base: Philox step counter of step 0, for later windows whose random streams continue. */
 int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32,
-            int64_t first_step, int64_t nsteps, double* q_param, double* q_out,
+            int64_t first_step, int64_t nsteps, int64_t rng_base, double* q_param, double* q_out,
             double* f_orbit, double* f_collect, double* f_dust, double* f_field,
             int64_t* n_inj, int64_t* dN_out) {
   odo_par* p = (odo_par*)malloc(sizeof(odo_par));
@@ -473,8 +555,8 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
   for (int g = 0; g < P; g++) q[g] = q_param[g];
 
   for (int64_t s = 0; s < nsteps; s++) {
-    int64_t step = first_step + s;
-    uint32_t st = (uint32_t)step;
+    int64_t step = first_step + s;        /* step of the window: step 0 keeps the charges */
+    uint32_t st = (uint32_t)(rng_base + step); /* Philox step counter (continues across windows) */
     if (p->coll != OD_COLL_NONE)
       for (int64_t i = 0; i < n; i++) collide(p, (uint32_t)i, st, v + 3 * i);
     /* addUpdateContextState; v += 0.5 dt f/m; x += dt v; v += 0.5 dt f/m (opendust.py:864-877) */
@@ -495,8 +577,27 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
         }
     }
     /* re-injection (opendust.py:923-975) */
-    for (int64_t i = 0; i < n; i++)
-      if (fl[i]) { inject_one(p, (uint32_t)i, st, x + 3 * i, v + 3 * i); ninj++; }
+    if (p->dist == OD_DIST_MATTHEWS) {
+      /* chains/matthews.py:653-682: past |z| = H/2 or inside a grain -> top face; past the side
+       * wall -> radial velocity reversed with the normal of the position before re-injection */
+      int grains = (1 << P) - 1;
+      for (int64_t i = 0; i < n; i++) {
+        if (!fl[i]) continue;
+        double xo = x[3 * i], yo = x[3 * i + 1];
+        if (fl[i] & (grains | (1 << 29))) inject_one(p, (uint32_t)i, st, x + 3 * i, v + 3 * i);
+        if (fl[i] & (1 << 30)) {
+          double rr = sqrt(xo * xo + yo * yo), nx = xo / rr, ny = yo / rr;
+          double vx = v[3 * i], vy = v[3 * i + 1];
+          double vn = vx * nx + vy * ny, vt = vx * ny - vy * nx;
+          v[3 * i] = -vn * nx + vt * ny;
+          v[3 * i + 1] = -vn * ny - vt * nx;
+        }
+        ninj++;
+      }
+    } else {
+      for (int64_t i = 0; i < n; i++)
+        if (fl[i]) { inject_one(p, (uint32_t)i, st, x + 3 * i, v + 3 * i); ninj++; }
+    }
     /* orbit sums on the re-injected positions (opendust.py:977-1037) */
     double S[OD_MAX_GRAINS][3];
     memset(S, 0, sizeof(S));
@@ -525,8 +626,11 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
         double kk = p->k * qn[g] * qn[j] / (r * r * r);
         fd[0] += kk * dx; fd[1] += kk * dy; fd[2] += kk * dz;
       }
-      double fo[3];
-      out_domain_force(c, p, c->grain_x[g], c->grain_y[g], c->grain_z[g], qn[g], fo);
+      double fo[3] = {0, 0, 0};
+      if (p->trap_kind == OD_TRAP_POLY)
+        out_domain_force(c, p, c->grain_x[g], c->grain_y[g], c->grain_z[g], qn[g], fo);
+      else if (p->trap_kind == OD_TRAP_TABLE)
+        for (int d = 0; d < 3; d++) fo[d] = qn[g] * p->gout[g][d];
       double so = qn[g] * p->k * p->q_s / (p->lam * p->lam);
       double sc = p->vunit * p->m_s / c->d_t;
       if (q_out) q_out[s * P + g] = qn[g];
@@ -534,8 +638,7 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
         if (f_orbit) f_orbit[(s * P + g) * 3 + d] = S[g][d] * so + fo[d];
         if (f_collect) f_collect[(s * P + g) * 3 + d] = M[g][d] * sc;
         if (f_dust) f_dust[(s * P + g) * 3 + d] = fd[d];
-        if (f_field) f_field[(s * P + g) * 3 + d] =
-            (d == 2 && p->dist == OD_DIST_FIELD_DRIVEN) ? qn[g] * c->E : 0.0;
+        if (f_field) f_field[(s * P + g) * 3 + d] = d == 2 ? qn[g] * p->gfield[g] : 0.0;
       }
       if (dN_out) dN_out[s * P + g] = (int64_t)dN[g];
     }
@@ -583,6 +686,28 @@ int odo_force_targets(const od_config* c, const double* pos, int64_t n, int roun
       gx += cc * dx; gy += cc * dy; gz += cc * dz;
     }
     force[3 * t] = F * gx; force[3 * t + 1] = F * gy; force[3 * t + 2] = F * gz;
+  }
+  free(xh); free(p);
+  return 0;
+}
+
+/* Screened potential sum over the ions at grid points (r_i, 0, z_j) in units of r_D_e
+ * (chains/matthews.py:397-421): pot[j * n_r + i] = sum_ions exp(-r)/(r + r_0). */
+int odo_ion_potential_grid(const od_config* c, const double* pos, int64_t n, int round32,
+                           const double* gr, const double* gz, int n_r, int n_z, double* pot) {
+  odo_par* p = (odo_par*)malloc(sizeof(odo_par));
+  if (!p || make_par(c, p)) { free(p); return 1; }
+  double* xh = (double*)malloc(sizeof(double) * 3 * n);
+  to_hat(p, pos, n, round32, xh);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int q = 0; q < n_r * n_z; q++) {
+    double gx = gr[q % n_r], gzz = gz[q / n_r], acc = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+      double dx = gx - xh[3 * i], dy = -xh[3 * i + 1], dz = gzz - xh[3 * i + 2];
+      double r = sqrt(dx * dx + dy * dy + dz * dz);
+      acc += exp(-r) / (r + p->rho0);
+    }
+    pot[q] = acc;
   }
   free(xh); free(p);
   return 0;

@@ -48,11 +48,13 @@ def load():
                                           POINTER(c_int64), POINTER(c_int64)]
         lib.odo_trap_potential.argtypes = [c_double, c_double, c_int, c_int, c_int64, c_uint64, _DP]
         lib.odo_inject.argtypes = [c_void_p, c_int64, c_int64, _DP, _DP]
-        lib.odo_run.argtypes = [c_void_p, _DP, _DP, c_int64, c_int, c_int64, c_int64, _DP, _DP, _DP,
-                                _DP, _DP, _DP, POINTER(c_int64), POINTER(c_int64)]
+        lib.odo_run.argtypes = [c_void_p, _DP, _DP, c_int64, c_int, c_int64, c_int64, c_int64, _DP,
+                                _DP, _DP, _DP, _DP, _DP, POINTER(c_int64), POINTER(c_int64)]
         lib.odo_accel.argtypes = [c_void_p, _DP, c_int64, c_int, _DP, _DP]
         lib.odo_force_targets.argtypes = [c_void_p, _DP, c_int64, c_int, POINTER(c_int64), c_int64,
                                           _DP]
+        lib.odo_ion_potential_grid.argtypes = [c_void_p, _DP, c_int64, c_int, _DP, _DP, c_int, c_int,
+                                               _DP]
         lib.odo_set_threads.argtypes = [c_int]
         lib.odo_max_threads.restype = c_int
         _lib = lib
@@ -138,9 +140,10 @@ def inject(holder, ion, step):
     return x, v
 
 
-def run(holder, pos, vel, first_step, nsteps, q_param=None, round32=True):
+def run(holder, pos, vel, first_step, nsteps, q_param=None, round32=True, rng_base=0):
     """Run steps [first_step, first_step+nsteps) of the reference program. Returns a dict
-    with the final state and the per-step series."""
+    with the final state and the per-step series. rng_base: Philox step counter of step 0 (a
+    later window of a simulation whose random streams continue)."""
     c = holder.cfg
     P = c.n_grains
     pos = np.array(pos, dtype=np.float64, order="C")
@@ -154,9 +157,22 @@ def run(holder, pos, vel, first_step, nsteps, q_param=None, round32=True):
     ninj = np.zeros(nsteps, dtype=np.int64)
     dN = np.zeros((nsteps, Pm), dtype=np.int64)
     rc = load().odo_run(_cfg(holder), _p(pos), _p(vel), pos.shape[0], int(round32), first_step,
-                        nsteps, _p(qp), _p(q), _p(fo), _p(fc), _p(fd), _p(ff),
+                        nsteps, int(rng_base), _p(qp), _p(q), _p(fo), _p(fc), _p(fd), _p(ff),
                         ninj.ctypes.data_as(POINTER(c_int64)), dN.ctypes.data_as(POINTER(c_int64)))
     assert rc == 0
     return {"pos": pos, "vel": vel, "q_param": qp, "q": q[:, :P], "orbit": fo[:, :P],
             "collect": fc[:, :P], "dust": fd[:, :P], "field": ff[:, :P], "n_inj": ninj,
             "dN": dN[:, :P]}
+
+
+def ion_potential_grid(holder, pos, gr, gz, round32=True):
+    """(len(gz), len(gr)) sum over ions of exp(-r)/(r + r_0) at (gr[i], 0, gz[j]) (units of r_D_e)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    gr = np.ascontiguousarray(gr, dtype=np.float64)
+    gz = np.ascontiguousarray(gz, dtype=np.float64)
+    pot = np.empty((len(gz), len(gr)))
+    rc = load().odo_ion_potential_grid(_cfg(holder), _p(pos), len(pos), int(round32), _p(gr), _p(gz),
+                                       len(gr), len(gz), _p(pot))
+    if rc:
+        raise ValueError("oracle rejected the configuration")
+    return pot
