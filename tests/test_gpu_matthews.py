@@ -165,3 +165,21 @@ def test_dust_dynamics_iterations(gpu_lib):
         assert np.all(np.isfinite(x)) and np.all(np.isfinite(f)) and np.all(q < 0)
         assert not np.allclose(x, x0)
         assert dd.eng.step_index == sim.n
+
+
+def test_fork_time_averages(gpu_lib):
+    # 300 steps of the fork model (tabulated trap, order-2 field, collisions, reflection):
+    # time-averaged charge and orbit force within 1 % of the oracle
+    holder, plasma, sim, grains, pos, vel, tab = fork(2048, 300)
+    with _lib.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        eng.step(300)
+        avg, navg = eng.averages()
+    ref = oracle.run(holder, pos, vel, 0, 300, round32=True)
+    assert navg == 150
+    for g in range(2):
+        dq = abs(avg[g, 0] - ref["q"][150:, g].mean()) / abs(ref["q"][150:, g].mean())
+        o_ref = ref["orbit"][150:, g].mean(0)
+        do = np.linalg.norm(avg[g, 1:4] - o_ref) / np.linalg.norm(o_ref)
+        print(f"fork time averages grain {g}: q rel {dq:.2e}, orbit rel {do:.2e}")
+        assert dq < 0.01 and do < 0.01
