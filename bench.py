@@ -43,6 +43,8 @@ FLOPS_PER_PAIR = 25
 KERNELS_PER_STEP = 6          # all pairs: kick/drift, pairs, kick/flag, collect, correct, tail
                               # (+ the tile-pair row sums with variant 7)
 KERNELS_PER_STEP_CUTOFF = 12  # + cell clear, count, scan, scatter, sort, chunk scan
+KERNELS_PER_STEP_CUTOFF_TILES = 16  # + clear, count, scan, scatter, sort, boxes, pairs,
+                                    # scan, list, tile-pair kernel, row sums (cutoff variant 3)
 
 
 def parse():
@@ -289,14 +291,20 @@ def run_ours(args, dist: Dist):
     achieved = pairs_per_launch * FLOPS_PER_PAIR / pair_avg_s / 1e12
     n3 = not cutoff and plan["variant"] == 7
     traffic = None if cutoff else load_traffic(N, plan["variant"])
-    if cutoff:
+    if cutoff and plan["variant"] == 3:
+        kernel = (f"Morton sort + tile-pair list + k_pairs_cutn3 (each pair once, {plan['jsplit']}-ion "
+                  "tiles, 64-ion group pairs beyond r_c skipped; pairs inside the cutoff credited)")
+    elif cutoff:
         kernel = "cell-list build + k_pairs_cut (pairs inside the cutoff)"
     elif n3:
         kernel = (f"k_pairs_n3 + k_n3_reduce (each unordered pair once, {plan['jsplit']}-ion tiles; "
                   "credited with the N(N-1) directed pair terms it replaces)")
     else:
         kernel = f"k_pairs_x2 variant {plan['variant']} (all-pairs ion-ion)"
-    launches = KERNELS_PER_STEP_CUTOFF if cutoff else KERNELS_PER_STEP + (1 if n3 else 0)
+    if cutoff:
+        launches = KERNELS_PER_STEP_CUTOFF_TILES if plan["variant"] == 3 else KERNELS_PER_STEP_CUTOFF
+    else:
+        launches = KERNELS_PER_STEP + (1 if n3 else 0)
 
     # e2e through the C ABI with host buffers (the calls simulate() makes)
     eng.close()

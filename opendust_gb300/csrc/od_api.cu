@@ -310,7 +310,10 @@ static void free_timing(od_handle* h) {
   h->ev_pair.clear();
 }
 
+static void free_cutn3(od_handle* h);
+
 static void free_all(od_handle* h) {
+  free_cutn3(h);
   if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
   free_timing(h);
@@ -336,6 +339,7 @@ static od_status alloc_scratch_for_plan(od_handle* h) {
 
 static od_status create_handle(const od_config* cfg, int32_t device, bool n3_default,
                                od_handle** out);
+static od_status alloc_cutn3(od_handle* h, int ipt, int T);
 
 extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle** out) {
   return create_handle(cfg, device, true, out);
@@ -452,6 +456,15 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
     OD_CKC(cudaMemcpy(h->cut.stencil, st.data(), sizeof(int4) * st.size(), cudaMemcpyHostToDevice));
     OD_CKC(cudaMemset(h->d_pairs, 0, sizeof(unsigned long long)));
     h->has_cut = true;
+    // default: tile pairs with each pair once (512-ion tiles, else 1024) when the tile-pair
+    // matrix fits the budget; the cell-stencil kernel otherwise
+    const int G = od_cutn3_grid(h->N);
+    const int cut_ipt = od_cutn3_bytes(h->N, 512, G) <= OD_N3_BUDGET ? 2
+                        : (od_cutn3_bytes(h->N, 1024, G) <= OD_N3_BUDGET ? 4 : 0);
+    if (cut_ipt && alloc_cutn3(h, cut_ipt, cut_ipt == 2 ? 512 : 1024) != OD_OK) {
+      cudaGetLastError();
+      h->err.clear();
+    }
   }
   OD_CKC(cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
   od_dstate s0{};
@@ -820,6 +833,75 @@ static bool plan_supported(int nt, int ipt, int variant) {
   }
 }
 
+static void free_cutn3(od_handle* h) {
+  od_cutn3* L = h->cut.n3;
+  if (!L) return;
+  void* ptrs[] = {L->cell_of, L->count, L->fill, L->start, L->perm, L->xs, L->ys, L->zs,
+                  L->box, L->gbox, L->adj, L->rowptr, L->pairs, L->S};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete L;
+  h->cut.n3 = nullptr;
+}
+
+// Cutoff variant 3: Morton-sorted tiles of T ions (ipt 4: 1024, ipt 2: 512) and the dense
+// tile-pair matrix of partial sums (24 bytes per ion and tile).
+static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
+  free_cutn3(h);
+  OD_CK(h, cudaSetDevice(h->device));
+  OD_CK(h, od_cutn3_prepare(ipt, T));
+  od_cutn3* L = new (std::nothrow) od_cutn3();
+  if (!L) return fail(h, OD_ERR_OOM, "host allocation");
+  h->cut.n3 = L;
+  const int N = h->N, G = od_cutn3_grid(N);
+  L->G = G;
+  L->bits = 0;
+  while ((1 << L->bits) < G) L->bits++;
+  L->ncells = G * G * G;
+  const double side = std::max(2.0 * h->hp.Rh, (double)h->hp.Hh) * 1.02;
+  L->lo = (float)(-side / 2.0);
+  L->inv_s = (float)(G / side);
+  L->T = T; L->ipt = ipt;
+  L->nT = (N + T - 1) / T;
+  L->nslots = L->nT * T;
+  L->nwords = (L->nT + 31) / 32;
+  L->grid = od_num_sms(h->device) * 3;
+  const size_t nT = L->nT, ns = L->nslots, nc = L->ncells;
+  auto al = [&](auto** p, size_t n) {
+    return cudaMalloc((void**)p, sizeof(**p) * std::max<size_t>(n, 1));
+  };
+  cudaError_t e = al(&L->cell_of, (size_t)N);
+  if (e == cudaSuccess) e = al(&L->count, nc);
+  if (e == cudaSuccess) e = al(&L->fill, nc);
+  if (e == cudaSuccess) e = al(&L->start, nc + 1);
+  if (e == cudaSuccess) e = al(&L->perm, ns);
+  if (e == cudaSuccess) e = al(&L->xs, ns);
+  if (e == cudaSuccess) e = al(&L->ys, ns);
+  if (e == cudaSuccess) e = al(&L->zs, ns);
+  if (e == cudaSuccess) e = al(&L->box, nT * 6);
+  if (e == cudaSuccess) e = al(&L->gbox, (ns / 64) * 6);
+  if (e == cudaSuccess) e = al(&L->adj, nT * L->nwords);
+  if (e == cudaSuccess) e = al(&L->rowptr, nT + 1);
+  if (e == cudaSuccess) e = al(&L->pairs, nT * (nT + 1) / 2);
+  if (e == cudaSuccess) e = al(&L->S, nT * nT * 6 * (size_t)T);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    free_cutn3(h);
+    return fail(h, OD_ERR_OOM, "no device memory for the tile-pair cutoff");
+  }
+  // tail slots: far-away sentinels that no ion owns
+  if (ns > (size_t)N) {
+    std::vector<float> sent(ns - N, OD_SENTINEL);
+    std::vector<int32_t> none(ns - N, -1);
+    OD_CK(h, cudaMemcpy(L->xs + N, sent.data(), sizeof(float) * (ns - N), cudaMemcpyHostToDevice));
+    OD_CK(h, cudaMemcpy(L->ys + N, sent.data(), sizeof(float) * (ns - N), cudaMemcpyHostToDevice));
+    OD_CK(h, cudaMemcpy(L->zs + N, sent.data(), sizeof(float) * (ns - N), cudaMemcpyHostToDevice));
+    OD_CK(h, cudaMemcpy(L->perm + N, none.data(), sizeof(int32_t) * (ns - N),
+                        cudaMemcpyHostToDevice));
+  }
+  return OD_OK;
+}
+
 static void drop_graph(od_handle* h) {
   if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
@@ -871,8 +953,21 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
                                       int32_t variant, int32_t jsplit) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (h->has_cut) {
-    // cutoff method: variant 0 selects the scalar pair kernel, 2 the packed one
-    if (variant != 0 && variant != 2) return fail(h, OD_ERR_INVALID, "cutoff variants are 0 and 2");
+    // cutoff method: variant 0 selects the scalar pair kernel, 2 the packed one, 3 the tile
+    // pairs with each pair once (targets_per_thread 4: 1024-ion tiles, 2: 512-ion tiles)
+    if (variant != 0 && variant != 2 && variant != 3)
+      return fail(h, OD_ERR_INVALID, "cutoff variants are 0, 2 and 3");
+    if (variant == 3) {
+      if (targets_per_thread != 2 && targets_per_thread != 4)
+        return fail(h, OD_ERR_INVALID, "cutoff variant 3 takes 2 or 4 targets per lane");
+      const int T = targets_per_thread == 4 ? 1024 : 512;
+      if (!h->cut.n3 || h->cut.n3->T != T) {
+        od_status st = alloc_cutn3(h, targets_per_thread, T);
+        if (st != OD_OK) return st;
+      }
+    } else {
+      free_cutn3(h);
+    }
     h->cut.packed = variant == 2;
     if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
     if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
@@ -1002,6 +1097,14 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
 
 extern "C" od_status od_get_pair_plan(const od_handle* h, int32_t* plan5) {
   if (!h || !plan5) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
+  if (h->has_cut) {  // cutoff variant: 3 (tile pairs), 2 (packed cells) or 0 (scalar cells)
+    plan5[0] = 256;
+    plan5[1] = h->cut.n3 ? h->cut.n3->ipt : 2;
+    plan5[2] = h->cut.n3 ? 3 : (h->cut.packed ? 2 : 0);
+    plan5[3] = h->cut.n3 ? h->cut.n3->T : 0;
+    plan5[4] = 0;
+    return OD_OK;
+  }
   plan5[0] = h->plan.nt; plan5[1] = h->plan.ipt; plan5[2] = h->plan.variant;
   plan5[3] = h->plan.variant == 7 ? h->plan.tile : h->plan.jsplit; plan5[4] = h->plan.chunk;
   return OD_OK;
@@ -1530,6 +1633,13 @@ extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes
   const od_pair_plan pl = default_plan((int)Np, 152);
   const int64_t P = std::max(cfg->n_grains, 1);
   int64_t b = 0;
+  if (cfg->force_method == OD_FORCE_CUTOFF) {  // tile-pair cutoff, as od_create chooses it
+    const int G = od_cutn3_grid((int)cfg->n_ions);
+    const size_t c512 = od_cutn3_bytes((int)cfg->n_ions, 512, G);
+    const size_t c1024 = od_cutn3_bytes((int)cfg->n_ions, 1024, G);
+    if (c512 <= OD_N3_BUDGET) b += (int64_t)c512;
+    else if (c1024 <= OD_N3_BUDGET) b += (int64_t)c1024;
+  }
   if (cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default((int)Np)) {
     int ipt = 0;
     const int tile = od_n3_default((int)Np, OD_N3_BUDGET, &ipt);

@@ -428,6 +428,8 @@ __global__ void k_chunks2(int ncells, const int32_t* __restrict__ count,
 cudaError_t od_launch_cutoff(const od_cutlist& L, const float4* pos, int n, int Npad,
                              float4* part_hi, float4* part_lo, float rho0, float rc, float rs,
                              uint32_t* err, unsigned long long* pair_count, cudaStream_t s) {
+  if (L.n3)
+    return od_launch_cutoff_n3(*L.n3, pos, n, part_hi, part_lo, rho0, rc, rs, err, pair_count, s);
   const od_cellgeom& g = L.g;
   k_cells_clear<<<(g.ncells + kBlk - 1) / kBlk, kBlk, 0, s>>>(g.ncells, L.count, L.fill);
   k_cells_count<<<(n + kBlk - 1) / kBlk, kBlk, 0, s>>>(g, n, pos, L.cell_of, L.count);

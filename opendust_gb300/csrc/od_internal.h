@@ -97,8 +97,35 @@ struct od_cellgeom {
   float c, inv_c, lox, loy, loz;
 };
 // Device cell list of the cutoff path.
+// Cutoff over tile pairs (cutoff variant 3, od_n3.cu): ions sorted along a Morton curve of a
+// G^3 cell grid, tiles of T consecutive sorted ions, and every tile pair whose bounding boxes
+// come within the cutoff evaluated with each unordered pair once (64-ion group pairs farther
+// apart than the cutoff skipped).
+struct od_cutn3 {
+  int G, bits, ncells;              // cells per axis (power of two), Morton bits per axis
+  float lo, inv_s;                  // grid origin (every axis) and 1 / cell side (lambda)
+  int T, ipt, nT, nslots, nwords;   // tile, targets per lane, tiles, nT*T slots, bitmap words
+  int32_t *cell_of, *count, *fill, *start;  // [N], [ncells], [ncells], [ncells + 1]
+  int32_t* perm;                    // [nslots] ion of each sorted slot, -1 for sentinels
+  float *xs, *ys, *zs;              // [nslots] sorted positions; sentinels in the tail
+  float* box;                       // [nT][6] min xyz, max xyz
+  float* gbox;                      // [nslots / 64][6] boxes of 64-slot groups
+  uint32_t* adj;                    // [nT][nwords] tile pairs (a, b >= a) within the cutoff
+  int32_t* rowptr;                  // [nT + 1] pair counts, then their exclusive prefix
+  int2* pairs;                      // [nT (nT + 1) / 2] listed pairs, row-major
+  float* S;                         // [nT][nT][6][T] two-float partial sums
+  int grid;                         // persistent blocks of the pair kernel
+};
+size_t od_cutn3_bytes(int N, int T, int G);
+int od_cutn3_grid(int N);           // cells per axis for N ions
+cudaError_t od_cutn3_prepare(int ipt, int T);
+cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
+                                float4* part_lo, float rho0, float rc, float rs, uint32_t* err,
+                                unsigned long long* pair_count, cudaStream_t s);
+
 struct od_cutlist {
   od_cellgeom g;
+  od_cutn3* n3;          // cutoff variant 3 (or NULL)
   int32_t *cell_of, *count, *fill, *start, *chunk_prefix, *perm;  // start/chunk_prefix: ncells+1
   float *ox, *oy, *oz;   // sorted cell-relative offsets, 8-padded segments
   int4* stencil;         // source-cell offsets within the cutoff of a target cell

@@ -35,15 +35,37 @@ namespace {
 
 constexpr int kWarps = 8;
 
+// Pair-term constants. CUT = 0: all pairs; 1: cutoff with OpenMM's switching polynomial on
+// the energy (S = (1-x)^3 (1 + 3x + 6x^2), x = (r - r_s)/(r_c - r_s) clamped to [0, 1], so that
+// pairs beyond r_c contribute exactly 0, opendust.py:481-485); 2: hard cutoff without switching.
 struct n3_consts {
-  od_u64 eps, rho, nl2e;
+  od_u64 eps, rho, nl2e, one, three, six, invw, nrsw, p30w;
+  float rc2;
+};
+struct n3_cut {
+  float rho0, rc2, rs, inv_w;
 };
 
-// two pair terms (target X,Y,Z broadcast in both halves; sources packed in QX,QY,QZ)
-template <bool REACT>
+__device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
+  n3_consts k;
+  k.eps = p2(1e-30f, 1e-30f);
+  k.rho = p2(c.rho0, c.rho0);
+  k.nl2e = p2(OD_NLOG2E, OD_NLOG2E);
+  k.one = p2(1.f, 1.f); k.three = p2(3.f, 3.f); k.six = p2(6.f, 6.f);
+  k.invw = p2(c.inv_w, c.inv_w);
+  k.nrsw = p2(-c.rs * c.inv_w, -c.rs * c.inv_w);
+  k.p30w = p2(30.f * c.inv_w, 30.f * c.inv_w);
+  k.rc2 = c.rc2;
+  return k;
+}
+
+// two pair terms (target X,Y,Z broadcast in both halves; sources packed in QX,QY,QZ); COUNT
+// adds the directed pairs inside the cutoff (self pairs, at r^2 = 1e-30, excluded)
+template <int CUT, bool REACT, bool COUNT>
 __device__ __forceinline__ void n3_pair(const n3_consts& k, od_u64 X, od_u64 Y, od_u64 Z,
                                         od_u64 QX, od_u64 QY, od_u64 QZ, od_u64& AX, od_u64& AY,
-                                        od_u64& AZ, od_u64& RX, od_u64& RY, od_u64& RZ) {
+                                        od_u64& AZ, od_u64& RX, od_u64& RY, od_u64& RZ,
+                                        unsigned int& cnt) {
   const od_u64 DX = sub2(X, QX), DY = sub2(Y, QY), DZ = sub2(Z, QZ);
   od_u64 R2 = fma2(DX, DX, k.eps);
   R2 = fma2(DY, DY, R2);
@@ -55,7 +77,27 @@ __device__ __forceinline__ void n3_pair(const n3_consts& k, od_u64 X, od_u64 Y, 
   const od_u64 SI = p2(od_rcp(s.x), od_rcp(s.y));
   const float2 ea = up2(mul2(R, k.nl2e));
   const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
-  const od_u64 C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
+  od_u64 C;
+  if (CUT == 0) {
+    C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
+  } else if (CUT == 1) {
+    const float2 xx = up2(fma2(R, k.invw, k.nrsw));
+    const od_u64 X2 = p2(fmaxf(xx.x, 0.f), fmaxf(xx.y, 0.f));
+    const float2 om = up2(sub2(k.one, X2));
+    const od_u64 OM = p2(fmaxf(om.x, 0.f), fmaxf(om.y, 0.f));
+    const od_u64 S = mul2(mul2(OM, OM), mul2(OM, fma2(X2, fma2(k.six, X2, k.three), k.one)));
+    const od_u64 Q = mul2(X2, OM);
+    // e (1/s + 1/s^2) S - e (1/s) S' with S' = -30 Q^2 / (r_c - r_s):
+    // = e (1/s) [(1 + 1/s) S + 30 Q^2 / (r_c - r_s)]
+    const od_u64 U = fma2(mul2(Q, Q), k.p30w, fma2(SI, S, S));
+    C = mul2(mul2(EX, RI), mul2(SI, U));
+  } else {
+    const float2 c = up2(mul2(mul2(EX, RI), fma2(SI, SI, SI)));
+    C = p2(r2.x < k.rc2 ? c.x : 0.f, r2.y < k.rc2 ? c.y : 0.f);
+  }
+  if (COUNT)
+    cnt += (REACT ? 2u : 1u) * ((unsigned)(r2.x < k.rc2 && r2.x > 1e-29f) +
+                                (unsigned)(r2.y < k.rc2 && r2.y > 1e-29f));
   AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
   if (REACT) { RX = fma2(C, DX, RX); RY = fma2(C, DY, RY); RZ = fma2(C, DZ, RZ); }
 }
@@ -67,21 +109,22 @@ __device__ __forceinline__ od_u64 shfl64(od_u64 v, int src) {
 // One group pair: 32 lane steps of MT x MS pair terms per lane with rotating sources. Each
 // source pack moves on as soon as its terms are done, so that its shuffles overlap the next
 // pack's arithmetic.
-template <int MT, int MS, bool REACT>
+template <int MT, int MS, int CUT, bool REACT, bool COUNT>
 __device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[MT],
                                          const od_u64 (&Y)[MT], const od_u64 (&Z)[MT],
                                          od_u64 (&QX)[MS / 2], od_u64 (&QY)[MS / 2],
                                          od_u64 (&QZ)[MS / 2], od_u64 (&AX)[MT], od_u64 (&AY)[MT],
                                          od_u64 (&AZ)[MT], od_u64 (&RX)[MS / 2],
-                                         od_u64 (&RY)[MS / 2], od_u64 (&RZ)[MS / 2], int src) {
+                                         od_u64 (&RY)[MS / 2], od_u64 (&RZ)[MS / 2], int src,
+                                         unsigned int& cnt) {
 #pragma unroll 1
   for (int st = 0; st < 32; st++) {
 #pragma unroll
     for (int q = 0; q < MS / 2; q++) {
 #pragma unroll
       for (int kt = 0; kt < MT; kt++)
-        n3_pair<REACT>(k, X[kt], Y[kt], Z[kt], QX[q], QY[q], QZ[q], AX[kt], AY[kt], AZ[kt],
-                       RX[q], RY[q], RZ[q]);
+        n3_pair<CUT, REACT, COUNT>(k, X[kt], Y[kt], Z[kt], QX[q], QY[q], QZ[q], AX[kt], AY[kt],
+                                   AZ[kt], RX[q], RY[q], RZ[q], cnt);
       QX[q] = shfl64(QX[q], src); QY[q] = shfl64(QY[q], src); QZ[q] = shfl64(QZ[q], src);
       if (REACT) {
         RX[q] = shfl64(RX[q], src); RY[q] = shfl64(RY[q], src); RZ[q] = shfl64(RZ[q], src);
@@ -113,14 +156,33 @@ struct n3_traits {
   static constexpr size_t SMEM = sizeof(float) * (6 * T + (HL_SMEM ? 6 * kWarps * GT : 0));
 };
 
-// Tile pair (a, b), a <= b, of one simulation: one block. sm: dynamic shared memory of
-// n3_traits::SMEM bytes.
-template <int MT, int MS, int PA>
-__device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
-                                             const float* __restrict__ sy,
-                                             const float* __restrict__ sz, int Npad, int nT,
-                                             float* __restrict__ S, float rho0, int a, int b,
-                                             float* sm) {
+// (union) box of n consecutive 64-ion groups starting at group g0; 6 floats min xyz, max xyz
+__device__ __forceinline__ void group_box(const float* __restrict__ gbox, int g0, int n,
+                                          float (&bx)[6]) {
+#pragma unroll
+  for (int d = 0; d < 6; d++) bx[d] = gbox[g0 * 6 + d];
+  for (int q = 1; q < n; q++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      bx[d] = fminf(bx[d], gbox[(g0 + q) * 6 + d]);
+      bx[3 + d] = fmaxf(bx[3 + d], gbox[(g0 + q) * 6 + 3 + d]);
+    }
+}
+
+// Tile pair (a, b), a <= b, of one simulation: one block. outT receives the two-float sums
+// of tile a's ions from tile b, outR those of tile b's ions from tile a (the same slice when
+// a == b); each [6][T]. sm: dynamic shared memory of n3_traits::SMEM bytes. CULL skips group
+// pairs whose 64-ion group boxes (gbox) are farther apart than sqrt(cull2). Returns the
+// directed pairs inside the cutoff when COUNT.
+template <int MT, int MS, int PA, int CUT, bool COUNT, bool CULL = false>
+__device__ __forceinline__ unsigned int n3_tile_pair(const float* __restrict__ sx,
+                                                     const float* __restrict__ sy,
+                                                     const float* __restrict__ sz, int Npad,
+                                                     float* __restrict__ outT,
+                                                     float* __restrict__ outR, const n3_cut& cut,
+                                                     int a, int b, float* sm,
+                                                     const float* __restrict__ gbox = nullptr,
+                                                     float cull2 = 0.f) {
   using TR = n3_traits<MT, MS, PA>;
   constexpr int GT = TR::GT, GS = TR::GS, T = TR::T, NBT = TR::NBT, NBS = TR::NBS;
   constexpr bool HLS = TR::HL_SMEM;
@@ -130,15 +192,15 @@ __device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
   const int ngt = Npad / GT, ngs = Npad / GS;
   for (int e = tid; e < 6 * T; e += kWarps * 32) sm[e] = 0.f;
   __syncthreads();
-  n3_consts k;
-  k.eps = p2(1e-30f, 1e-30f);
-  k.rho = p2(rho0, rho0);
-  k.nl2e = p2(OD_NLOG2E, OD_NLOG2E);
+  const n3_consts k = make_consts(cut);
+  unsigned int cnt = 0;
   for (int p = 0; p < PA; p++) {
     const int ga = w + kWarps * p;
     const int GA = a * NBT + ga;
     const bool ta_ok = GA < ngt;
     od_u64 X[MT], Y[MT], Z[MT];
+    float tb[6];  // CULL: box of the target group
+    if (CULL && ta_ok) group_box(gbox, GA * (GT / 64), GT / 64, tb);
     // two-float target sums: registers, or this warp's shared-memory slice (lane-private words)
     float hreg[HLS ? 1 : 6 * MT];
     float* const hsm = sm + 6 * T + w * 6 * GT + lane;
@@ -158,6 +220,18 @@ __device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
       if (ta_ok && GB < ngs) {
         const int s0 = gb * GS, t0 = ga * GT;  // tile-local first ions (GS divides GT)
         mode = (!diag || s0 >= t0 + GT) ? 2 : (s0 >= t0 ? 1 : 0);
+        if (CULL && mode == 2) {
+          // skip group pairs whose boxes are farther apart than the cutoff
+          float sb[6];
+          group_box(gbox, GB * (GS / 64), GS / 64, sb);
+          float d2 = 0.f;
+#pragma unroll
+          for (int d = 0; d < 3; d++) {
+            const float gap = fmaxf(fmaxf(sb[d] - tb[3 + d], tb[d] - sb[3 + d]), 0.f);
+            d2 = fmaf(gap, gap, d2);
+          }
+          if (!(d2 < cull2)) mode = 0;
+        }
       }
       if (mode != 0) {
         od_u64 QX[MS / 2], QY[MS / 2], QZ[MS / 2], RX[MS / 2], RY[MS / 2], RZ[MS / 2];
@@ -173,9 +247,11 @@ __device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
 #pragma unroll
         for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
         if (mode == 2)
-          n3_group<MT, MS, true>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
+          n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                             cnt);
         else
-          n3_group<MT, MS, false>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src);
+          n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                              cnt);
 #pragma unroll
         for (int kt = 0; kt < MT; kt++) {
           od_acc2(N3_H(0, kt), N3_H(3, kt), sum2(AX[kt]));
@@ -210,7 +286,7 @@ __device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
           acc2x2(sm[2 * T + e], sm[5 * T + e], N3_H(2, kt), N3_H(5, kt));
         }
       } else {
-        float* o = S + ((size_t)a * nT + b) * (6 * (size_t)T);
+        float* o = outT;
 #pragma unroll
         for (int kt = 0; kt < MT; kt++) {
           const int e = ga * GT + lane + 32 * kt;
@@ -222,8 +298,8 @@ __device__ __forceinline__ void n3_tile_pair(const float* __restrict__ sx,
     __syncthreads();
   }
 #undef N3_H
-  float* o = S + ((size_t)b * nT + a) * (6 * (size_t)T);
-  for (int e = tid; e < 6 * T; e += kWarps * 32) o[e] = sm[e];
+  for (int e = tid; e < 6 * T; e += kWarps * 32) outR[e] = sm[e];
+  return cnt;
 }
 
 // (a, b) of the k-th pair of the b-major upper triangle
@@ -241,7 +317,10 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
                float rho0) {
   extern __shared__ float sm[];
   const int2 ab = tri_pair(blockIdx.x);
-  n3_tile_pair<MT, MS, PA>(sx, sy, sz, Npad, nT, S, rho0, ab.x, ab.y, sm);
+  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
+  n3_tile_pair<MT, MS, PA, 0, false>(sx, sy, sz, Npad, S + ((size_t)ab.x * nT + ab.y) * T6,
+                                     S + ((size_t)ab.y * nT + ab.x) * T6, n3_cut{rho0, 0.f, 0.f, 0.f},
+                                     ab.x, ab.y, sm);
 }
 
 // Batched form: block k takes work item k = (simulation, tile a, tile b) of a table that lists
@@ -252,7 +331,11 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   extern __shared__ float sm[];
   const int4 w = items[blockIdx.x];
   const od_simdesc& d = sims[w.x];
-  n3_tile_pair<MT, MS, PA>(d.b.sx, d.b.sy, d.b.sz, d.Npad, w.w, d.b.n3, d.rho0, w.y, w.z, sm);
+  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
+  n3_tile_pair<MT, MS, PA, 0, false>(d.b.sx, d.b.sy, d.b.sz, d.Npad,
+                                     d.b.n3 + ((size_t)w.y * w.w + w.z) * T6,
+                                     d.b.n3 + ((size_t)w.z * w.w + w.y) * T6,
+                                     n3_cut{d.rho0, 0.f, 0.f, 0.f}, w.y, w.z, sm);
 }
 
 // Row sums of S in a fixed order: slab 0 of (ph, pl) for ion i < Npad.
@@ -312,6 +395,291 @@ cudaError_t launch_n3(const od_pair_io& io, int Npad, float* S, float4* ph, floa
                                                                       nT, S, rho0);
   k_n3_reduce<<<(Npad + 255) / 256, 256, 0, s>>>(S, nT, TR::T, Npad, ph, pl);
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ cutoff over tile pairs
+// Cell grid of G^3 cells over the cube [lo, lo + G/inv_s)^3; a cell's key is the Morton
+// interleave of its coordinates, so that consecutive keys (and the ions sorted by key) stay
+// close in space and groups of consecutive sorted ions have small bounding boxes.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bit k -> bit 3k (v < 2^10)
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void k_mc_clear(int ncells, int32_t* __restrict__ count, int32_t* __restrict__ fill) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncells) { count[c] = 0; fill[c] = 0; }
+}
+
+__global__ void k_mc_count(int n, const float4* __restrict__ pos, float lo, float inv_s, int G,
+                           int32_t* __restrict__ cell_of, int32_t* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  const int cx = min(max((int)floorf((p.x - lo) * inv_s), 0), G - 1);
+  const int cy = min(max((int)floorf((p.y - lo) * inv_s), 0), G - 1);
+  const int cz = min(max((int)floorf((p.z - lo) * inv_s), 0), G - 1);
+  const int c = (int)(spread3((uint32_t)cx) | (spread3((uint32_t)cy) << 1) |
+                      (spread3((uint32_t)cz) << 2));
+  cell_of[i] = c;
+  atomicAdd(&count[c], 1);
+}
+
+// exclusive scan of in[0..n) into out[0..n], out[n] = total (one 1024-thread block; in and out
+// may be the same array: every thread reads each of its entries before writing it)
+__global__ void __launch_bounds__(1024) k_scan_excl(int n, const int32_t* in, int32_t* out) {
+  __shared__ int s_w[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (n + 1023) / 1024;
+  const int c0 = min(tid * per, n), c1 = min(c0 + per, n);
+  int a = 0;
+  for (int c = c0; c < c1; c++) a += in[c];
+  int ia = a;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, ia, o);
+    if (lane >= o) ia += y;
+  }
+  if (lane == 31) s_w[wid] = ia;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = s_w[lane];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    s_w[lane] = x - v;
+  }
+  __syncthreads();
+  int off = s_w[wid] + ia - a;
+  for (int c = c0; c < c1; c++) {
+    const int v = in[c];
+    out[c] = off;
+    off += v;
+  }
+  if (tid == 1023) out[n] = off;
+}
+
+__global__ void k_mc_scatter(int n, const int32_t* __restrict__ cell_of,
+                             const int32_t* __restrict__ start, int32_t* __restrict__ fill,
+                             int32_t* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell_of[i];
+  perm[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+// One block per cell: sort the cell's ions by index (bitonic in shared memory; the order of
+// the atomic scatter is not reproducible, the sorted order is) and write their positions.
+constexpr int kCellMax = 2048;
+__global__ void __launch_bounds__(128) k_mc_sort(const int32_t* __restrict__ count,
+                                                 const int32_t* __restrict__ start,
+                                                 const float4* __restrict__ pos,
+                                                 int32_t* __restrict__ perm, float* __restrict__ xs,
+                                                 float* __restrict__ ys, float* __restrict__ zs,
+                                                 uint32_t* __restrict__ err) {
+  __shared__ int32_t key[kCellMax];
+  const int c = blockIdx.x;
+  const int n0 = count[c];
+  if (n0 == 0) return;
+  if (n0 > kCellMax) {
+    if (threadIdx.x == 0) atomicOr(err, OD_DERR_CELL);
+    return;
+  }
+  const int s0 = start[c];
+  int m = 1;
+  while (m < n0) m <<= 1;
+  for (int k = threadIdx.x; k < m; k += 128) key[k] = k < n0 ? perm[s0 + k] : 0x7fffffff;
+  __syncthreads();
+  for (int size = 2; size <= m; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int k = threadIdx.x; k < m; k += 128) {
+        const int l = k ^ stride;
+        if (l > k) {
+          const bool up = (k & size) == 0;
+          const int a = key[k], b = key[l];
+          if ((a > b) == up) { key[k] = b; key[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  for (int k = threadIdx.x; k < n0; k += 128) {
+    const int i = key[k];
+    const float4 p = pos[i];
+    perm[s0 + k] = i;
+    xs[s0 + k] = p.x; ys[s0 + k] = p.y; zs[s0 + k] = p.z;
+  }
+}
+
+// bounding boxes of every 64-slot group of tile t (real ions only; a group without ions gets
+// an inverted box that is never within range) and of the tile itself
+__global__ void __launch_bounds__(256) k_tile_box(int n, int T, const float* __restrict__ xs,
+                                                  const float* __restrict__ ys,
+                                                  const float* __restrict__ zs,
+                                                  float* __restrict__ gbox, float* __restrict__ box) {
+  __shared__ float tb[8][6];
+  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float um[6] = {3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f};  // this warp's union
+  for (int g = w; g < T / 64; g += 8) {
+    float mn[3] = {3e38f, 3e38f, 3e38f}, mx[3] = {-3e38f, -3e38f, -3e38f};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int i = t * T + g * 64 + h * 32 + lane;
+      if (i < n) {
+        const float v[3] = {xs[i], ys[i], zs[i]};
+#pragma unroll
+        for (int d = 0; d < 3; d++) { mn[d] = fminf(mn[d], v[d]); mx[d] = fmaxf(mx[d], v[d]); }
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+        mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+      }
+    if (lane < 6) gbox[((size_t)t * (T / 64) + g) * 6 + lane] = lane < 3 ? mn[lane] : mx[lane - 3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) { um[d] = fminf(um[d], mn[d]); um[3 + d] = fmaxf(um[3 + d], mx[d]); }
+  }
+  if (lane == 0)
+    for (int d = 0; d < 6; d++) tb[w][d] = um[d];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float v = tb[0][threadIdx.x];
+    for (int k = 1; k < 8; k++)
+      v = threadIdx.x < 3 ? fminf(v, tb[k][threadIdx.x]) : fmaxf(v, tb[k][threadIdx.x]);
+    box[t * 6 + threadIdx.x] = v;
+  }
+}
+
+// row a of the tile-pair bitmap: b >= a whose box comes within the cutoff (box distance in
+// FP32 with a relative margin of 1e-5, so that no pair inside r_c is dropped by rounding)
+__global__ void __launch_bounds__(128) k_tile_adj(int nT, int nwords, const float* __restrict__ box,
+                                                  float rc2m, uint32_t* __restrict__ adj,
+                                                  int32_t* __restrict__ rowcnt) {
+  __shared__ int s_cnt;
+  const int a = blockIdx.x;
+  uint32_t* row = adj + (size_t)a * nwords;
+  for (int w = threadIdx.x; w < nwords; w += 128) row[w] = 0u;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const float* A = box + a * 6;
+  int cnt = 0;
+  for (int b = a + threadIdx.x; b < nT; b += 128) {
+    const float* B = box + b * 6;
+    float d2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const float g = fmaxf(fmaxf(B[d] - A[3 + d], A[d] - B[3 + d]), 0.f);
+      d2 = fmaf(g, g, d2);
+    }
+    if (d2 < rc2m) { atomicOr(&row[b >> 5], 1u << (b & 31)); cnt++; }
+  }
+  atomicAdd(&s_cnt, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0) rowcnt[a] = s_cnt;
+}
+
+// listed pairs of row a in increasing b (one thread per row: at most nT bits)
+__global__ void k_tile_list(int nT, int nwords, const uint32_t* __restrict__ adj,
+                            const int32_t* __restrict__ rowptr, int2* __restrict__ pairs) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nT) return;
+  const uint32_t* row = adj + (size_t)a * nwords;
+  int k = rowptr[a];
+  for (int w = a >> 5; w < nwords; w++) {
+    uint32_t bits = row[w];
+    while (bits) {
+      const int j = __ffs(bits) - 1;
+      bits &= bits - 1;
+      pairs[k++] = make_int2(a, w * 32 + j);
+    }
+  }
+}
+
+// every listed tile pair, each unordered ion pair once (static assignment: pair k to block
+// k mod grid), group pairs beyond the cutoff skipped
+template <int MT, int MS, int PA, int CUT, bool COUNT>
+__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
+    k_pairs_cutn3(const float* __restrict__ xs, const float* __restrict__ ys,
+                  const float* __restrict__ zs, int nslots, int nT,
+                  const int2* __restrict__ pairs, const int32_t* __restrict__ npairs,
+                  float* __restrict__ S, n3_cut cut, const float* __restrict__ gbox, float cull2,
+                  unsigned long long* __restrict__ pair_count) {
+  extern __shared__ float sm[];
+  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
+  const int np = *npairs;
+  unsigned int cnt = 0;
+  for (int k = blockIdx.x; k < np; k += gridDim.x) {
+    const int2 ab = pairs[k];
+    cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots,
+                                                      S + ((size_t)ab.x * nT + ab.y) * T6,
+                                                      S + ((size_t)ab.y * nT + ab.x) * T6, cut,
+                                                      ab.x, ab.y, sm, gbox, cull2);
+  }
+  if (COUNT) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(pair_count, (unsigned long long)cnt);
+  }
+}
+
+// Row sums over the tiles that share a listed pair with tile t, in increasing tile order,
+// written to the ions' entries of (ph, pl).
+__global__ void __launch_bounds__(256) k_tile_reduce(int nT, int nwords, int T,
+                                                     const uint32_t* __restrict__ adj,
+                                                     const float* __restrict__ S,
+                                                     const int32_t* __restrict__ perm,
+                                                     float4* __restrict__ ph,
+                                                     float4* __restrict__ pl) {
+  extern __shared__ int32_t nb[];  // [nT] neighbour tiles, then [8] warp counts
+  int32_t* wcnt = nb + nT;
+  __shared__ int s_m;
+  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_m = 0;
+  __syncthreads();
+  // ordered compaction of {y : pair (min(t, y), max(t, y)) listed}, 256 candidates per round
+  for (int y0 = 0; y0 < nT; y0 += 256) {
+    const int y = y0 + threadIdx.x;
+    bool f = false;
+    if (y < nT)
+      f = y < t ? (adj[(size_t)y * nwords + (t >> 5)] >> (t & 31)) & 1u
+                : (adj[(size_t)t * nwords + (y >> 5)] >> (y & 31)) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wcnt[w] = __popc(bal);
+    __syncthreads();
+    int base = s_m;
+    for (int k = 0; k < w; k++) base += wcnt[k];
+    if (f) nb[base + __popc(bal & ((1u << lane) - 1u))] = y;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int k = 0; k < 8; k++) tot += wcnt[k];
+      s_m += tot;
+    }
+    __syncthreads();
+  }
+  const int m = s_m;
+  for (int e = threadIdx.x; e < T; e += 256) {
+    const int slot = t * T + e;
+    const int i = perm[slot];
+    if (i < 0) continue;
+    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    for (int q = 0; q < m; q++) {
+      const float* r = S + ((size_t)t * nT + nb[q]) * 6 * (size_t)T + e;
+      acc2x2(hx, lx, r[0], r[3 * T]);
+      acc2x2(hy, ly, r[T], r[4 * T]);
+      acc2x2(hz, lz, r[2 * T], r[5 * T]);
+    }
+    ph[i] = make_float4(hx, hy, hz, 0.f);
+    pl[i] = make_float4(lx, ly, lz, 0.f);
+  }
 }
 
 template <int MT, int MS, int PA>
@@ -396,4 +764,76 @@ int od_n3_batch_plan(int Npad, size_t budget_bytes, int* ipt) {
   if (sizeof(float) * od_n3_floats(Npad, T) > budget_bytes) return 0;
   *ipt = T == 1024 ? 4 : 8;
   return T;
+}
+
+int od_cutn3_grid(int N) {
+  // about 16 ions per cell: G the smallest power of two with G^3 >= N / 22, 8 <= G <= 128
+  int G = 8;
+  while (G < 128 && (double)G * G * G * 8.0 * 16.0 < (double)N * 1.4142) G <<= 1;
+  return G;
+}
+
+size_t od_cutn3_bytes(int N, int T, int G) {
+  const size_t nT = (size_t)((N + T - 1) / T), ns = nT * T, nc = (size_t)G * G * G;
+  const size_t nw = (nT + 31) / 32;
+  return sizeof(float) * nT * nT * 6 * T                      // S
+         + sizeof(int2) * nT * (nT + 1) / 2                   // pairs
+         + sizeof(uint32_t) * nT * nw                         // bitmap
+         + sizeof(float) * (3 * ns + 6 * nT + 6 * (ns / 64))  // sorted positions, boxes
+         + sizeof(int32_t) * (ns + N + 3 * nc + nT + 4);
+}
+
+cudaError_t od_cutn3_prepare(int ipt, int T) {
+  if (ipt == 4 && T == 1024) {
+    const int smem = (int)n3_traits<4, 4, 1>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 1, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 1, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 2, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 2, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
+  }
+  if (ipt == 2 && T == 512) return cudaSuccess;  // (2, 2, 1): 12 KB, no opt-in needed
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
+                                float4* part_lo, float rho0, float rc, float rs, uint32_t* err,
+                                unsigned long long* pair_count, cudaStream_t s) {
+  k_mc_clear<<<(L.ncells + 255) / 256, 256, 0, s>>>(L.ncells, L.count, L.fill);
+  k_mc_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, L.lo, L.inv_s, L.G, L.cell_of, L.count);
+  k_scan_excl<<<1, 1024, 0, s>>>(L.ncells, L.count, L.start);
+  k_mc_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, L.cell_of, L.start, L.fill, L.perm);
+  k_mc_sort<<<L.ncells, 128, 0, s>>>(L.count, L.start, pos, L.perm, L.xs, L.ys, L.zs, err);
+  k_tile_box<<<L.nT, 256, 0, s>>>(n, L.T, L.xs, L.ys, L.zs, L.gbox, L.box);
+  const float rc2m = rc * rc * 1.00001f;
+  k_tile_adj<<<L.nT, 128, 0, s>>>(L.nT, L.nwords, L.box, rc2m, L.adj, L.rowptr);
+  k_scan_excl<<<1, 1024, 0, s>>>(L.nT, L.rowptr, L.rowptr);
+  k_tile_list<<<(L.nT + 127) / 128, 128, 0, s>>>(L.nT, L.nwords, L.adj, L.rowptr, L.pairs);
+  const bool sw = rs < rc;
+  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f};
+  const int32_t* np = L.rowptr + L.nT;
+#define OD_CUTN3(MT, MS, PA, CUT, CNT)                                                        \
+  k_pairs_cutn3<MT, MS, PA, CUT, CNT><<<L.grid, kWarps * 32, n3_traits<MT, MS, PA>::SMEM, s>>>( \
+      L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.S, cut, L.gbox, rc2m, pair_count)
+  if (L.ipt == 4 && L.T == 1024) {
+    if (sw) { if (pair_count) OD_CUTN3(4, 4, 1, 1, true); else OD_CUTN3(4, 4, 1, 1, false); }
+    else { if (pair_count) OD_CUTN3(4, 4, 1, 2, true); else OD_CUTN3(4, 4, 1, 2, false); }
+  } else if (L.ipt == 2 && L.T == 512) {
+    if (sw) { if (pair_count) OD_CUTN3(2, 2, 1, 1, true); else OD_CUTN3(2, 2, 1, 1, false); }
+    else { if (pair_count) OD_CUTN3(2, 2, 1, 2, true); else OD_CUTN3(2, 2, 1, 2, false); }
+  } else {
+    return cudaErrorInvalidValue;
+  }
+#undef OD_CUTN3
+  const size_t smem = sizeof(int32_t) * (L.nT + 8);
+  k_tile_reduce<<<L.nT, 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm, part_hi,
+                                        part_lo);
+  return cudaGetLastError();
 }

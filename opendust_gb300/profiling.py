@@ -2,6 +2,7 @@
 
     python -m opendust_gb300.profiling pairs  --n 65536  --plan 256,1,5 --steps 2
     python -m opendust_gb300.profiling cutoff --n 131072 --variant 2    --steps 2
+    python -m opendust_gb300.profiling cutoff --n 524288 --variant 3 --plan 256,2,3 --steps 2
     python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576 [--plans '256,1,5;256,4,7']
 
 `pairs` steps the small_plain workload with the given all-pairs plan, `cutoff` the field_chain
@@ -35,12 +36,12 @@ def run_pairs(N, plan, steps):
         print("ok", eng.pair_plan(), eng.series()["q"][-1])
 
 
-def run_cutoff(N, variant, steps):
+def run_cutoff(N, variant, steps, plan=None):
     plasma, sim, grains, dist, ext = workloads.field_chain(N=N, n=steps + 4)
     holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, **ext)
     with _lib.Engine(holder) as eng:
         eng.set_graph(False)
-        eng.set_pair_plan(128, 1, variant)
+        eng.set_pair_plan(*(plan or (128, 1, variant)))
         eng.init_state(setup_host.field_driven_vz_table(plasma.v_fl, plasma.v_T))
         eng.step(steps)
         print("ok", eng.series()["q"][-1])
@@ -77,7 +78,8 @@ def main():
     if a.what == "pairs":
         run_pairs(int(a.n), tuple(int(x) for x in a.plan.split(",")), a.steps)
     elif a.what == "cutoff":
-        run_cutoff(int(a.n), a.variant, a.steps)
+        plan = tuple(int(x) for x in a.plan.split(",")) if a.variant == 3 else None
+        run_cutoff(int(a.n), a.variant, a.steps, plan)
     else:
         plans = [tuple(int(x) for x in p.split(",")) for p in a.plans.split(";") if p]
         run_sweep([int(x) for x in a.n.split(",")], plans)

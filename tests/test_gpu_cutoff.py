@@ -1,4 +1,6 @@
-"""GPU tests of the cutoff force path (device cell list) against the CPU oracle.
+"""GPU tests of the cutoff force path against the CPU oracle: variants 0 and 2 walk a stencil
+of cells per target cell; variant 3 (the default) sorts the ions along a Morton curve and
+evaluates each unordered pair once over tile pairs whose bounding boxes come within r_c.
 
 Tolerances:
   * with OpenMM's switching polynomial (the reference's cutOff=True: cutoff 3.2 lambda, switch
@@ -22,13 +24,17 @@ def _cut_case(N, seed, **kw):
     return case(N=N, n=4, seed=seed, **kw)
 
 
-@pytest.mark.parametrize("variant", [0, 2])
+PLANS = {0: (128, 1, 0), 2: (128, 1, 2), 3: (256, 4, 3), 32: (256, 2, 3)}
+
+
+@pytest.mark.parametrize("variant", [0, 2, 3, 32])
 def test_cutoff_switching_snapshot(gpu_lib, variant):
     holder, pos, vel, plasma, sim, grains = _cut_case(4096, 21, cutOff=True)
     assert holder.cfg.force_method == _lib.OD_FORCE_CUTOFF
     pos = plant_close_pairs(pos, plasma.r_D_e, np.random.default_rng(3), n_pairs=32, dmin=2e-4)
     with _lib.Engine(holder) as eng:
-        eng.set_pair_plan(128, 1, variant)
+        eng.set_pair_plan(*PLANS[variant])
+        assert eng.pair_plan()["variant"] == PLANS[variant][2]
         f = eng.force_snapshot(pos)
     ref = oracle.force_snapshot(holder, pos, round32=True)
     err = rel_err_per_ion(f, ref)
@@ -36,14 +42,15 @@ def test_cutoff_switching_snapshot(gpu_lib, variant):
     assert err.max() <= 1e-5
 
 
-@pytest.mark.parametrize("N,variant", [(4096, 0), (4096, 2), (2**17, 2)])
+@pytest.mark.parametrize("N,variant", [(4096, 0), (4096, 2), (2**17, 2), (4096, 3), (2**17, 3),
+                                       (2**17, 32)])
 def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N, variant):
     spatial = pytest.importorskip("scipy.spatial")
     holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=22, builder=workloads.field_chain,
                                                  switch_distance=0.0)
     assert holder.cfg.switch_dist == 0.0
     with _lib.Engine(holder) as eng:
-        eng.set_pair_plan(128, 1, variant)
+        eng.set_pair_plan(*PLANS[variant])
         f = eng.force_snapshot(pos)
         eng.set_state(pos, vel)
         eng.set_timing(True)
