@@ -232,15 +232,17 @@ def run_reference(args, dist: Dist):
     return 0
 
 
-def load_traffic(n_ions: int, variant: int):
-    """DRAM bytes per all-pairs force evaluation from the committed ncu capture of the same size
-    and kernel variant."""
-    path = os.path.join(ROOT, "profiles", "allpairs_traffic.json")
+def load_traffic(n_ions: int, plan: dict, cutoff: bool = False):
+    """DRAM bytes per force evaluation from the committed ncu capture of the same size and
+    kernel variant (all-pairs kernel, or the cutoff force chain with its tile size)."""
+    name = "cutoff_traffic.json" if cutoff else "allpairs_traffic.json"
     try:
-        d = json.load(open(path))
+        d = json.load(open(os.path.join(ROOT, "profiles", name)))
     except (OSError, ValueError):
         return None
-    ok = d.get("n_ions") == n_ions and d.get("variant") == variant
+    ok = d.get("n_ions") == n_ions and d.get("variant") == plan["variant"]
+    if "tile" in d:
+        ok = ok and d["tile"] == plan["jsplit"]
     return d.get("dram_bytes_per_launch") if ok else None
 
 
@@ -254,7 +256,7 @@ def run_ours(args, dist: Dist):
     torch.cuda.set_device(device)
     K, W = args.steps, args.warmup
     K_e2e = max(2, K)
-    n_total = W + K + K_e2e + 4
+    n_total = W + K + K_e2e + 5
     plasma, sim, grains, d, ext = workload(args.workload, n_total)
     seed = 1000 + dist.rank
     holder, _ = build_simulation(plasma, sim, grains, d, seed=seed, device=device, **ext)
@@ -267,7 +269,7 @@ def run_ours(args, dist: Dist):
     plan = eng.pair_plan()
     eng.set_state(pos, vel)
     eng.step(W)  # warm-up (graph replay path)
-    eng.set_timing(True)
+    eng.set_timing(True, count_pairs=False)
     clocks = Clocks(device)
     dist.barrier()
     torch.cuda.synchronize()
@@ -280,7 +282,12 @@ def run_ours(args, dist: Dist):
     clk = clocks.stop()
     dist.barrier()
     step_ms, nsteps, pair_ms, pair_launches = eng.timing()
-    cut_pairs = eng.cutoff_pairs()
+    cut_pairs = 0
+    if holder.cfg.force_method == _lib.OD_FORCE_CUTOFF:
+        # one more (untimed) step with the counting kernel: pairs inside the cutoff per launch
+        eng.set_timing(True, count_pairs=True)
+        eng.step(1)
+        cut_pairs = eng.cutoff_pairs() * pair_launches / max(eng.timing()[3], 1)
     eng.set_timing(False)
     t_max = dist.reduce(step_ms, "max")
     ions_all = dist.reduce(float(N * K), "sum")
@@ -290,7 +297,7 @@ def run_ours(args, dist: Dist):
     pairs_per_launch = cut_pairs / pair_launches if cutoff else N * (N - 1)
     achieved = pairs_per_launch * FLOPS_PER_PAIR / pair_avg_s / 1e12
     n3 = not cutoff and plan["variant"] == 7
-    traffic = None if cutoff else load_traffic(N, plan["variant"])
+    traffic = load_traffic(N, plan, cutoff)
     if cutoff and plan["variant"] == 3:
         kernel = (f"Morton sort + tile-pair list + k_pairs_cutn3 (each pair once, {plan['jsplit']}-ion "
                   "tiles, 64-ion group pairs beyond r_c skipped; pairs inside the cutoff credited)")

@@ -243,7 +243,9 @@ od_status od_step(od_handle* h, int64_t nsteps);
  * time.time(), performance/NVIDIA-V100/benchmark.py:82-87). With timing enabled, od_step
  * launches kernel by kernel and records CUDA events on the handle's stream around every step
  * and every all-pairs force launch; od_get_timing returns the summed device milliseconds.
- * Enabling resets the sums. Without timing, od_step replays a CUDA graph of one step. */
+ * enable: 0 off, 1 on (the cutoff force kernels also count the pairs inside the cutoff for
+ * od_get_cutoff_pairs), 2 on without counting (the kernels a step runs untimed). Enabling
+ * resets the sums and the count. Without timing, od_step replays a CUDA graph of one step. */
 od_status od_set_timing(od_handle* h, int32_t enable);
 od_status od_get_timing(od_handle* h, double* step_ms, int64_t* steps, double* pair_ms,
                         int64_t* pair_launches);

@@ -391,8 +391,11 @@ class Engine:
         check(self._lib.od_get_averages(self.h, _dptr(out), ctypes.byref(n)), self.h)
         return out, int(n.value)
 
-    def set_timing(self, enable: bool = True):
-        check(self._lib.od_set_timing(self.h, int(bool(enable))), self.h)
+    def set_timing(self, enable: bool = True, count_pairs: bool = True):
+        """Kernel-by-kernel steps with device events; count_pairs: the cutoff kernels also
+        count the pairs inside the cutoff (cutoff_pairs())."""
+        mode = 0 if not enable else (1 if count_pairs else 2)
+        check(self._lib.od_set_timing(self.h, mode), self.h)
 
     def timing(self):
         """(step_ms, steps, pair_ms, pair_launches) summed since timing was enabled."""

@@ -42,6 +42,7 @@ struct od_handle {
   bool use_graph = true;
   // device timing (events on the handle's stream)
   bool timing = false;
+  bool count_pairs = false;  // timing mode 1: the cutoff kernel also counts its pairs
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, int>> ev_step, ev_pair;  // indices into ev_pool
   double t_step_ms = 0, t_pair_ms = 0;
@@ -708,7 +709,7 @@ static od_status event_at(od_handle* h, size_t slot, int* idx) {
 // launch (timing mode).
 static od_status step_timed(od_handle* h, int64_t nsteps) {
   size_t slot = 0;
-  const od_force_ctx fc = force_ctx(h, true);
+  const od_force_ctx fc = force_ctx(h, h->count_pairs);
   h->ev_step.clear();
   h->ev_pair.clear();
   for (int64_t s = 0; s < nsteps; s++) {
@@ -786,7 +787,9 @@ extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
 
 extern "C" od_status od_set_timing(od_handle* h, int32_t enable) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (enable < 0 || enable > 2) return fail(h, OD_ERR_INVALID, "timing mode must be 0, 1 or 2");
   h->timing = enable != 0;
+  h->count_pairs = enable == 1;
   h->t_step_ms = h->t_pair_ms = 0;
   h->t_steps = h->t_pair_launches = 0;
   if (h->d_pairs) OD_CK(h, cudaMemsetAsync(h->d_pairs, 0, sizeof(unsigned long long), h->stream));
@@ -954,14 +957,16 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (h->has_cut) {
     // cutoff method: variant 0 selects the scalar pair kernel, 2 the packed one, 3 the tile
-    // pairs with each pair once (targets_per_thread 4: 1024-ion tiles, 2: 512-ion tiles)
+    // pairs with each pair once (targets_per_thread 2: 512-ion tiles, 4: 1024-ion tiles; a
+    // positive jsplit must name that tile size)
     if (variant != 0 && variant != 2 && variant != 3)
       return fail(h, OD_ERR_INVALID, "cutoff variants are 0, 2 and 3");
     if (variant == 3) {
-      if (targets_per_thread != 2 && targets_per_thread != 4)
-        return fail(h, OD_ERR_INVALID, "cutoff variant 3 takes 2 or 4 targets per lane");
-      const int T = targets_per_thread == 4 ? 1024 : 512;
-      if (!h->cut.n3 || h->cut.n3->T != T) {
+      const int T = jsplit > 0 ? jsplit : (targets_per_thread == 4 ? 1024 : 512);
+      if (!od_cutn3_supported(targets_per_thread, T))
+        return fail(h, OD_ERR_INVALID,
+                    "cutoff variant 3 takes (2, 512) or (4, 1024) as (targets per lane, tile)");
+      if (!h->cut.n3 || h->cut.n3->T != T || h->cut.n3->ipt != targets_per_thread) {
         od_status st = alloc_cutn3(h, targets_per_thread, T);
         if (st != OD_OK) return st;
       }

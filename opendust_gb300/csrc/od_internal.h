@@ -118,6 +118,7 @@ struct od_cutn3 {
 };
 size_t od_cutn3_bytes(int N, int T, int G);
 int od_cutn3_grid(int N);           // cells per axis for N ions
+bool od_cutn3_supported(int ipt, int T);
 cudaError_t od_cutn3_prepare(int ipt, int T);
 cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
                                 float4* part_lo, float rho0, float rc, float rs, uint32_t* err,

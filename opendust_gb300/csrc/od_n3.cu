@@ -603,9 +603,228 @@ __global__ void k_tile_list(int nT, int nwords, const uint32_t* __restrict__ adj
   }
 }
 
+// Balanced tile pair of the cutoff path: 512-ion tiles, NBT target groups of GT = 32·MT ions
+// and NBS source groups of GS = 32·MS ions per tile (MT targets and MS sources per lane). The
+// group pairs whose boxes come within the cutoff form a list in (target group, source group)
+// order, and warp w takes the contiguous slice [w·n/8, (w+1)·n/8) of it, so that the warps
+// evaluate the same number of group pairs (± 1) whatever the culling left and no barrier
+// separates them. A warp keeps one target group while consecutive items share it and sums its
+// targets into a segment slot of its own (a new segment at every change of target group and
+// at every slice start: at most NBT + 7); every item stores its FP32 reaction sums in a slot of
+// its own. The block then sums the slots of each ion in a fixed order — target segments in list
+// order, then reactions in target-group order — so the result does not depend on which warp
+// ran what, or when.
+template <int MT, int MS>
+struct cut_traits {
+  static constexpr int GT = 32 * MT, GS = 32 * MS;    // target and source group sizes
+  static constexpr int T = 512;                       // ions per tile
+  static constexpr int NBT = T / GT, NBS = T / GS;    // groups per tile
+  static constexpr int NI = NBT * NBS;                // group pairs per tile pair (<= 64)
+  static constexpr int NSEG = NBT + kWarps;           // target segments
+  static constexpr bool HS = MT > 2;                  // target sums kept in the segment slot
+  static constexpr size_t RFL = (size_t)NI * 3 * GS;  // reaction slots (floats)
+  static constexpr size_t TFL = (size_t)NSEG * 6 * GT;  // two-float target segment slots
+  static constexpr size_t SMEM = sizeof(float) * (RFL + TFL) + 256;  // + list metadata
+};
+
+// warp that owns list entry i of n
+__device__ __forceinline__ int cut_owner(int i, int n) {
+  int w = 0;
+  while (w < kWarps - 1 && (((w + 1) * n) >> 3) <= i) w++;
+  return w;
+}
+
+// group pair (ga, gb) of a diagonal tile: 2 each pair once, 1 directed (the sources lie in the
+// target group), 0 skipped (counted from the other side)
+template <int GT, int GS>
+__device__ __forceinline__ int cut_diag_mode(int ga, int gb) {
+  const int t0 = ga * GT, s0 = gb * GS;
+  return s0 >= t0 + GT ? 2 : (s0 >= t0 ? 1 : 0);
+}
+
+template <int MT, int MS, int CUT, bool COUNT>
+__device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ sx,
+                                                      const float* __restrict__ sy,
+                                                      const float* __restrict__ sz,
+                                                      float* __restrict__ outT,
+                                                      float* __restrict__ outR,
+                                                      const n3_consts& k, int a, int b, float* sm,
+                                                      const float* __restrict__ gbox,
+                                                      float cull2) {
+  using CT = cut_traits<MT, MS>;
+  constexpr int GT = CT::GT, GS = CT::GS, T = CT::T, NBT = CT::NBT, NBS = CT::NBS, NI = CT::NI;
+  constexpr int MS2 = MS / 2;
+  constexpr bool HS = CT::HS;
+  static_assert(NI % 32 == 0 && NI <= 64 && NBT <= 8, "list of at most 64 group pairs");
+  float* const R = sm;              // [NI][3][GS] reaction sums of each listed group pair
+  float* const Tg = sm + CT::RFL;   // [NSEG][6][GT] two-float target sums of each segment
+  unsigned char* const items = reinterpret_cast<unsigned char*>(Tg + CT::TFL);  // ga·NBS + gb
+  unsigned char* const segid = items + 64;                                       // per entry
+  signed char* const item_of = reinterpret_cast<signed char*>(items + 128);      // by ga·NBS+gb
+  signed char* const gs0 = item_of + 64;  // first and last segment of each target group
+  signed char* const gs1 = gs0 + 8;
+  int* const s_n = reinterpret_cast<int*>(items + 208);
+  const bool diag = a == b;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
+
+  // 1. the list (warp 0): group pairs within range; on a diagonal tile the source groups
+  // inside a target group (directed) and those above it
+  if (w == 0) {
+    int n = 0;
+    for (int r = 0; r < NI / 32; r++) {
+      const int c = r * 32 + lane, ga = c / NBS, gb = c % NBS;
+      const int mode = diag ? cut_diag_mode<GT, GS>(ga, gb) : 2;
+      bool keep = mode == 1;
+      if (mode == 2) {
+        float ta[6], tb[6];
+        group_box(gbox, (a * NBT + ga) * (GT / 64), GT / 64, ta);
+        group_box(gbox, (b * NBS + gb) * (GS / 64), GS / 64, tb);
+        float d2 = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float gap = fmaxf(fmaxf(tb[d] - ta[3 + d], ta[d] - tb[3 + d]), 0.f);
+          d2 = fmaf(gap, gap, d2);
+        }
+        keep = d2 < cull2;
+      }
+      const unsigned int bal = __ballot_sync(0xffffffffu, keep);
+      const int pos = n + __popc(bal & ((1u << lane) - 1u));
+      if (keep) items[pos] = (unsigned char)c;
+      item_of[c] = keep ? (signed char)pos : (signed char)-1;
+      n += __popc(bal);
+    }
+    __syncwarp();
+    // a segment starts at every change of target group and at the start of every slice
+    int nseg = 0;
+    for (int r = 0; r < 2; r++) {
+      const int i = r * 32 + lane;
+      bool f = false;
+      if (i < n)
+        f = i == 0 || items[i - 1] / NBS != items[i] / NBS ||
+            cut_owner(i - 1, n) != cut_owner(i, n);
+      const unsigned int bal = __ballot_sync(0xffffffffu, f);
+      if (i < n) segid[i] = (unsigned char)(nseg + __popc(bal & ((2u << lane) - 1u)) - 1);
+      nseg += __popc(bal);
+    }
+    if (lane < 8) { gs0[lane] = 0; gs1[lane] = -1; }
+    __syncwarp();
+    for (int r = 0; r < 2; r++) {
+      const int i = r * 32 + lane;
+      if (i < n) {
+        const int ga = items[i] / NBS;
+        if (i == 0 || items[i - 1] / NBS != ga) gs0[ga] = (signed char)segid[i];
+        if (i == n - 1 || items[i + 1] / NBS != ga) gs1[ga] = (signed char)segid[i];
+      }
+    }
+    if (lane == 0) *s_n = n;
+  }
+  __syncthreads();
+
+  // 2. this warp's slice of the list
+  const int n = *s_n, i0 = (w * n) >> 3, i1 = ((w + 1) * n) >> 3;
+  unsigned int cnt = 0;
+  od_u64 X[MT], Y[MT], Z[MT];
+  float hreg[HS ? 1 : 6 * MT];
+  float* hs = Tg + lane;  // HS: this warp's current segment slot (lane-private words)
+#define CUT_H(c, kt) (HS ? hs[(c) * GT + 32 * (kt)] : hreg[(c) * MT + (kt)])
+  int cur = -1;
+  for (int i = i0; i < i1; i++) {
+    const int c = items[i], ga = c / NBS, gb = c % NBS;
+    if (ga != cur) {
+      if (!HS && cur >= 0) {
+        float* t = Tg + (size_t)segid[i - 1] * 6 * GT + lane;
+#pragma unroll
+        for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
+      }
+      if (HS) hs = Tg + (size_t)segid[i] * 6 * GT + lane;
+#pragma unroll
+      for (int kt = 0; kt < MT; kt++) {
+        const int j = (a * NBT + ga) * GT + lane + 32 * kt;
+        const float x = sx[j], y = sy[j], z = sz[j];
+        X[kt] = p2(x, x); Y[kt] = p2(y, y); Z[kt] = p2(z, z);
+#pragma unroll
+        for (int q = 0; q < 6; q++) CUT_H(q, kt) = 0.f;
+      }
+      cur = ga;
+    }
+    od_u64 QX[MS2], QY[MS2], QZ[MS2], RX[MS2], RY[MS2], RZ[MS2], AX[MT], AY[MT], AZ[MT];
+#pragma unroll
+    for (int q = 0; q < MS2; q++) {
+      const int j = (b * NBS + gb) * GS + lane + 64 * q;
+      QX[q] = p2(sx[j], sx[j + 32]);
+      QY[q] = p2(sy[j], sy[j + 32]);
+      QZ[q] = p2(sz[j], sz[j + 32]);
+      RX[q] = RY[q] = RZ[q] = 0ull;
+    }
+#pragma unroll
+    for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
+    if (diag && cut_diag_mode<GT, GS>(ga, gb) == 1) {
+      n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                          cnt);
+    } else {
+      n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                         cnt);
+      // the force on the sources is minus the accumulated terms
+      float* r = R + (size_t)i * 3 * GS + lane;
+#pragma unroll
+      for (int q = 0; q < MS2; q++) {
+        const float2 rx = up2(RX[q]), ry = up2(RY[q]), rz = up2(RZ[q]);
+        r[64 * q] = -rx.x; r[64 * q + 32] = -rx.y;
+        r[GS + 64 * q] = -ry.x; r[GS + 64 * q + 32] = -ry.y;
+        r[2 * GS + 64 * q] = -rz.x; r[2 * GS + 64 * q + 32] = -rz.y;
+      }
+    }
+#pragma unroll
+    for (int kt = 0; kt < MT; kt++) {
+      od_acc2(CUT_H(0, kt), CUT_H(3, kt), sum2(AX[kt]));
+      od_acc2(CUT_H(1, kt), CUT_H(4, kt), sum2(AY[kt]));
+      od_acc2(CUT_H(2, kt), CUT_H(5, kt), sum2(AZ[kt]));
+    }
+  }
+  if (!HS && cur >= 0) {
+    float* t = Tg + (size_t)segid[i1 - 1] * 6 * GT + lane;
+#pragma unroll
+    for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
+  }
+#undef CUT_H
+  __syncthreads();
+
+  // 3. fixed-order sums of the slots; every ion of both tiles is written (zeros when no group
+  // pair reached it)
+  for (int e = tid; e < T; e += kWarps * 32) {
+    const int g = e / GT, l = e % GT;
+    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    for (int s = gs0[g]; s <= gs1[g]; s++) {
+      const float* t = Tg + (size_t)s * 6 * GT + l;
+      acc2x2(hx, lx, t[0], t[3 * GT]);
+      acc2x2(hy, ly, t[GT], t[4 * GT]);
+      acc2x2(hz, lz, t[2 * GT], t[5 * GT]);
+    }
+    if (!diag) {
+      outT[e] = hx; outT[T + e] = hy; outT[2 * T + e] = hz;
+      outT[3 * T + e] = lx; outT[4 * T + e] = ly; outT[5 * T + e] = lz;
+      hx = hy = hz = lx = ly = lz = 0.f;
+    }
+    const int gb = e / GS, l2 = e % GS;
+    for (int ga = 0; ga < NBT; ga++) {
+      const int it = item_of[ga * NBS + gb];
+      if (it < 0 || (diag && cut_diag_mode<GT, GS>(ga, gb) == 1)) continue;
+      const float* r = R + (size_t)it * 3 * GS + l2;
+      od_acc2(hx, lx, r[0]);
+      od_acc2(hy, ly, r[GS]);
+      od_acc2(hz, lz, r[2 * GS]);
+    }
+    outR[e] = hx; outR[T + e] = hy; outR[2 * T + e] = hz;
+    outR[3 * T + e] = lx; outR[4 * T + e] = ly; outR[5 * T + e] = lz;
+  }
+  __syncthreads();  // the next tile pair rewrites the list and the slots
+  return cnt;
+}
+
 // every listed tile pair, each unordered ion pair once (static assignment: pair k to block
-// k mod grid), group pairs beyond the cutoff skipped
-template <int MT, int MS, int PA, int CUT, bool COUNT>
+// k mod grid), group pairs beyond the cutoff skipped. BAL: the balanced list routine above
+// (512-ion tiles); otherwise the staggered tile-pair routine.
+template <int MT, int MS, int PA, int CUT, bool COUNT, bool BAL>
 __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
     k_pairs_cutn3(const float* __restrict__ xs, const float* __restrict__ ys,
                   const float* __restrict__ zs, int nslots, int nT,
@@ -613,15 +832,26 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
                   float* __restrict__ S, n3_cut cut, const float* __restrict__ gbox, float cull2,
                   unsigned long long* __restrict__ pair_count) {
   extern __shared__ float sm[];
-  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
+  constexpr size_t T6 = 6 * (size_t)(BAL ? cut_traits<MT, MS>::T : n3_traits<MT, MS, PA>::T);
+  static_assert(!BAL || PA == 1, "balanced list: one pass");
   const int np = *npairs;
   unsigned int cnt = 0;
-  for (int k = blockIdx.x; k < np; k += gridDim.x) {
-    const int2 ab = pairs[k];
-    cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots,
-                                                      S + ((size_t)ab.x * nT + ab.y) * T6,
-                                                      S + ((size_t)ab.y * nT + ab.x) * T6, cut,
-                                                      ab.x, ab.y, sm, gbox, cull2);
+  if constexpr (BAL) {
+    const n3_consts kc = make_consts(cut);
+    for (int k = blockIdx.x; k < np; k += gridDim.x) {
+      const int2 ab = pairs[k];
+      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, S + ((size_t)ab.x * nT + ab.y) * T6,
+                                               S + ((size_t)ab.y * nT + ab.x) * T6, kc, ab.x,
+                                               ab.y, sm, gbox, cull2);
+    }
+  } else {
+    for (int k = blockIdx.x; k < np; k += gridDim.x) {
+      const int2 ab = pairs[k];
+      cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots,
+                                                        S + ((size_t)ab.x * nT + ab.y) * T6,
+                                                        S + ((size_t)ab.y * nT + ab.x) * T6, cut,
+                                                        ab.x, ab.y, sm, gbox, cull2);
+    }
   }
   if (COUNT) {
 #pragma unroll
@@ -783,23 +1013,32 @@ size_t od_cutn3_bytes(int N, int T, int G) {
          + sizeof(int32_t) * (ns + N + 3 * nc + nT + 4);
 }
 
-cudaError_t od_cutn3_prepare(int ipt, int T) {
-  if (ipt == 4 && T == 1024) {
-    const int smem = (int)n3_traits<4, 4, 1>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 1, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 1, true>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 2, false>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_pairs_cutn3<4, 4, 1, 2, true>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    return e;
+// cutoff tile-pair shapes: (ipt, T) = (2, 512) the balanced list with 2 x 2 targets x sources
+// per lane, (4, 1024) the staggered tile pair with 4 x 4. Measured on GB300 at 2^19 ions
+// (field_chain): 45.2 ms per step with (2, 512), 48.1 with the balanced list at 4 x 2 (128-ion
+// target groups: more arithmetic per shuffle, but coarser culling), 55.7 with (4, 1024).
+template <int MT, int MS, bool BAL>
+cudaError_t prepare_cutn3(int smem) {
+  void* fn[4] = {(void*)k_pairs_cutn3<MT, MS, 1, 1, false, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 1, true, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 2, false, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 2, true, BAL>};
+  for (int q = 0; q < 4; q++) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn[q], cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
   }
-  if (ipt == 2 && T == 512) return cudaSuccess;  // (2, 2, 1): 12 KB, no opt-in needed
+  return cudaSuccess;
+}
+
+bool od_cutn3_supported(int ipt, int T) {
+  return (ipt == 2 && T == 512) || (ipt == 4 && T == 1024);
+}
+
+cudaError_t od_cutn3_prepare(int ipt, int T) {
+  if (ipt == 2 && T == 512) return prepare_cutn3<2, 2, true>((int)cut_traits<2, 2>::SMEM);
+  if (ipt == 4 && T == 1024)
+    return prepare_cutn3<4, 4, false>((int)n3_traits<4, 4, 1>::SMEM);
   return cudaErrorInvalidValue;
 }
 
@@ -819,18 +1058,23 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
   const bool sw = rs < rc;
   const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f};
   const int32_t* np = L.rowptr + L.nT;
-#define OD_CUTN3(MT, MS, PA, CUT, CNT)                                                        \
-  k_pairs_cutn3<MT, MS, PA, CUT, CNT><<<L.grid, kWarps * 32, n3_traits<MT, MS, PA>::SMEM, s>>>( \
+#define OD_CUTN3(MT, MS, BAL, SM)                                                             \
+  do {                                                                                        \
+    if (sw) {                                                                                 \
+      if (pair_count) OD_CUTN3L(MT, MS, 1, true, BAL, SM);                                    \
+      else OD_CUTN3L(MT, MS, 1, false, BAL, SM);                                              \
+    } else {                                                                                  \
+      if (pair_count) OD_CUTN3L(MT, MS, 2, true, BAL, SM);                                    \
+      else OD_CUTN3L(MT, MS, 2, false, BAL, SM);                                              \
+    }                                                                                         \
+  } while (0)
+#define OD_CUTN3L(MT, MS, CUT, CNT, BAL, SM)                                                  \
+  k_pairs_cutn3<MT, MS, 1, CUT, CNT, BAL><<<L.grid, kWarps * 32, SM, s>>>(                    \
       L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.S, cut, L.gbox, rc2m, pair_count)
-  if (L.ipt == 4 && L.T == 1024) {
-    if (sw) { if (pair_count) OD_CUTN3(4, 4, 1, 1, true); else OD_CUTN3(4, 4, 1, 1, false); }
-    else { if (pair_count) OD_CUTN3(4, 4, 1, 2, true); else OD_CUTN3(4, 4, 1, 2, false); }
-  } else if (L.ipt == 2 && L.T == 512) {
-    if (sw) { if (pair_count) OD_CUTN3(2, 2, 1, 1, true); else OD_CUTN3(2, 2, 1, 1, false); }
-    else { if (pair_count) OD_CUTN3(2, 2, 1, 2, true); else OD_CUTN3(2, 2, 1, 2, false); }
-  } else {
-    return cudaErrorInvalidValue;
-  }
+  if (L.ipt == 2 && L.T == 512) OD_CUTN3(2, 2, true, (cut_traits<2, 2>::SMEM));
+  else if (L.ipt == 4 && L.T == 1024) OD_CUTN3(4, 4, false, (n3_traits<4, 4, 1>::SMEM));
+  else return cudaErrorInvalidValue;
+#undef OD_CUTN3L
 #undef OD_CUTN3
   const size_t smem = sizeof(int32_t) * (L.nT + 8);
   k_tile_reduce<<<L.nT, 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm, part_hi,

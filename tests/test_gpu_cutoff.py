@@ -24,6 +24,8 @@ def _cut_case(N, seed, **kw):
     return case(N=N, n=4, seed=seed, **kw)
 
 
+# 3: 1024-ion tiles with 4 x 4 targets x sources per lane (staggered tile pairs); 32: 512-ion
+# tiles with 2 x 2 (balanced group-pair lists, the default)
 PLANS = {0: (128, 1, 0), 2: (128, 1, 2), 3: (256, 4, 3), 32: (256, 2, 3)}
 
 
@@ -43,7 +45,7 @@ def test_cutoff_switching_snapshot(gpu_lib, variant):
 
 
 @pytest.mark.parametrize("N,variant", [(4096, 0), (4096, 2), (2**17, 2), (4096, 3), (2**17, 3),
-                                       (2**17, 32)])
+                                       (2**17, 32), (4096, 32)])
 def test_cutoff_hard_snapshot_and_pair_count(gpu_lib, N, variant):
     spatial = pytest.importorskip("scipy.spatial")
     holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=22, builder=workloads.field_chain,
