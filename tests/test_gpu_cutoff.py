@@ -90,3 +90,18 @@ def test_cutoff_deterministic_and_one_step(gpu_lib):
     print(f"cutoff one step: max |dx| {dpos:.3e} lambda, max |dv| {dvel:.3e} v_T")
     assert dpos < 1e-5
     assert dvel < 1e-4
+
+
+def test_timing_modes_count_pairs_only_when_asked(gpu_lib):
+    # timing mode 2 runs the production kernel (no counter); mode 1 counts; other modes are rejected
+    holder, pos, vel, plasma, sim, grains = _cut_case(4096, 24, cutOff=True)
+    with _lib.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        eng.set_timing(True, count_pairs=False)
+        eng.step(1)
+        assert eng.cutoff_pairs() == 0 and eng.timing()[1] == 1
+        eng.set_timing(True, count_pairs=True)
+        eng.step(1)
+        assert eng.cutoff_pairs() > 0
+        assert eng._lib.od_set_timing(eng.h, 3) == 1  # OD_ERR_INVALID
+        eng.set_timing(False)
