@@ -105,3 +105,26 @@ def test_timing_modes_count_pairs_only_when_asked(gpu_lib):
         assert eng.cutoff_pairs() > 0
         assert eng._lib.od_set_timing(eng.h, 3) == 1  # OD_ERR_INVALID
         eng.set_timing(False)
+
+
+def test_cutoff_time_averages(gpu_lib):
+    # field-driven chain of 5 grains with the 2 lambda cutoff (the C3 physics at 2048 ions):
+    # time-averaged charges and orbit forces over the last 150 of 300 steps within 1 % of the
+    # oracle's (orbit forces as one norm over the chain: inner grains are shielded and carry
+    # small net forces)
+    holder, pos, vel, plasma, *_ = case(N=2048, n=300, seed=25, builder=workloads.field_chain,
+                                        avg_start=150)
+    with _lib.Engine(holder) as eng:
+        assert eng.pair_plan()["variant"] == 3
+        eng.set_state(pos, vel)
+        eng.step(300)
+        avg, navg = eng.averages()
+    ref = oracle.run(holder, pos, vel, 0, 300, round32=True)
+    assert navg == 150
+    q_ref = ref["q"][150:].mean(0)
+    o_ref = ref["orbit"][150:].mean(0)
+    dq = np.max(np.abs(avg[:, 0] - q_ref) / np.abs(q_ref))
+    do = np.linalg.norm(avg[:, 1:4] - o_ref) / np.linalg.norm(o_ref)
+    print(f"cutoff time averages (5 grains): q rel {dq:.3e}, orbit rel {do:.3e}")
+    assert dq < 0.01
+    assert do < 0.01
