@@ -861,7 +861,9 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
 }
 
 // Row sums over the tiles that share a listed pair with tile t, in increasing tile order,
-// written to the ions' entries of (ph, pl).
+// written to the ions' entries of (ph, pl). Block (t, c) sums ions c·256 .. c·256+255 of tile t,
+// one ion per thread; the matrix rows are read once (streaming loads, four neighbours in flight
+// per thread), so the kernel runs at the HBM rate.
 __global__ void __launch_bounds__(256) k_tile_reduce(int nT, int nwords, int T,
                                                      const uint32_t* __restrict__ adj,
                                                      const float* __restrict__ S,
@@ -896,20 +898,35 @@ __global__ void __launch_bounds__(256) k_tile_reduce(int nT, int nwords, int T,
     __syncthreads();
   }
   const int m = s_m;
-  for (int e = threadIdx.x; e < T; e += 256) {
-    const int slot = t * T + e;
-    const int i = perm[slot];
-    if (i < 0) continue;
-    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-    for (int q = 0; q < m; q++) {
-      const float* r = S + ((size_t)t * nT + nb[q]) * 6 * (size_t)T + e;
-      acc2x2(hx, lx, r[0], r[3 * T]);
-      acc2x2(hy, ly, r[T], r[4 * T]);
-      acc2x2(hz, lz, r[2 * T], r[5 * T]);
+  const int e = blockIdx.y * 256 + threadIdx.x;
+  const int i = perm[t * T + e];
+  if (i < 0) return;  // sentinel slot (no barrier follows)
+  const float* row = S + (size_t)t * nT * 6 * (size_t)T + e;
+  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+  int q = 0;
+  for (; q + 4 <= m; q += 4) {
+    float v[4][6];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float* r = row + (size_t)nb[q + u] * 6 * T;
+#pragma unroll
+      for (int c = 0; c < 6; c++) v[u][c] = __ldcs(r + c * T);
     }
-    ph[i] = make_float4(hx, hy, hz, 0.f);
-    pl[i] = make_float4(lx, ly, lz, 0.f);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      acc2x2(hx, lx, v[u][0], v[u][3]);
+      acc2x2(hy, ly, v[u][1], v[u][4]);
+      acc2x2(hz, lz, v[u][2], v[u][5]);
+    }
   }
+  for (; q < m; q++) {
+    const float* r = row + (size_t)nb[q] * 6 * T;
+    acc2x2(hx, lx, __ldcs(r), __ldcs(r + 3 * T));
+    acc2x2(hy, ly, __ldcs(r + T), __ldcs(r + 4 * T));
+    acc2x2(hz, lz, __ldcs(r + 2 * T), __ldcs(r + 5 * T));
+  }
+  ph[i] = make_float4(hx, hy, hz, 0.f);
+  pl[i] = make_float4(lx, ly, lz, 0.f);
 }
 
 template <int MT, int MS, int PA>
@@ -1077,7 +1094,7 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
 #undef OD_CUTN3L
 #undef OD_CUTN3
   const size_t smem = sizeof(int32_t) * (L.nT + 8);
-  k_tile_reduce<<<L.nT, 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm, part_hi,
-                                        part_lo);
+  k_tile_reduce<<<dim3(L.nT, L.T / 256), 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm,
+                                                        part_hi, part_lo);
   return cudaGetLastError();
 }
