@@ -299,7 +299,7 @@ def run_ours(args, dist: Dist):
     n3 = not cutoff and plan["variant"] == 7
     traffic = load_traffic(N, plan, cutoff)
     if cutoff and plan["variant"] == 3:
-        kernel = (f"Morton sort + tile-pair list + k_pairs_cutn3 (each pair once, {plan['jsplit']}-ion "
+        kernel = (f"Hilbert-order sort + tile-pair list + k_pairs_cutn3 (each pair once, {plan['jsplit']}-ion "
                   "tiles, 64-ion group pairs beyond r_c skipped; pairs inside the cutoff credited)")
     elif cutoff:
         kernel = "cell-list build + k_pairs_cut (pairs inside the cutoff)"

@@ -847,7 +847,7 @@ static void free_cutn3(od_handle* h) {
   h->cut.n3 = nullptr;
 }
 
-// Cutoff variant 3: Morton-sorted tiles of T ions (ipt 4: 1024, ipt 2: 512) and the dense
+// Cutoff variant 3: Hilbert-sorted tiles of T ions (ipt 4: 1024, ipt 2: 512) and the dense
 // tile-pair matrix of partial sums (24 bytes per ion and tile).
 static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   free_cutn3(h);

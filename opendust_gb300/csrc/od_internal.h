@@ -97,12 +97,12 @@ struct od_cellgeom {
   float c, inv_c, lox, loy, loz;
 };
 // Device cell list of the cutoff path.
-// Cutoff over tile pairs (cutoff variant 3, od_n3.cu): ions sorted along a Morton curve of a
+// Cutoff over tile pairs (cutoff variant 3, od_n3.cu): ions sorted along a Hilbert curve of a
 // G^3 cell grid, tiles of T consecutive sorted ions, and every tile pair whose bounding boxes
 // come within the cutoff evaluated with each unordered pair once (64-ion group pairs farther
 // apart than the cutoff skipped).
 struct od_cutn3 {
-  int G, bits, ncells;              // cells per axis (power of two), Morton bits per axis
+  int G, bits, ncells;              // cells per axis (power of two), key bits per axis
   float lo, inv_s;                  // grid origin (every axis) and 1 / cell side (lambda)
   int T, ipt, nT, nslots, nwords;   // tile, targets per lane, tiles, nT*T slots, bitmap words
   int32_t *cell_of, *count, *fill, *start;  // [N], [ncells], [ncells], [ncells + 1]

@@ -1,5 +1,5 @@
 """GPU tests of the cutoff force path against the CPU oracle: variants 0 and 2 walk a stencil
-of cells per target cell; variant 3 (the default) sorts the ions along a Morton curve and
+of cells per target cell; variant 3 (the default) sorts the ions along a Hilbert curve and
 evaluates each unordered pair once over tile pairs whose bounding boxes come within r_c.
 
 Tolerances:
