@@ -1,0 +1,631 @@
+// od_cutn3.cu — ion–ion forces within a cutoff over tile pairs (cutoff variant 3): ions sorted
+// along a Hilbert curve of a cell grid, 512- or 1024-ion tiles of consecutive sorted ions, the tile
+// pairs whose bounding boxes come within the cutoff listed, each unordered pair inside the cutoff
+// evaluated once (od_n3_pair.cuh) with 64-ion group pairs beyond it skipped, and the tiles' rows of
+// partial sums added in a fixed order. Every result bit is independent of scheduling.
+#include "od_hilbert.h"
+#include "od_n3_pair.cuh"
+
+namespace {
+
+// ------------------------------------------------------------------ cutoff over tile pairs
+// Cell grid of G^3 cells over the cube [lo, lo + G/inv_s)^3; a cell's key is its index along
+// a Hilbert curve (od_hilbert.h), so that the ions sorted by key fill tiles and 64-ion groups
+// with compact bounding boxes: at 2^19 ions in the 3 x 6 lambda cylinder the group boxes keep
+// 1.73x the pairs inside a 2 lambda cutoff, against 1.94x in Morton order.
+__global__ void k_mc_clear(int ncells, int32_t* __restrict__ count, int32_t* __restrict__ fill) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncells) { count[c] = 0; fill[c] = 0; }
+}
+
+__global__ void k_mc_count(int n, const float4* __restrict__ pos, float lo, float inv_s, int G,
+                           int32_t* __restrict__ cell_of, int32_t* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  const int cx = min(max((int)floorf((p.x - lo) * inv_s), 0), G - 1);
+  const int cy = min(max((int)floorf((p.y - lo) * inv_s), 0), G - 1);
+  const int cz = min(max((int)floorf((p.z - lo) * inv_s), 0), G - 1);
+  const int c = (int)od_hilbert3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz, 31 - __clz(G));
+  cell_of[i] = c;
+  atomicAdd(&count[c], 1);
+}
+
+// exclusive scan of in[0..n) into out[0..n], out[n] = total (one 1024-thread block; in and out
+// may be the same array: every thread reads each of its entries before writing it)
+__global__ void __launch_bounds__(1024) k_scan_excl(int n, const int32_t* in, int32_t* out) {
+  __shared__ int s_w[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (n + 1023) / 1024;
+  const int c0 = min(tid * per, n), c1 = min(c0 + per, n);
+  int a = 0;
+  for (int c = c0; c < c1; c++) a += in[c];
+  int ia = a;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, ia, o);
+    if (lane >= o) ia += y;
+  }
+  if (lane == 31) s_w[wid] = ia;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = s_w[lane];
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    s_w[lane] = x - v;
+  }
+  __syncthreads();
+  int off = s_w[wid] + ia - a;
+  for (int c = c0; c < c1; c++) {
+    const int v = in[c];
+    out[c] = off;
+    off += v;
+  }
+  if (tid == 1023) out[n] = off;
+}
+
+__global__ void k_mc_scatter(int n, const int32_t* __restrict__ cell_of,
+                             const int32_t* __restrict__ start, int32_t* __restrict__ fill,
+                             int32_t* __restrict__ perm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = cell_of[i];
+  perm[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+// One block per cell: sort the cell's ions by index (bitonic in shared memory; the order of
+// the atomic scatter is not reproducible, the sorted order is) and write their positions.
+constexpr int kCellMax = 2048;
+__global__ void __launch_bounds__(128) k_mc_sort(const int32_t* __restrict__ count,
+                                                 const int32_t* __restrict__ start,
+                                                 const float4* __restrict__ pos,
+                                                 int32_t* __restrict__ perm, float* __restrict__ xs,
+                                                 float* __restrict__ ys, float* __restrict__ zs,
+                                                 uint32_t* __restrict__ err) {
+  __shared__ int32_t key[kCellMax];
+  const int c = blockIdx.x;
+  const int n0 = count[c];
+  if (n0 == 0) return;
+  if (n0 > kCellMax) {
+    if (threadIdx.x == 0) atomicOr(err, OD_DERR_CELL);
+    return;
+  }
+  const int s0 = start[c];
+  int m = 1;
+  while (m < n0) m <<= 1;
+  for (int k = threadIdx.x; k < m; k += 128) key[k] = k < n0 ? perm[s0 + k] : 0x7fffffff;
+  __syncthreads();
+  for (int size = 2; size <= m; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int k = threadIdx.x; k < m; k += 128) {
+        const int l = k ^ stride;
+        if (l > k) {
+          const bool up = (k & size) == 0;
+          const int a = key[k], b = key[l];
+          if ((a > b) == up) { key[k] = b; key[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  for (int k = threadIdx.x; k < n0; k += 128) {
+    const int i = key[k];
+    const float4 p = pos[i];
+    perm[s0 + k] = i;
+    xs[s0 + k] = p.x; ys[s0 + k] = p.y; zs[s0 + k] = p.z;
+  }
+}
+
+// bounding boxes of every 64-slot group of tile t (real ions only; a group without ions gets
+// an inverted box that is never within range) and of the tile itself
+__global__ void __launch_bounds__(256) k_tile_box(int n, int T, const float* __restrict__ xs,
+                                                  const float* __restrict__ ys,
+                                                  const float* __restrict__ zs,
+                                                  float* __restrict__ gbox, float* __restrict__ box) {
+  __shared__ float tb[8][6];
+  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float um[6] = {3e38f, 3e38f, 3e38f, -3e38f, -3e38f, -3e38f};  // this warp's union
+  for (int g = w; g < T / 64; g += 8) {
+    float mn[3] = {3e38f, 3e38f, 3e38f}, mx[3] = {-3e38f, -3e38f, -3e38f};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int i = t * T + g * 64 + h * 32 + lane;
+      if (i < n) {
+        const float v[3] = {xs[i], ys[i], zs[i]};
+#pragma unroll
+        for (int d = 0; d < 3; d++) { mn[d] = fminf(mn[d], v[d]); mx[d] = fmaxf(mx[d], v[d]); }
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+        mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+      }
+    if (lane < 6) gbox[((size_t)t * (T / 64) + g) * 6 + lane] = lane < 3 ? mn[lane] : mx[lane - 3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) { um[d] = fminf(um[d], mn[d]); um[3 + d] = fmaxf(um[3 + d], mx[d]); }
+  }
+  if (lane == 0)
+    for (int d = 0; d < 6; d++) tb[w][d] = um[d];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float v = tb[0][threadIdx.x];
+    for (int k = 1; k < 8; k++)
+      v = threadIdx.x < 3 ? fminf(v, tb[k][threadIdx.x]) : fmaxf(v, tb[k][threadIdx.x]);
+    box[t * 6 + threadIdx.x] = v;
+  }
+}
+
+// row a of the tile-pair bitmap: b >= a whose box comes within the cutoff (box distance in
+// FP32 with a relative margin of 1e-5, so that no pair inside r_c is dropped by rounding)
+__global__ void __launch_bounds__(128) k_tile_adj(int nT, int nwords, const float* __restrict__ box,
+                                                  float rc2m, uint32_t* __restrict__ adj,
+                                                  int32_t* __restrict__ rowcnt) {
+  __shared__ int s_cnt;
+  const int a = blockIdx.x;
+  uint32_t* row = adj + (size_t)a * nwords;
+  for (int w = threadIdx.x; w < nwords; w += 128) row[w] = 0u;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const float* A = box + a * 6;
+  int cnt = 0;
+  for (int b = a + threadIdx.x; b < nT; b += 128) {
+    const float* B = box + b * 6;
+    float d2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const float g = fmaxf(fmaxf(B[d] - A[3 + d], A[d] - B[3 + d]), 0.f);
+      d2 = fmaf(g, g, d2);
+    }
+    if (d2 < rc2m) { atomicOr(&row[b >> 5], 1u << (b & 31)); cnt++; }
+  }
+  atomicAdd(&s_cnt, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0) rowcnt[a] = s_cnt;
+}
+
+// listed pairs of row a in increasing b (one thread per row: at most nT bits)
+__global__ void k_tile_list(int nT, int nwords, const uint32_t* __restrict__ adj,
+                            const int32_t* __restrict__ rowptr, int2* __restrict__ pairs) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nT) return;
+  const uint32_t* row = adj + (size_t)a * nwords;
+  int k = rowptr[a];
+  for (int w = a >> 5; w < nwords; w++) {
+    uint32_t bits = row[w];
+    while (bits) {
+      const int j = __ffs(bits) - 1;
+      bits &= bits - 1;
+      pairs[k++] = make_int2(a, w * 32 + j);
+    }
+  }
+}
+
+// Balanced tile pair of the cutoff path: 512-ion tiles, NBT target groups of GT = 32·MT ions
+// and NBS source groups of GS = 32·MS ions per tile (MT targets and MS sources per lane). The
+// group pairs whose boxes come within the cutoff form a list in (target group, source group)
+// order, and warp w takes the contiguous slice [w·n/8, (w+1)·n/8) of it, so that the warps
+// evaluate the same number of group pairs (± 1) whatever the culling left and no barrier
+// separates them. A warp keeps one target group while consecutive items share it and sums its
+// targets into a segment slot of its own (a new segment at every change of target group and
+// at every slice start: at most NBT + 7); every item stores its FP32 reaction sums in a slot of
+// its own. The block then sums the slots of each ion in a fixed order — target segments in list
+// order, then reactions in target-group order — so the result does not depend on which warp
+// ran what, or when.
+template <int MT, int MS>
+struct cut_traits {
+  static constexpr int GT = 32 * MT, GS = 32 * MS;    // target and source group sizes
+  static constexpr int T = 512;                       // ions per tile
+  static constexpr int NBT = T / GT, NBS = T / GS;    // groups per tile
+  static constexpr int NI = NBT * NBS;                // group pairs per tile pair (<= 64)
+  static constexpr int NSEG = NBT + kWarps;           // target segments
+  static constexpr bool HS = MT > 2;                  // target sums kept in the segment slot
+  static constexpr size_t RFL = (size_t)NI * 3 * GS;  // reaction slots (floats)
+  static constexpr size_t TFL = (size_t)NSEG * 6 * GT;  // two-float target segment slots
+  static constexpr size_t SMEM = sizeof(float) * (RFL + TFL) + 256;  // + list metadata
+};
+
+// warp that owns list entry i of n
+__device__ __forceinline__ int cut_owner(int i, int n) {
+  int w = 0;
+  while (w < kWarps - 1 && (((w + 1) * n) >> 3) <= i) w++;
+  return w;
+}
+
+// group pair (ga, gb) of a diagonal tile: 2 each pair once, 1 directed (the sources lie in the
+// target group), 0 skipped (counted from the other side)
+template <int GT, int GS>
+__device__ __forceinline__ int cut_diag_mode(int ga, int gb) {
+  const int t0 = ga * GT, s0 = gb * GS;
+  return s0 >= t0 + GT ? 2 : (s0 >= t0 ? 1 : 0);
+}
+
+template <int MT, int MS, int CUT, bool COUNT>
+__device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ sx,
+                                                      const float* __restrict__ sy,
+                                                      const float* __restrict__ sz,
+                                                      float* __restrict__ outT,
+                                                      float* __restrict__ outR,
+                                                      const n3_consts& k, int a, int b, float* sm,
+                                                      const float* __restrict__ gbox,
+                                                      float cull2) {
+  using CT = cut_traits<MT, MS>;
+  constexpr int GT = CT::GT, GS = CT::GS, T = CT::T, NBT = CT::NBT, NBS = CT::NBS, NI = CT::NI;
+  constexpr int MS2 = MS / 2;
+  constexpr bool HS = CT::HS;
+  static_assert(NI % 32 == 0 && NI <= 64 && NBT <= 8, "list of at most 64 group pairs");
+  float* const R = sm;              // [NI][3][GS] reaction sums of each listed group pair
+  float* const Tg = sm + CT::RFL;   // [NSEG][6][GT] two-float target sums of each segment
+  unsigned char* const items = reinterpret_cast<unsigned char*>(Tg + CT::TFL);  // ga·NBS + gb
+  unsigned char* const segid = items + 64;                                       // per entry
+  signed char* const item_of = reinterpret_cast<signed char*>(items + 128);      // by ga·NBS+gb
+  signed char* const gs0 = item_of + 64;  // first and last segment of each target group
+  signed char* const gs1 = gs0 + 8;
+  int* const s_n = reinterpret_cast<int*>(items + 208);
+  const bool diag = a == b;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
+
+  // 1. the list (warp 0): group pairs within range; on a diagonal tile the source groups
+  // inside a target group (directed) and those above it
+  if (w == 0) {
+    int n = 0;
+    for (int r = 0; r < NI / 32; r++) {
+      const int c = r * 32 + lane, ga = c / NBS, gb = c % NBS;
+      const int mode = diag ? cut_diag_mode<GT, GS>(ga, gb) : 2;
+      bool keep = mode == 1;
+      if (mode == 2) {
+        float ta[6], tb[6];
+        group_box(gbox, (a * NBT + ga) * (GT / 64), GT / 64, ta);
+        group_box(gbox, (b * NBS + gb) * (GS / 64), GS / 64, tb);
+        float d2 = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float gap = fmaxf(fmaxf(tb[d] - ta[3 + d], ta[d] - tb[3 + d]), 0.f);
+          d2 = fmaf(gap, gap, d2);
+        }
+        keep = d2 < cull2;
+      }
+      const unsigned int bal = __ballot_sync(0xffffffffu, keep);
+      const int pos = n + __popc(bal & ((1u << lane) - 1u));
+      if (keep) items[pos] = (unsigned char)c;
+      item_of[c] = keep ? (signed char)pos : (signed char)-1;
+      n += __popc(bal);
+    }
+    __syncwarp();
+    // a segment starts at every change of target group and at the start of every slice
+    int nseg = 0;
+    for (int r = 0; r < 2; r++) {
+      const int i = r * 32 + lane;
+      bool f = false;
+      if (i < n)
+        f = i == 0 || items[i - 1] / NBS != items[i] / NBS ||
+            cut_owner(i - 1, n) != cut_owner(i, n);
+      const unsigned int bal = __ballot_sync(0xffffffffu, f);
+      if (i < n) segid[i] = (unsigned char)(nseg + __popc(bal & ((2u << lane) - 1u)) - 1);
+      nseg += __popc(bal);
+    }
+    if (lane < 8) { gs0[lane] = 0; gs1[lane] = -1; }
+    __syncwarp();
+    for (int r = 0; r < 2; r++) {
+      const int i = r * 32 + lane;
+      if (i < n) {
+        const int ga = items[i] / NBS;
+        if (i == 0 || items[i - 1] / NBS != ga) gs0[ga] = (signed char)segid[i];
+        if (i == n - 1 || items[i + 1] / NBS != ga) gs1[ga] = (signed char)segid[i];
+      }
+    }
+    if (lane == 0) *s_n = n;
+  }
+  __syncthreads();
+
+  // 2. this warp's slice of the list
+  const int n = *s_n, i0 = (w * n) >> 3, i1 = ((w + 1) * n) >> 3;
+  unsigned int cnt = 0;
+  od_u64 X[MT], Y[MT], Z[MT];
+  float hreg[HS ? 1 : 6 * MT];
+  float* hs = Tg + lane;  // HS: this warp's current segment slot (lane-private words)
+#define CUT_H(c, kt) (HS ? hs[(c) * GT + 32 * (kt)] : hreg[(c) * MT + (kt)])
+  int cur = -1;
+  for (int i = i0; i < i1; i++) {
+    const int c = items[i], ga = c / NBS, gb = c % NBS;
+    if (ga != cur) {
+      if (!HS && cur >= 0) {
+        float* t = Tg + (size_t)segid[i - 1] * 6 * GT + lane;
+#pragma unroll
+        for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
+      }
+      if (HS) hs = Tg + (size_t)segid[i] * 6 * GT + lane;
+#pragma unroll
+      for (int kt = 0; kt < MT; kt++) {
+        const int j = (a * NBT + ga) * GT + lane + 32 * kt;
+        const float x = sx[j], y = sy[j], z = sz[j];
+        X[kt] = p2(x, x); Y[kt] = p2(y, y); Z[kt] = p2(z, z);
+#pragma unroll
+        for (int q = 0; q < 6; q++) CUT_H(q, kt) = 0.f;
+      }
+      cur = ga;
+    }
+    od_u64 QX[MS2], QY[MS2], QZ[MS2], RX[MS2], RY[MS2], RZ[MS2], AX[MT], AY[MT], AZ[MT];
+#pragma unroll
+    for (int q = 0; q < MS2; q++) {
+      const int j = (b * NBS + gb) * GS + lane + 64 * q;
+      QX[q] = p2(sx[j], sx[j + 32]);
+      QY[q] = p2(sy[j], sy[j + 32]);
+      QZ[q] = p2(sz[j], sz[j + 32]);
+      RX[q] = RY[q] = RZ[q] = 0ull;
+    }
+#pragma unroll
+    for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
+    if (diag && cut_diag_mode<GT, GS>(ga, gb) == 1) {
+      n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                          cnt);
+    } else {
+      n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                         cnt);
+      // the force on the sources is minus the accumulated terms
+      float* r = R + (size_t)i * 3 * GS + lane;
+#pragma unroll
+      for (int q = 0; q < MS2; q++) {
+        const float2 rx = up2(RX[q]), ry = up2(RY[q]), rz = up2(RZ[q]);
+        r[64 * q] = -rx.x; r[64 * q + 32] = -rx.y;
+        r[GS + 64 * q] = -ry.x; r[GS + 64 * q + 32] = -ry.y;
+        r[2 * GS + 64 * q] = -rz.x; r[2 * GS + 64 * q + 32] = -rz.y;
+      }
+    }
+#pragma unroll
+    for (int kt = 0; kt < MT; kt++) {
+      od_acc2(CUT_H(0, kt), CUT_H(3, kt), sum2(AX[kt]));
+      od_acc2(CUT_H(1, kt), CUT_H(4, kt), sum2(AY[kt]));
+      od_acc2(CUT_H(2, kt), CUT_H(5, kt), sum2(AZ[kt]));
+    }
+  }
+  if (!HS && cur >= 0) {
+    float* t = Tg + (size_t)segid[i1 - 1] * 6 * GT + lane;
+#pragma unroll
+    for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
+  }
+#undef CUT_H
+  __syncthreads();
+
+  // 3. fixed-order sums of the slots; every ion of both tiles is written (zeros when no group
+  // pair reached it)
+  for (int e = tid; e < T; e += kWarps * 32) {
+    const int g = e / GT, l = e % GT;
+    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+    for (int s = gs0[g]; s <= gs1[g]; s++) {
+      const float* t = Tg + (size_t)s * 6 * GT + l;
+      acc2x2(hx, lx, t[0], t[3 * GT]);
+      acc2x2(hy, ly, t[GT], t[4 * GT]);
+      acc2x2(hz, lz, t[2 * GT], t[5 * GT]);
+    }
+    if (!diag) {
+      outT[e] = hx; outT[T + e] = hy; outT[2 * T + e] = hz;
+      outT[3 * T + e] = lx; outT[4 * T + e] = ly; outT[5 * T + e] = lz;
+      hx = hy = hz = lx = ly = lz = 0.f;
+    }
+    const int gb = e / GS, l2 = e % GS;
+    for (int ga = 0; ga < NBT; ga++) {
+      const int it = item_of[ga * NBS + gb];
+      if (it < 0 || (diag && cut_diag_mode<GT, GS>(ga, gb) == 1)) continue;
+      const float* r = R + (size_t)it * 3 * GS + l2;
+      od_acc2(hx, lx, r[0]);
+      od_acc2(hy, ly, r[GS]);
+      od_acc2(hz, lz, r[2 * GS]);
+    }
+    outR[e] = hx; outR[T + e] = hy; outR[2 * T + e] = hz;
+    outR[3 * T + e] = lx; outR[4 * T + e] = ly; outR[5 * T + e] = lz;
+  }
+  __syncthreads();  // the next tile pair rewrites the list and the slots
+  return cnt;
+}
+
+// ions per tile of the staggered tile pair, or of the balanced list (BAL)
+template <bool BAL, int MT, int MS, int PA>
+struct cutn3_tile {
+  static constexpr int T = n3_traits<MT, MS, PA>::T;
+};
+template <int MT, int MS, int PA>
+struct cutn3_tile<true, MT, MS, PA> {
+  static constexpr int T = cut_traits<MT, MS>::T;
+};
+
+// every listed tile pair, each unordered ion pair once (static assignment: pair k to block
+// k mod grid), group pairs beyond the cutoff skipped. BAL: the balanced list routine above
+// (512-ion tiles); otherwise the staggered tile-pair routine.
+template <int MT, int MS, int PA, int CUT, bool COUNT, bool BAL>
+__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
+    k_pairs_cutn3(const float* __restrict__ xs, const float* __restrict__ ys,
+                  const float* __restrict__ zs, int nslots, int nT,
+                  const int2* __restrict__ pairs, const int32_t* __restrict__ npairs,
+                  float* __restrict__ S, n3_cut cut, const float* __restrict__ gbox, float cull2,
+                  unsigned long long* __restrict__ pair_count) {
+  extern __shared__ float sm[];
+  constexpr size_t T6 = 6 * (size_t)cutn3_tile<BAL, MT, MS, PA>::T;
+  static_assert(!BAL || PA == 1, "balanced list: one pass");
+  const int np = *npairs;
+  unsigned int cnt = 0;
+  if constexpr (BAL) {
+    const n3_consts kc = make_consts(cut);
+    for (int k = blockIdx.x; k < np; k += gridDim.x) {
+      const int2 ab = pairs[k];
+      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, S + ((size_t)ab.x * nT + ab.y) * T6,
+                                               S + ((size_t)ab.y * nT + ab.x) * T6, kc, ab.x,
+                                               ab.y, sm, gbox, cull2);
+    }
+  } else {
+    for (int k = blockIdx.x; k < np; k += gridDim.x) {
+      const int2 ab = pairs[k];
+      cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots,
+                                                        S + ((size_t)ab.x * nT + ab.y) * T6,
+                                                        S + ((size_t)ab.y * nT + ab.x) * T6, cut,
+                                                        ab.x, ab.y, sm, gbox, cull2);
+    }
+  }
+  if (COUNT) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(pair_count, (unsigned long long)cnt);
+  }
+}
+
+// Row sums over the tiles that share a listed pair with tile t, in increasing tile order,
+// written to the ions' entries of (ph, pl). Block (t, c) sums ions c·256 .. c·256+255 of tile t,
+// one ion per thread; the matrix rows are read once (streaming loads, four neighbours in flight
+// per thread), so the kernel runs at the HBM rate.
+__global__ void __launch_bounds__(256) k_tile_reduce(int nT, int nwords, int T,
+                                                     const uint32_t* __restrict__ adj,
+                                                     const float* __restrict__ S,
+                                                     const int32_t* __restrict__ perm,
+                                                     float4* __restrict__ ph,
+                                                     float4* __restrict__ pl) {
+  extern __shared__ int32_t nb[];  // [nT] neighbour tiles, then [8] warp counts
+  int32_t* wcnt = nb + nT;
+  __shared__ int s_m;
+  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_m = 0;
+  __syncthreads();
+  // ordered compaction of {y : pair (min(t, y), max(t, y)) listed}, 256 candidates per round
+  for (int y0 = 0; y0 < nT; y0 += 256) {
+    const int y = y0 + threadIdx.x;
+    bool f = false;
+    if (y < nT)
+      f = y < t ? (adj[(size_t)y * nwords + (t >> 5)] >> (t & 31)) & 1u
+                : (adj[(size_t)t * nwords + (y >> 5)] >> (y & 31)) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, f);
+    if (lane == 0) wcnt[w] = __popc(bal);
+    __syncthreads();
+    int base = s_m;
+    for (int k = 0; k < w; k++) base += wcnt[k];
+    if (f) nb[base + __popc(bal & ((1u << lane) - 1u))] = y;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int k = 0; k < 8; k++) tot += wcnt[k];
+      s_m += tot;
+    }
+    __syncthreads();
+  }
+  const int m = s_m;
+  const int e = blockIdx.y * 256 + threadIdx.x;
+  const int i = perm[t * T + e];
+  if (i < 0) return;  // sentinel slot (no barrier follows)
+  const float* row = S + (size_t)t * nT * 6 * (size_t)T + e;
+  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+  int q = 0;
+  for (; q + 4 <= m; q += 4) {
+    float v[4][6];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const float* r = row + (size_t)nb[q + u] * 6 * T;
+#pragma unroll
+      for (int c = 0; c < 6; c++) v[u][c] = __ldcs(r + c * T);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      acc2x2(hx, lx, v[u][0], v[u][3]);
+      acc2x2(hy, ly, v[u][1], v[u][4]);
+      acc2x2(hz, lz, v[u][2], v[u][5]);
+    }
+  }
+  for (; q < m; q++) {
+    const float* r = row + (size_t)nb[q] * 6 * T;
+    acc2x2(hx, lx, __ldcs(r), __ldcs(r + 3 * T));
+    acc2x2(hy, ly, __ldcs(r + T), __ldcs(r + 4 * T));
+    acc2x2(hz, lz, __ldcs(r + 2 * T), __ldcs(r + 5 * T));
+  }
+  ph[i] = make_float4(hx, hy, hz, 0.f);
+  pl[i] = make_float4(lx, ly, lz, 0.f);
+}
+
+}  // namespace
+
+int od_cutn3_grid(int N) {
+  // about 16 ions per cell: G the smallest power of two with G^3 >= N / 22, 8 <= G <= 128
+  int G = 8;
+  while (G < 128 && (double)G * G * G * 8.0 * 16.0 < (double)N * 1.4142) G <<= 1;
+  return G;
+}
+
+size_t od_cutn3_bytes(int N, int T, int G) {
+  const size_t nT = (size_t)((N + T - 1) / T), ns = nT * T, nc = (size_t)G * G * G;
+  const size_t nw = (nT + 31) / 32;
+  return sizeof(float) * nT * nT * 6 * T                      // S
+         + sizeof(int2) * nT * (nT + 1) / 2                   // pairs
+         + sizeof(uint32_t) * nT * nw                         // bitmap
+         + sizeof(float) * (3 * ns + 6 * nT + 6 * (ns / 64))  // sorted positions, boxes
+         + sizeof(int32_t) * (ns + N + 3 * nc + nT + 4);
+}
+
+// cutoff tile-pair shapes: (ipt, T) = (2, 512) the balanced list with 2 x 2 targets x sources
+// per lane, (4, 1024) the staggered tile pair with 4 x 4. Measured on GB300 at 2^19 ions
+// (field_chain): 45.2 ms per step with (2, 512), 48.1 with the balanced list at 4 x 2 (128-ion
+// target groups: more arithmetic per shuffle, but coarser culling), 55.7 with (4, 1024).
+template <int MT, int MS, bool BAL>
+cudaError_t prepare_cutn3(int smem) {
+  void* fn[4] = {(void*)k_pairs_cutn3<MT, MS, 1, 1, false, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 1, true, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 2, false, BAL>,
+                 (void*)k_pairs_cutn3<MT, MS, 1, 2, true, BAL>};
+  for (int q = 0; q < 4; q++) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(fn[q], cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+bool od_cutn3_supported(int ipt, int T) {
+  return (ipt == 2 && T == 512) || (ipt == 4 && T == 1024);
+}
+
+cudaError_t od_cutn3_prepare(int ipt, int T) {
+  if (ipt == 2 && T == 512) return prepare_cutn3<2, 2, true>((int)cut_traits<2, 2>::SMEM);
+  if (ipt == 4 && T == 1024)
+    return prepare_cutn3<4, 4, false>((int)n3_traits<4, 4, 1>::SMEM);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
+                                float4* part_lo, float rho0, float rc, float rs, uint32_t* err,
+                                unsigned long long* pair_count, cudaStream_t s) {
+  k_mc_clear<<<(L.ncells + 255) / 256, 256, 0, s>>>(L.ncells, L.count, L.fill);
+  k_mc_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, L.lo, L.inv_s, L.G, L.cell_of, L.count);
+  k_scan_excl<<<1, 1024, 0, s>>>(L.ncells, L.count, L.start);
+  k_mc_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, L.cell_of, L.start, L.fill, L.perm);
+  k_mc_sort<<<L.ncells, 128, 0, s>>>(L.count, L.start, pos, L.perm, L.xs, L.ys, L.zs, err);
+  k_tile_box<<<L.nT, 256, 0, s>>>(n, L.T, L.xs, L.ys, L.zs, L.gbox, L.box);
+  const float rc2m = rc * rc * 1.00001f;
+  k_tile_adj<<<L.nT, 128, 0, s>>>(L.nT, L.nwords, L.box, rc2m, L.adj, L.rowptr);
+  k_scan_excl<<<1, 1024, 0, s>>>(L.nT, L.rowptr, L.rowptr);
+  k_tile_list<<<(L.nT + 127) / 128, 128, 0, s>>>(L.nT, L.nwords, L.adj, L.rowptr, L.pairs);
+  const bool sw = rs < rc;
+  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f};
+  const int32_t* np = L.rowptr + L.nT;
+#define OD_CUTN3(MT, MS, BAL, SM)                                                             \
+  do {                                                                                        \
+    if (sw) {                                                                                 \
+      if (pair_count) OD_CUTN3L(MT, MS, 1, true, BAL, SM);                                    \
+      else OD_CUTN3L(MT, MS, 1, false, BAL, SM);                                              \
+    } else {                                                                                  \
+      if (pair_count) OD_CUTN3L(MT, MS, 2, true, BAL, SM);                                    \
+      else OD_CUTN3L(MT, MS, 2, false, BAL, SM);                                              \
+    }                                                                                         \
+  } while (0)
+#define OD_CUTN3L(MT, MS, CUT, CNT, BAL, SM)                                                  \
+  k_pairs_cutn3<MT, MS, 1, CUT, CNT, BAL><<<L.grid, kWarps * 32, SM, s>>>(                    \
+      L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.S, cut, L.gbox, rc2m, pair_count)
+  if (L.ipt == 2 && L.T == 512) OD_CUTN3(2, 2, true, (cut_traits<2, 2>::SMEM));
+  else if (L.ipt == 4 && L.T == 1024) OD_CUTN3(4, 4, false, (n3_traits<4, 4, 1>::SMEM));
+  else return cudaErrorInvalidValue;
+#undef OD_CUTN3L
+#undef OD_CUTN3
+  const size_t smem = sizeof(int32_t) * (L.nT + 8);
+  k_tile_reduce<<<dim3(L.nT, L.T / 256), 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm,
+                                                        part_hi, part_lo);
+  return cudaGetLastError();
+}

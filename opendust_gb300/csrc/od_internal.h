@@ -97,7 +97,7 @@ struct od_cellgeom {
   float c, inv_c, lox, loy, loz;
 };
 // Device cell list of the cutoff path.
-// Cutoff over tile pairs (cutoff variant 3, od_n3.cu): ions sorted along a Hilbert curve of a
+// Cutoff over tile pairs (cutoff variant 3, od_cutn3.cu): ions sorted along a Hilbert curve of a
 // G^3 cell grid, tiles of T consecutive sorted ions, and every tile pair whose bounding boxes
 // come within the cutoff evaluated with each unordered pair once (64-ion group pairs farther
 // apart than the cutoff skipped).
