@@ -128,3 +128,18 @@ def test_cutoff_time_averages(gpu_lib):
     print(f"cutoff time averages (5 grains): q rel {dq:.3e}, orbit rel {do:.3e}")
     assert dq < 0.01
     assert do < 0.01
+
+
+@pytest.mark.parametrize("N", [200, 3000, 70001])
+def test_cutoff_ragged_sizes(gpu_lib, N):
+    # ion counts that leave the last 512-ion tile partly empty (sentinel slots), a single tile,
+    # and an odd count with many tiles: the default kernel against the oracle, switching on
+    holder, pos, vel, plasma, sim, grains = case(N=N, n=4, seed=26, builder=workloads.field_chain)
+    with _lib.Engine(holder) as eng:
+        assert eng.pair_plan()["variant"] == 3
+        f = eng.force_snapshot(pos)
+    idx = np.arange(N) if N <= 4096 else np.sort(np.random.default_rng(1).choice(N, 2048, replace=False))
+    ref = oracle.force_targets(holder, pos, idx, round32=True)
+    err = rel_err_per_ion(f[idx], ref)
+    print(f"cutoff N={N}: per-ion rel err max {err.max():.3e}")
+    assert err.max() <= 1e-5
