@@ -354,6 +354,20 @@ od_status od_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_b
  * do not allocate it) (admission control). */
 od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes);
 
+/* Trajectory dumps of OpenDust.simulate() (opendust.py:1071-1098, which writes them with a Python
+ * loop per ion). Host only, no device work. Positions are n x 3 doubles in nm. Numbers are
+ * written as Python's "{}".format writes a float (shortest round-trip digits; fixed notation for
+ * decimal exponents -4..15, else d.ddde+XX), so the files are byte-identical to the reference's.
+ * od_write_xyz_frame appends "n\nframe\n" and one "Ar\tx\ty\tz\n" line per ion to path;
+ * od_write_csv_frame writes the file path with the header "x,y,z,density,mass" and one row per
+ * ion, "\r\n" line ends as Python's csv.writer. Failures to open or write return OD_ERR_INVALID
+ * (od_last_error(NULL) names the file). od_format_double writes one number (at most 32 chars
+ * and a terminating NUL) and returns its length. */
+od_status od_write_xyz_frame(const char* path, const double* xyz_nm, int64_t n, int64_t frame);
+od_status od_write_csv_frame(const char* path, const double* xyz_nm, int64_t n, double density,
+                             double mass);
+int32_t od_format_double(double v, char* buf);
+
 /* Ion–ion forces for callers that cannot allocate device memory (no counterpart in the
  * reference). Plug-ins that live inside another runtime's allocator, loops that forbid
  * cudaMalloc after start-up, or frameworks that own every device buffer can still evaluate

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libopendust_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["od_api.cu", "od_kernels.cu", "od_cutoff.cu", "od_n3.cu", "od_cutn3.cu"]
+SOURCES = ["od_api.cu", "od_kernels.cu", "od_cutoff.cu", "od_n3.cu", "od_cutn3.cu", "od_io.cu"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17",

@@ -176,6 +176,9 @@ def load(path: str | None = None):
             c_int32,
             [c_double, c_double, c_int32, c_int32, c_int64, c_uint64, c_int32, _DP],
         ),
+        "od_write_xyz_frame": (c_int32, [c_char_p, _DP, c_int64, c_int64]),
+        "od_write_csv_frame": (c_int32, [c_char_p, _DP, c_int64, c_double, c_double]),
+        "od_format_double": (c_int32, [c_double, c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -576,6 +579,35 @@ def batch_pair_plan(n_ions: int) -> tuple:
     a = (c_int32 * 5)()
     check(load().od_batch_pair_plan(int(n_ions), a), None)
     return tuple(a[:4])
+
+
+def _xyz_nm(pos_nm) -> np.ndarray:
+    a = np.ascontiguousarray(pos_nm, dtype=np.float64)
+    if a.ndim != 2 or a.shape[1] != 3:
+        raise ValueError("positions must be an (n, 3) array")
+    return a
+
+
+def write_xyz_frame(path: str, pos_nm, frame: int):
+    """Append one XYZ frame ("n", "frame", then "Ar\tx\ty\tz" per ion, nm) as the reference's
+    simulate() writes it (opendust.py:1079-1084), byte for byte."""
+    a = _xyz_nm(pos_nm)
+    check(load().od_write_xyz_frame(os.fsencode(path), _dptr(a), a.shape[0], int(frame)))
+
+
+def write_csv_frame(path: str, pos_nm, density: float, mass: float):
+    """Write one CSV frame ("x,y,z,density,mass" rows, nm) as the reference's simulate() writes
+    it with csv.writer (opendust.py:1086-1097), byte for byte."""
+    a = _xyz_nm(pos_nm)
+    check(load().od_write_csv_frame(os.fsencode(path), _dptr(a), a.shape[0], float(density),
+                                    float(mass)))
+
+
+def format_double(v: float) -> str:
+    """The library's formatting of one double (Python's repr of a float)."""
+    buf = ctypes.create_string_buffer(40)
+    n = load().od_format_double(float(v), buf)
+    return buf.raw[:n].decode()
 
 
 def fp32_peak_tflops(device: int = 0) -> float:

@@ -56,6 +56,7 @@ static od_status fail(od_handle* h, od_status st, const std::string& msg) {
   if (h) h->err = msg; else g_err = msg;
   return st;
 }
+od_status od_fail_nohandle(od_status st, const std::string& msg) { return fail(nullptr, st, msg); }
 static od_status cuda_fail(od_handle* h, cudaError_t e, const char* what) {
   std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
   return fail(h, e == cudaErrorMemoryAllocation ? OD_ERR_OOM : OD_ERR_CUDA, m);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <string>
 #include "od_common.cuh"
 
 // Work decomposition of the all-pairs force kernel.
@@ -183,3 +185,7 @@ cudaError_t od_launch_set_charges(const od_dparams* dp, od_dstate* ds, float* cq
                                   cudaStream_t s);
 cudaError_t od_launch_trap(double Rh, double Hh, int n_r, int n_h, int64_t n_points, uint64_t seed,
                            double* part, int nchunks, cudaStream_t s);
+
+// Record msg as the last error of calls without a handle (od_last_error(NULL)); returns st.
+od_status od_fail_nohandle(od_status st, const std::string& msg);
+

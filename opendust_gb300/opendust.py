@@ -13,8 +13,9 @@ and ``t`` exactly as the reference does and also returns ``(q, forces)``.
 """
 from __future__ import annotations
 
-import csv
+import queue
 import re
+import threading
 
 import numpy as np
 
@@ -352,34 +353,69 @@ class OpenDust:
         if want_files:
             marks |= set(range(0, n, nFileOutput))
         marks.add(n - 1)
+        writer = _FrameWriter(self, out, plasma) if want_files else None
         done = 0
-        for i in sorted(marks):
-            eng.step(i + 1 - done)
-            done = i + 1
-            if i % nOutput == 0 and not quiet:
-                if i == 0:
-                    print("#########################################")
-                    print("###        Start simulation           ###")
-                    print("#########################################")
-                    print("\n")
-                print("Step: {} out of {}".format(i, n))
-            if want_files and i % nFileOutput == 0:
-                pos, _ = eng.get_state()
-                self._write_frames(out, plasma, pos * 1e9, i // nFileOutput)
+        try:
+            for i in sorted(marks):
+                eng.step(i + 1 - done)
+                done = i + 1
+                if i % nOutput == 0 and not quiet:
+                    if i == 0:
+                        print("#########################################")
+                        print("###        Start simulation           ###")
+                        print("#########################################")
+                        print("\n")
+                    print("Step: {} out of {}".format(i, n))
+                if writer is not None and i % nFileOutput == 0:
+                    pos, _ = eng.get_state()
+                    writer.put(pos * 1e9, i // nFileOutput)
+        finally:
+            if writer is not None:
+                writer.close()
         if out.restartFileName:
             pos, vel = eng.get_state()
             sh.write_restart(out.restartFileName, pos, vel)
 
     def _write_frames(self, out, plasma, pos_nm, frame):
-        """XYZ and CSV dumps in nm (opendust.py:1072-1098)."""
+        """XYZ and CSV dumps in nm (opendust.py:1072-1098), written by the library's formatter:
+        the same bytes as the reference's Python loops."""
         if out.xyzOutputFileName:
-            with open(out.xyzOutputFileName, "a") as f:
-                f.write("{}\n{}\n".format(self.N, frame))
-                for x, y, z in pos_nm:
-                    f.write("Ar\t{}\t{}\t{}\n".format(x, y, z))
+            _lib.write_xyz_frame(out.xyzOutputFileName, pos_nm, frame)
         if out.csvOutputFileName:
-            with open(out.csvOutputFileName + "{}.csv".format(frame), "w") as f:
-                w = csv.writer(f)
-                w.writerow(["x", "y", "z", "density", "mass"])
-                for x, y, z in pos_nm:
-                    w.writerow([x, y, z, plasma.n_inf * 1e-27, self.N_s])
+            _lib.write_csv_frame(out.csvOutputFileName + "{}.csv".format(frame), pos_nm,
+                                 plasma.n_inf * 1e-27, self.N_s)
+
+
+class _FrameWriter:
+    """Writes the XYZ/CSV frames of one simulate() call on a background thread, in order, while
+    the GPU steps on (the library's writer releases the GIL). At most two frames wait in memory;
+    an error in a write is raised by the next put() or by close()."""
+
+    def __init__(self, od, out, plasma):
+        self._od, self._out, self._plasma = od, out, plasma
+        self._q = queue.Queue(maxsize=2)
+        self._err = None
+        self._t = threading.Thread(target=self._run, name="opendust-frames", daemon=True)
+        self._t.start()
+
+    def _run(self):
+        while True:
+            item = self._q.get()
+            if item is None:
+                return
+            if self._err is None:
+                try:
+                    self._od._write_frames(self._out, self._plasma, *item)
+                except BaseException as e:  # noqa: BLE001 - re-raised on the caller's thread
+                    self._err = e
+
+    def put(self, pos_nm, frame):
+        if self._err is not None:
+            raise self._err
+        self._q.put((pos_nm, frame))
+
+    def close(self):
+        self._q.put(None)
+        self._t.join()
+        if self._err is not None:
+            raise self._err
