@@ -367,6 +367,13 @@ od_status od_write_xyz_frame(const char* path, const double* xyz_nm, int64_t n, 
 od_status od_write_csv_frame(const char* path, const double* xyz_nm, int64_t n, double density,
                              double mass);
 int32_t od_format_double(double v, char* buf);
+/* The restart file of OpenDust.simulate() (opendust.py:1099-1115; read at :452-466): one ion per
+ * line, "x\ty\tz\tvx\tvy\tvz\n" in nm and nm/ps, numbers formatted as above. od_read_restart
+ * reads the first n lines (strtod, as Python's float()); a file with fewer lines or fields
+ * returns OD_ERR_INVALID. */
+od_status od_write_restart(const char* path, const double* pos_nm, const double* vel_nmps,
+                           int64_t n);
+od_status od_read_restart(const char* path, int64_t n, double* pos_nm, double* vel_nmps);
 
 /* Ion–ion forces for callers that cannot allocate device memory (no counterpart in the
  * reference). Plug-ins that live inside another runtime's allocator, loops that forbid

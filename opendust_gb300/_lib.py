@@ -179,6 +179,8 @@ def load(path: str | None = None):
         "od_write_xyz_frame": (c_int32, [c_char_p, _DP, c_int64, c_int64]),
         "od_write_csv_frame": (c_int32, [c_char_p, _DP, c_int64, c_double, c_double]),
         "od_format_double": (c_int32, [c_double, c_char_p]),
+        "od_write_restart": (c_int32, [c_char_p, _DP, _DP, c_int64]),
+        "od_read_restart": (c_int32, [c_char_p, c_int64, _DP, _DP]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -601,6 +603,23 @@ def write_csv_frame(path: str, pos_nm, density: float, mass: float):
     a = _xyz_nm(pos_nm)
     check(load().od_write_csv_frame(os.fsencode(path), _dptr(a), a.shape[0], float(density),
                                     float(mass)))
+
+
+def write_restart_file(path: str, pos_nm, vel_nmps):
+    """The reference's restart file (opendust.py:1099-1115): "x\ty\tz\tvx\tvy\tvz" per ion in
+    nm and nm/ps, byte for byte."""
+    p, v = _xyz_nm(pos_nm), _xyz_nm(vel_nmps)
+    if p.shape != v.shape:
+        raise ValueError("positions and velocities differ in shape")
+    check(load().od_write_restart(os.fsencode(path), _dptr(p), _dptr(v), p.shape[0]))
+
+
+def read_restart_file(path: str, n: int):
+    """The first n ions of a restart file: (positions nm, velocities nm/ps), each (n, 3)."""
+    p = np.empty((n, 3))
+    v = np.empty((n, 3))
+    check(load().od_read_restart(os.fsencode(path), int(n), _dptr(p), _dptr(v)))
+    return p, v
 
 
 def format_double(v: float) -> str:

@@ -1,5 +1,6 @@
 // od_io.cu — trajectory dumps of OpenDust.simulate() (opendust.py:1071-1098): one XYZ frame
-// appended per call, or one CSV file per frame. Host code only. The reference formats every
+// appended per call, or one CSV file per frame; and the restart file (opendust.py:1099-1115,
+// read back at :452-466). Host code only. The reference formats every
 // coordinate with Python's "{}".format (the shortest decimal string that reads back to the same
 // double, in fixed notation for decimal exponents -4 .. 15 and scientific notation outside);
 // the same text is produced here from std::to_chars, formatted in parallel host threads, so that
@@ -9,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -178,5 +180,61 @@ extern "C" od_status od_write_csv_frame(const char* path, const double* xyz_nm, 
   });
   if ((n > 0 && body.empty()) || !write_all(path, "wb", "x,y,z,density,mass\r\n", body))
     return od_fail_nohandle(OD_ERR_INVALID, std::string("cannot write ") + path);
+  return OD_OK;
+}
+
+extern "C" od_status od_write_restart(const char* path, const double* pos_nm,
+                                      const double* vel_nmps, int64_t n) {
+  if (!path || (n > 0 && (!pos_nm || !vel_nmps)) || n < 0)
+    return od_fail_nohandle(OD_ERR_INVALID, "od_write_restart: NULL path or arrays");
+  const auto body = format_lines(n, 128, [pos_nm, vel_nmps](int64_t i0, int64_t i1,
+                                                             std::string& s) {
+    for (int64_t i = i0; i < i1; i++) {
+      for (int c = 0; c < 3; c++) {
+        append_repr(s, pos_nm[3 * i + c]);
+        s += '\t';
+      }
+      for (int c = 0; c < 3; c++) {
+        append_repr(s, vel_nmps[3 * i + c]);
+        s += c < 2 ? '\t' : '\n';
+      }
+    }
+  });
+  if ((n > 0 && body.empty()) || !write_all(path, "wb", std::string(), body))
+    return od_fail_nohandle(OD_ERR_INVALID, std::string("cannot write ") + path);
+  return OD_OK;
+}
+
+extern "C" od_status od_read_restart(const char* path, int64_t n, double* pos_nm,
+                                     double* vel_nmps) {
+  if (!path || (n > 0 && (!pos_nm || !vel_nmps)) || n < 0)
+    return od_fail_nohandle(OD_ERR_INVALID, "od_read_restart: NULL path or arrays");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return od_fail_nohandle(OD_ERR_INVALID, std::string("cannot open ") + path);
+  std::string buf;
+  char chunk[1 << 16];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, got);
+  std::fclose(f);
+  // the first n lines, six tab-separated numbers each (the reference's float() per field)
+  const char* p = buf.c_str();
+  const char* end = p + buf.size();
+  for (int64_t i = 0; i < n; i++) {
+    for (int c = 0; c < 6; c++) {
+      char* q = nullptr;
+      const double v = std::strtod(p, &q);
+      if (q == p)
+        return od_fail_nohandle(OD_ERR_INVALID, std::string(path) + ": line " +
+                                                    std::to_string(i + 1) + " holds fewer than 6 numbers"
+                                                    " (or the file fewer lines than ions)");
+      (c < 3 ? pos_nm[3 * i + c] : vel_nmps[3 * i + c - 3]) = v;
+      p = q;
+      if (c < 5) {
+        if (p < end && *p == '\t') p++;
+      }
+    }
+    while (p < end && *p != '\n') p++;  // rest of the line
+    if (p < end) p++;
+  }
   return OD_OK;
 }

@@ -217,17 +217,18 @@ def initial_state(N: int, R: float, H: float, grains: list, v_fl: float, v_T: fl
 def read_restart(path: str, N: int):
     """Restart file: one ion per line, ``x y z vx vy vz`` tab-separated in nm and nm/ps
     (opendust.py:452-466, :1100-1115). Returns SI arrays."""
-    data = np.loadtxt(path, delimiter="\t", max_rows=N, ndmin=2)
-    if data.shape[0] < N:
-        raise ValueError(f"restart file {path} holds {data.shape[0]} ions, {N} needed")
-    return data[:, :3] * 1e-9, data[:, 3:6] * NMPS
+    from . import _lib
+    try:
+        p, v = _lib.read_restart_file(path, N)
+    except _lib.OpenDustError as e:
+        raise ValueError(str(e)) from None
+    return p * 1e-9, v * NMPS
 
 
 def write_restart(path: str, pos: np.ndarray, vel: np.ndarray):
-    """Same format as read_restart."""
-    with open(path, "w") as f:
-        for p, v in zip(pos * 1e9, vel / NMPS):
-            f.write("{}\t{}\t{}\t{}\t{}\t{}\n".format(p[0], p[1], p[2], v[0], v[1], v[2]))
+    """Same format as read_restart, the reference's bytes (numbers as Python's "{}".format)."""
+    from . import _lib
+    _lib.write_restart_file(path, np.asarray(pos) * 1e9, np.asarray(vel) / NMPS)
 
 
 # ----------------------------------------------------------------- chains/matthews.py fork

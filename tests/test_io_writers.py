@@ -96,3 +96,23 @@ def test_frame_writer_keeps_order_and_reports_errors():
         w.close()
     assert not w._t.is_alive()
     assert [f for f, _ in rec.frames] == [0, 1, 2]
+
+
+def test_restart_file_byte_identical_and_read_back(tmp_path):
+    import pytest
+    rng = np.random.default_rng(2)
+    pos = rng.uniform(-3.5e6, 3.5e6, (3000, 3))
+    vel = rng.normal(0, 0.3, (3000, 3))
+    a, b = tmp_path / "lib.restart", tmp_path / "py.restart"
+    _lib.write_restart_file(str(a), pos, vel)
+    with open(b, "w") as f:  # the reference's loop (opendust.py:1109-1114)
+        for j in range(3000):
+            f.write("{}\t{}\t{}\t{}\t{}\t{}\n".format(pos[j, 0], pos[j, 1], pos[j, 2],
+                                                      vel[j, 0], vel[j, 1], vel[j, 2]))
+    assert a.read_bytes() == b.read_bytes()
+    p2, v2 = _lib.read_restart_file(str(b), 3000)
+    assert np.array_equal(p2, pos) and np.array_equal(v2, vel)  # shortest repr reads back exactly
+    p3, _ = _lib.read_restart_file(str(b), 10)
+    assert np.array_equal(p3, pos[:10])
+    with pytest.raises(_lib.OpenDustError, match="fewer"):
+        _lib.read_restart_file(str(b), 3001)
