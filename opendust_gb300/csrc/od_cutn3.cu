@@ -245,6 +245,8 @@ __device__ __forceinline__ int cut_diag_mode(int ga, int gb) {
   return s0 >= t0 + GT ? 2 : (s0 >= t0 ? 1 : 0);
 }
 
+constexpr int kItem = 63, kInner = 128;  // list entry: group pair index | inner flag
+
 template <int MT, int MS, int CUT, bool COUNT>
 __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ sx,
                                                       const float* __restrict__ sy,
@@ -253,7 +255,7 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
                                                       float* __restrict__ outR,
                                                       const n3_consts& k, int a, int b, float* sm,
                                                       const float* __restrict__ gbox,
-                                                      float cull2) {
+                                                      float cull2, float k_in2) {
   using CT = cut_traits<MT, MS>;
   constexpr int GT = CT::GT, GS = CT::GS, T = CT::T, NBT = CT::NBT, NBS = CT::NBS, NI = CT::NI;
   constexpr int MS2 = MS / 2;
@@ -277,22 +279,27 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
     for (int r = 0; r < NI / 32; r++) {
       const int c = r * 32 + lane, ga = c / NBS, gb = c % NBS;
       const int mode = diag ? cut_diag_mode<GT, GS>(ga, gb) : 2;
-      bool keep = mode == 1;
-      if (mode == 2) {
+      bool keep = mode == 1, inner = false;
+      if (mode != 0) {
         float ta[6], tb[6];
         group_box(gbox, (a * NBT + ga) * (GT / 64), GT / 64, ta);
         group_box(gbox, (b * NBS + gb) * (GS / 64), GS / 64, tb);
-        float d2 = 0.f;
+        float d2 = 0.f, f2 = 0.f;  // nearest and farthest box distances, squared
 #pragma unroll
         for (int d = 0; d < 3; d++) {
           const float gap = fmaxf(fmaxf(tb[d] - ta[3 + d], ta[d] - tb[3 + d]), 0.f);
+          const float far = fmaxf(tb[3 + d] - ta[d], ta[3 + d] - tb[d]);
           d2 = fmaf(gap, gap, d2);
+          f2 = fmaf(far, far, f2);
         }
-        keep = d2 < cull2;
+        if (mode == 2) keep = d2 < cull2;
+        // every pair of the two groups closer than the switching radius (hard cutoff: the
+        // cutoff): the switching factor is exactly 1 there, so the plain term applies
+        inner = f2 < k_in2;
       }
       const unsigned int bal = __ballot_sync(0xffffffffu, keep);
       const int pos = n + __popc(bal & ((1u << lane) - 1u));
-      if (keep) items[pos] = (unsigned char)c;
+      if (keep) items[pos] = (unsigned char)(c | (inner ? kInner : 0));
       item_of[c] = keep ? (signed char)pos : (signed char)-1;
       n += __popc(bal);
     }
@@ -303,7 +310,7 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
       const int i = r * 32 + lane;
       bool f = false;
       if (i < n)
-        f = i == 0 || items[i - 1] / NBS != items[i] / NBS ||
+        f = i == 0 || (items[i - 1] & kItem) / NBS != (items[i] & kItem) / NBS ||
             cut_owner(i - 1, n) != cut_owner(i, n);
       const unsigned int bal = __ballot_sync(0xffffffffu, f);
       if (i < n) segid[i] = (unsigned char)(nseg + __popc(bal & ((2u << lane) - 1u)) - 1);
@@ -314,9 +321,9 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
     for (int r = 0; r < 2; r++) {
       const int i = r * 32 + lane;
       if (i < n) {
-        const int ga = items[i] / NBS;
-        if (i == 0 || items[i - 1] / NBS != ga) gs0[ga] = (signed char)segid[i];
-        if (i == n - 1 || items[i + 1] / NBS != ga) gs1[ga] = (signed char)segid[i];
+        const int ga = (items[i] & kItem) / NBS;
+        if (i == 0 || (items[i - 1] & kItem) / NBS != ga) gs0[ga] = (signed char)segid[i];
+        if (i == n - 1 || (items[i + 1] & kItem) / NBS != ga) gs1[ga] = (signed char)segid[i];
       }
     }
     if (lane == 0) *s_n = n;
@@ -332,7 +339,8 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
 #define CUT_H(c, kt) (HS ? hs[(c) * GT + 32 * (kt)] : hreg[(c) * MT + (kt)])
   int cur = -1;
   for (int i = i0; i < i1; i++) {
-    const int c = items[i], ga = c / NBS, gb = c % NBS;
+    const int c = items[i] & kItem, ga = c / NBS, gb = c % NBS;
+    const bool inner = (items[i] & kInner) != 0;
     if (ga != cur) {
       if (!HS && cur >= 0) {
         float* t = Tg + (size_t)segid[i - 1] * 6 * GT + lane;
@@ -362,11 +370,19 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
 #pragma unroll
     for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
     if (diag && cut_diag_mode<GT, GS>(ga, gb) == 1) {
-      n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+      if (inner)
+        n3_group<MT, MS, 0, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
                                           cnt);
+      else
+        n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                            cnt);
     } else {
-      n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+      if (inner)
+        n3_group<MT, MS, 0, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
                                          cnt);
+      else
+        n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
+                                           cnt);
       // the force on the sources is minus the accumulated terms
       float* r = R + (size_t)i * 3 * GS + lane;
 #pragma unroll
@@ -455,7 +471,7 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
       const int2 ab = pairs[k];
       cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, S + ((size_t)ab.x * nT + ab.y) * T6,
                                                S + ((size_t)ab.y * nT + ab.x) * T6, kc, ab.x,
-                                               ab.y, sm, gbox, cull2);
+                                               ab.y, sm, gbox, cull2, cut.in2);
     }
   } else {
     for (int k = blockIdx.x; k < np; k += gridDim.x) {
@@ -604,7 +620,10 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
   k_scan_excl<<<1, 1024, 0, s>>>(L.nT, L.rowptr, L.rowptr);
   k_tile_list<<<(L.nT + 127) / 128, 128, 0, s>>>(L.nT, L.nwords, L.adj, L.rowptr, L.pairs);
   const bool sw = rs < rc;
-  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f};
+  // group pairs whose farthest box distance is below the switching radius (hard cutoff: the
+  // cutoff), with a relative margin of 1e-5 against rounding, skip the switching polynomial
+  const float rin = (sw ? rs : rc) * (1.0f - 1e-5f);
+  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f, rin * rin};
   const int32_t* np = L.rowptr + L.nT;
 #define OD_CUTN3(MT, MS, BAL, SM)                                                             \
   do {                                                                                        \

@@ -18,6 +18,7 @@ struct n3_consts {
 };
 struct n3_cut {
   float rho0, rc2, rs, inv_w;
+  float in2;  // cutoff tile pairs: group pairs closer than sqrt(in2) take the CUT = 0 term
 };
 
 __device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
