@@ -265,7 +265,13 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * ions, 8 with two; jsplit = ions per tile, 1024, 2048 or 4096 (not 1024 with 8), <= 0 for the
  * default; needs 24 bytes of device memory per ion and tile, OD_ERR_OOM when that does not
  * fit). From 2^15 ions od_create selects variant 7 when its memory fits 32 GiB.
- * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step. */
+ * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step.
+ * Cutoff method (force_method OD_FORCE_CUTOFF): variant 0 or 2 walks a stencil of cells per
+ * target cell (scalar or packed); variant 3 (the default when its memory fits 32 GiB) sorts
+ * the ions along a Hilbert curve and evaluates each pair inside the cutoff once over tile
+ * pairs whose bounding boxes come within it — targets_per_thread 2 with 512-ion tiles
+ * (balanced group-pair lists) or 4 with 1024-ion tiles; a positive jsplit must name that tile
+ * size; 24 bytes of device memory per ion and tile. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);
 /* Autotuner: times every supported (threads, targets_per_thread, variant) and three source
