@@ -347,7 +347,7 @@ od_status od_batch_step(od_batch* b, int64_t nsteps);
 od_status od_batch_last_step_ms(const od_batch* b, double* ms);
 /* The all-pairs plan a batch member with n_ions ions steps with (plan5 as od_get_pair_plan;
  * jsplit 0 = the member's default split): variant 7 with 4 x 4 ions per lane and 1024-ion
- * tiles up to 2^17 ions, 8 x 2 and 2048-ion tiles above, or variant 5 when the tile-pair matrix
+ * tiles up to 2^16 ions, 8 x 2 and 2048-ion tiles above, or variant 5 when the tile-pair matrix
  * does not fit. A single simulation given the same plan produces bitwise the same results. No
  * counterpart in the reference (it has no batching). */
 od_status od_batch_pair_plan(int64_t n_ions, int32_t* plan5);

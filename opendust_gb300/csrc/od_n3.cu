@@ -173,11 +173,12 @@ cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int
 }
 
 int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
-  // 4 x 4 with 1024-ion tiles up to 2^17 ions (2.87e12 pair terms/s at 2^17 against 2.85e12
-  // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.94e12 at 2^18, 2.99e12 at 2^20), then 4 x 4
-  // with 4096-ion tiles: the first whose tile-pair matrix fits the budget
+  // 4 x 4 with 1024-ion tiles up to 2^16 ions (2.79e12 pair terms/s at 2^16 against 2.51e12
+  // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.91e12 at 2^17 against 2.87e12 for 4 x 4,
+  // 2.99e12 at 2^18, 3.05e12 at 2^20), then 4 x 4 with 4096-ion tiles: the first whose
+  // tile-pair matrix fits the budget
   const int cand[3][2] = {{4, 1024}, {8, 2048}, {4, 4096}};
-  for (int c = Npad <= (1 << 17) ? 0 : 1; c < 3; c++)
+  for (int c = Npad <= (1 << 16) ? 0 : 1; c < 3; c++)
     if (sizeof(float) * od_n3_floats(Npad, cand[c][1]) <= budget_bytes) {
       *ipt = cand[c][0];
       return cand[c][1];
@@ -204,10 +205,11 @@ cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s) {
 }
 
 int od_n3_batch_plan(int Npad, size_t budget_bytes, int* ipt) {
-  // batch members: 4 x 4 with 1024-ion tiles up to 2^17 ions (also below 2^15, where the tile
-  // pairs of the other members fill the GPU), 8 x 2 with 2048-ion tiles above; 0 when the
-  // matrix does not fit (the member then takes the directed-pair kernel)
-  const int T = Npad <= (1 << 17) ? 1024 : 2048;
+  // batch members: 4 x 4 with 1024-ion tiles up to 2^16 ions (also below 2^15, where the tile
+  // pairs of the other members fill the GPU), 8 x 2 with 2048-ion tiles above, as a member
+  // stepped alone; 0 when the matrix does not fit (the member then takes the directed-pair
+  // kernel)
+  const int T = Npad <= (1 << 16) ? 1024 : 2048;
   if (sizeof(float) * od_n3_floats(Npad, T) > budget_bytes) return 0;
   *ipt = T == 1024 ? 4 : 8;
   return T;

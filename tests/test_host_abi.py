@@ -130,8 +130,8 @@ def test_config_validation(cpu_lib):
 def test_batch_pair_plan_rule():
     # the plan a batch member steps with (host arithmetic only, no device call)
     assert _lib.batch_pair_plan(2048) == (256, 4, 7, 1024)
-    assert _lib.batch_pair_plan(2**17) == (256, 4, 7, 1024)
-    assert _lib.batch_pair_plan(2**17 + 1) == (256, 8, 7, 2048)
+    assert _lib.batch_pair_plan(2**16) == (256, 4, 7, 1024)
+    assert _lib.batch_pair_plan(2**16 + 1) == (256, 8, 7, 2048)
     assert _lib.batch_pair_plan(2**20) == (256, 8, 7, 2048)
     # 2^22 ions: the tile-pair matrix (206 GB) exceeds the 32 GiB budget -> directed pairs
     assert _lib.batch_pair_plan(2**22)[2] == 5
