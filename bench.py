@@ -34,6 +34,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -109,7 +110,9 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples: $OD_CLOCKS_DIR if set (to keep them), else the system temp directory
+        self.path = os.path.join(os.environ.get("OD_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"opendust_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
