@@ -267,7 +267,7 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * fit). From 2^15 ions od_create selects variant 7 when its memory fits 32 GiB.
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step.
  * Cutoff method (force_method OD_FORCE_CUTOFF): variant 0 or 2 walks a stencil of cells per
- * target cell (scalar or packed); variant 3 (the default when its memory fits 32 GiB) sorts
+ * target cell (scalar or packed); variant 3 (the default when its memory fits 64 GiB) sorts
  * the ions along a Hilbert curve and evaluates each pair inside the cutoff once over tile
  * pairs whose bounding boxes come within it — targets_per_thread 2 with 512-ion tiles
  * (balanced group-pair lists) or 4 with 1024-ion tiles; a positive jsplit must name that tile

@@ -279,10 +279,14 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
 // (variant 5, the fastest measured on GB300 from 2^16 to 2^20 ions), with enough source chunks
 // for several waves on every SM.
 // From 2^15 padded ions the default is variant 7 (each unordered pair once: 4 x 4 ions per lane
-// with 1024-ion tiles up to 2^17 ions, then 8 x 2 with 2048-ion tiles) when its tile-pair matrix
+// with 1024-ion tiles up to 2^16 ions, then 8 x 2 with 2048-ion tiles) when its tile-pair matrix
 // fits OD_N3_BUDGET (about a ninth of a GB300's memory: 2048-ion tiles up to 2^20 ions, 4096-ion
 // tiles up to 2^21); od_create falls back to the plan below otherwise.
 static constexpr size_t OD_N3_BUDGET = (size_t)32 << 30;
+// The cutoff's tile-pair matrix (cutoff variant 3) may take up to a quarter of a GB300's memory:
+// 512-ion tiles, with the balanced group-pair lists (1.4x faster per step than the 1024-ion
+// fallback at 2^19 ions), up to about 2^20 ions.
+static constexpr size_t OD_CUTN3_BUDGET = (size_t)64 << 30;
 static bool uses_n3_default(int Npad) { return Npad >= 32768; }
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile);
 
@@ -461,8 +465,8 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
     // default: tile pairs with each pair once (512-ion tiles, else 1024) when the tile-pair
     // matrix fits the budget; the cell-stencil kernel otherwise
     const int G = od_cutn3_grid(h->N);
-    const int cut_ipt = od_cutn3_bytes(h->N, 512, G) <= OD_N3_BUDGET ? 2
-                        : (od_cutn3_bytes(h->N, 1024, G) <= OD_N3_BUDGET ? 4 : 0);
+    const int cut_ipt = od_cutn3_bytes(h->N, 512, G) <= OD_CUTN3_BUDGET ? 2
+                        : (od_cutn3_bytes(h->N, 1024, G) <= OD_CUTN3_BUDGET ? 4 : 0);
     if (cut_ipt && alloc_cutn3(h, cut_ipt, cut_ipt == 2 ? 512 : 1024) != OD_OK) {
       cudaGetLastError();
       h->err.clear();
@@ -1643,8 +1647,8 @@ extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes
     const int G = od_cutn3_grid((int)cfg->n_ions);
     const size_t c512 = od_cutn3_bytes((int)cfg->n_ions, 512, G);
     const size_t c1024 = od_cutn3_bytes((int)cfg->n_ions, 1024, G);
-    if (c512 <= OD_N3_BUDGET) b += (int64_t)c512;
-    else if (c1024 <= OD_N3_BUDGET) b += (int64_t)c1024;
+    if (c512 <= OD_CUTN3_BUDGET) b += (int64_t)c512;
+    else if (c1024 <= OD_CUTN3_BUDGET) b += (int64_t)c1024;
   }
   if (cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default((int)Np)) {
     int ipt = 0;
