@@ -216,7 +216,9 @@ __global__ void k_tile_list(int nT, int nwords, const uint32_t* __restrict__ adj
 // at every slice start: at most NBT + 7); every item stores its FP32 reaction sums in a slot of
 // its own. The block then sums the slots of each ion in a fixed order — target segments in list
 // order, then reactions in target-group order — so the result does not depend on which warp
-// ran what, or when.
+// ran what, or when. A group pair whose farthest box distance is below the switching radius
+// (hard cutoff: the cutoff) is marked inner and takes the plain screened term: the switching
+// factor is exactly 1 for all its pairs.
 template <int MT, int MS>
 struct cut_traits {
   static constexpr int GT = 32 * MT, GS = 32 * MS;    // target and source group sizes
