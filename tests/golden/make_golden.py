@@ -1,8 +1,9 @@
 """Extract the reference's published example results into tests/golden/reference_examples.json.
 
-Reads the run logs committed with the reference (OpenDust) under its examples/ directory
-and records, for each run, the printed time-averaged forces together with the run's
-parameters taken from the launch script next to the log. The reference's runs are
+Reads the run logs and result files committed with the reference (OpenDust) under its
+examples/ directory and records, for each run, the time-averaged forces (and, for the
+field-driven Patacchini 2008 runs, the grain charge) together with the run's parameters taken
+from the launch script next to them. The reference's runs are
 unseeded, so these values pin the physics statistically, not bit for bit.
 
 Usage (only where the reference tree is available):
@@ -48,6 +49,30 @@ def main(ref):
                 **common, "name": f"piel2017_fig5_M{M}", "source": f"examples/Piel2017/{log}",
                 "M": M, "N": 2**16, "n": 5000, "avg_after": 3000, "grain_z_lambda": 0.0,
                 "method": "oml", "q0_e": 392500.0, "F_orbit_z": orb, "F_collect_z": col})
+    # field-driven plasma (Patacchini 2008, Fig. 3): per collision frequency, the time averages
+    # over steps > 150000 written by the launch script to charge.txt and force.txt
+    fig = os.path.join(ex, "Patacchini2008", "Figure3")
+    script = open(os.path.join(fig, "launchPatacchini2008Figure3.py")).read()
+
+    def _array(name):
+        body = re.search(name + r"\s*=\s*np\.asarray\(\s*\[(.*?)\]", script, re.S).group(1)
+        return [float(x) for x in re.findall(r"[-0-9.e+]+", body)]
+
+    w_c, E = _array("w_c_array"), _array("E_array")
+    charge = [tuple(float(x) for x in line.split()) for line in open(os.path.join(fig, "charge.txt"))
+              if line.strip()]
+    force = [tuple(float(x) for x in line.split()) for line in open(os.path.join(fig, "force.txt"))
+             if line.strip()]
+    for k, (wc, e) in enumerate(zip(w_c, E)):
+        qrow = next(r for r in charge if abs(r[0] / wc - 1) < 1e-6)
+        frow = next(r for r in force if abs(r[0] / wc - 1) < 1e-6)
+        out["runs"].append({
+            "name": f"patacchini2008_fig3_p{k + 1}", "source": "examples/Patacchini2008/Figure3",
+            "distribution": "fieldDriven", "T_e": 30000.0, "T_n": 300.0, "n_inf": 3.57167962497e15,
+            "m_i": 1.673557e-27, "E": e, "w_c": wc, "R_lambda": 3.0, "H_lambda": 6.0,
+            "N": 2**17, "n": 200000, "d_t": 1e-11, "avg_after": 150000, "grain_r": 1e-5,
+            "grain_z_lambda": -1.0, "method": "consistent", "q0_e": 0.0, "q": qrow[1],
+            "F_orbit_z": frow[1], "F_collect_z": frow[2]})
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_examples.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)

@@ -34,14 +34,38 @@ RUNS = {r["name"]: r for r in json.load(open(os.path.join(HERE, "golden", "refer
 def test_golden_fixture_consistent():
     from opendust_gb300 import PlasmaParametersInSIUnitsMaxwell, SimulationParametersInSIUnits
 
-    assert len(RUNS) == 15
+    assert len(RUNS) == 28
     r = RUNS["piel2017_fig5_M2.0"]
     p = PlasmaParametersInSIUnitsMaxwell(r["T_i"], r["T_e"], r["n_inf"], r["M"], r["m_i"])
     s = SimulationParametersInSIUnits(3 * p.r_D_e, 6 * p.r_D_e, r["N"], r["n"], r["d_t"], p)
     # N_s printed by the reference run (examples/Piel2017/Figure5/outputPiel2017Fig5)
     assert s.N_s == pytest.approx(420.3631132989799, rel=1e-12)
     for run in RUNS.values():
-        assert run["F_orbit_z"] > 0
+        if run["distribution"] == "Maxwellian":
+            assert run["F_orbit_z"] > 0
+
+
+def test_golden_fixture_field_driven():
+    # the 13 field-driven runs of examples/Patacchini2008/Figure3 (Mach 1 at every collision
+    # frequency); the parameter classes reproduce the values the reference printed in
+    # examples/Patacchini2008/Figure3/outputPatacchini2008
+    from opendust_gb300 import PlasmaParametersInSIUnitsFieldDriven, SimulationParametersInSIUnits
+
+    runs = [r for r in RUNS.values() if r["distribution"] == "fieldDriven"]
+    assert len(runs) == 13
+    assert [r["w_c"] for r in runs] == sorted(r["w_c"] for r in runs)
+    assert all(r["q"] < 0 for r in runs)
+    r = runs[0]
+    p = PlasmaParametersInSIUnitsFieldDriven(r["T_n"], r["T_e"], r["n_inf"], r["E"], r["w_c"], r["m_i"])
+    assert p.r_D_e == pytest.approx(0.0002000000000000135, rel=1e-12)
+    assert p.v_B == pytest.approx(15731.930327435968, rel=1e-12)
+    assert p.M == pytest.approx(1.0000000012668968, rel=1e-12)
+    s = SimulationParametersInSIUnits(3 * p.r_D_e, 6 * p.r_D_e, r["N"], r["n"], r["d_t"], p)
+    assert s.N_s == pytest.approx(36.982493495016854, rel=1e-12)
+    for r in runs:
+        p = PlasmaParametersInSIUnitsFieldDriven(r["T_n"], r["T_e"], r["n_inf"], r["E"], r["w_c"],
+                                                 r["m_i"])
+        assert p.M == pytest.approx(1.0, rel=1e-6)
 
 
 def run_example(r, seed):
