@@ -3,12 +3,13 @@
     python -m opendust_gb300.profiling pairs  --n 65536  --plan 256,1,5 --steps 2
     python -m opendust_gb300.profiling cutoff --n 131072 --variant 2    --steps 2
     python -m opendust_gb300.profiling cutoff --n 524288 --variant 3 --plan 256,2,3 --steps 2
-    python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576 [--plans '256,1,5;256,4,7']
+    python -m opendust_gb300.profiling sweep  --n 65536,262144,1048576 [--plans '256,1,5;256,8,7']
 
 `pairs` steps the small_plain workload with the given all-pairs plan, `cutoff` the field_chain
-workload (cutoff 2 lambda over the cell list), both launching kernel by kernel (no CUDA graph) so
-that `ncu -k regex:<kernel>` sees individual launches. `sweep` times every all-pairs plan with
-CUDA events and prints pairs/s.
+workload (cutoff 2 lambda; variants 0 and 2 walk a cell stencil, variant 3 with --plan takes the
+tile pairs over Hilbert-sorted ions), both launching kernel by kernel (no CUDA graph) so that
+`ncu -k regex:<kernel>` sees individual launches. `sweep` times every all-pairs plan with CUDA
+events and prints pairs/s (a plan may carry the tile size as a fourth number, e.g. 256,8,7,2048).
 """
 from __future__ import annotations
 
