@@ -214,3 +214,31 @@ def test_injection_tables_shape():
     p2, s2, g2, d2, _ = workloads.field_chain(N=2, n=2)
     t2, pr2 = setup_host.injection_setup(p2.v_fl, p2.v_T, s2.R, s2.H, d2)
     assert len(t2[3][0]) > 10 and abs(sum(pr2) - 1) < 1e-12
+
+
+def test_two_ion_cutoff_switching():
+    # OpenMM's switching function on the energy (opendust.py:481-485): U(r) S(x), S = 1 - 10x^3
+    # + 15x^4 - 6x^5, x = (r - r_s)/(r_c - r_s) on [r_s, r_c]; S = 1 below r_s, the force 0 above
+    # r_c. The reference force is the central difference of the switched energy.
+    holder, plasma, sim, _ = _cfg(N=2, builder=workloads.field_chain)
+    c = holder.cfg
+    lam = plasma.r_D_e
+    rc, rs = c.cutoff, c.switch_dist
+    assert rc == pytest.approx(2 * lam) and rs == pytest.approx(2 * lam * 3.0 / 3.2)
+    k = 1 / (4 * np.pi * plasma.eps_0)
+    q_s = abs(plasma.e) * sim.N_s
+
+    def energy(r):
+        x = min(max((r - rs) / (rc - rs), 0.0), 1.0)
+        return k * q_s**2 * math.exp(-r / lam) / (r + sim.r_0) * (1 - 10 * x**3 + 15 * x**4 - 6 * x**5)
+
+    for d in (0.5, 1.8, 1.88, 1.93, 1.99, 2.01, 2.5):
+        r = d * lam
+        pos = np.array([[0.2 * lam, -0.1 * lam, 0.3 * lam], [0.2 * lam + r, -0.1 * lam, 0.3 * lam]])
+        f = oracle.force_snapshot(holder, pos, round32=False)
+        h = 1e-7 * lam
+        mag = -(energy(r + h) - energy(r - h)) / (2 * h)  # force along +d on ion 1, -d on ion 0
+        np.testing.assert_allclose(f[1, 0], mag, rtol=1e-6, atol=1e-12 * abs(mag) + 1e-300)
+        np.testing.assert_allclose(f[0, 0], -mag, rtol=1e-6, atol=1e-12 * abs(mag) + 1e-300)
+        if d > 2.0:
+            assert f[1, 0] == 0.0
