@@ -15,10 +15,12 @@
 //     source groups and a __syncthreads() between steps makes the shared-memory updates
 //     race-free.
 //   * Inside a group pair the sources rotate around the warp: at each of the 32 lane steps every
-//     lane evaluates its MT targets against the MS sources it holds (packed f32x2, two sources
-//     per operation), then passes the sources — positions and their FP32 reaction sums — to the
-//     previous lane. After 32 steps every source is back in its own lane with the sum of the
-//     GT target reactions on it.
+//     lane evaluates its MT targets against the MS sources it holds, then passes the sources —
+//     positions and their FP32 reaction sums — to the previous lane. After 32 steps every source
+//     is back in its own lane with the sum of the GT target reactions on it. The packed f32x2
+//     operations pair two sources against one target (each target duplicated in both halves)
+//     or, with 8 targets per lane, two targets against one broadcast source (n3_group_tp: half
+//     the target registers, more independent pair chains in flight).
 //   * Diagonal tiles (a == b) evaluate the source groups inside a warp's own target group as
 //     directed pairs (no reaction; the self pair contributes exactly 0) and skip source groups
 //     below it.
