@@ -45,13 +45,19 @@ def _flux_field(v_fl, v_T, weight_v: bool):
 
 
 def _table_from_nodes(v, xi):
-    """Rounded piecewise-linear inverse CDF: v[i-1] + (u - xi[i-1]) * slope[i]."""
+    """Rounded piecewise-linear inverse CDF: v[i-1] + (u - xi[i-1]) * slope[i].
+
+    Where the CDF is flat to double precision (a tail whose flux underflows, so that two nodes
+    hold the same CDF value) the interval is empty and its slope is set to 0: a draw of exactly
+    that CDF value (u = 0 below a flat leading tail) then yields the node's speed instead of
+    0 * inf = NaN."""
     n = len(v)
     vr = np.array([_r8(x) for x in v])
     xr = np.array([_r8(x) for x in xi])
     sl = np.zeros(n)
     for i in range(1, n):
-        sl[i] = _r8((v[i] - v[i - 1]) / (xi[i] - xi[i - 1]))
+        dx = xi[i] - xi[i - 1]
+        sl[i] = _r8((v[i] - v[i - 1]) / dx) if dx > 0 else 0.0
     return vr * NMPS, xr, sl * NMPS
 
 

@@ -36,3 +36,28 @@ def test_field_driven_vz_table_is_a_cdf():
     vz = sh.field_driven_vz(v_fl, v_T, u)
     assert np.all(np.isfinite(vz)) and v.min() <= vz.min() and vz.max() <= v.max()
     assert 0.5 * v_fl < vz.mean() < 2.0 * v_fl
+
+
+def _tab_eval(v, xi, sl, u):
+    # the device's and the oracle's lookup (first node at or above u, linear from the one before)
+    i = 1
+    while i < len(v) - 1 and u > xi[i]:
+        i += 1
+    return v[i - 1] + (u - xi[i - 1]) * sl[i]
+
+
+def test_injection_tables_finite_at_every_draw():
+    # a slow field-driven flow (Mach 0.02: the test_gpu_api plasma) leaves the side v_z CDF flat
+    # (0 to double precision) over its leading nodes, as fast flows can for the face fluxes;
+    # draws of exactly 0 and 1 must still give finite speeds
+    for M in (0.0196582722, 1.0, 2.0):
+        v_T = 249.87926383157722
+        for dist in ("Maxwellian", "fieldDriven"):
+            tables, probs = sh.injection_setup(M * 2457.3, v_T, 3e-3, 6e-3, dist)
+            for v, xi, sl in tables:
+                v, xi, sl = (np.asarray(a, dtype=np.float64) for a in (v, xi, sl))
+                if len(v) == 0:
+                    continue
+                assert np.all(np.isfinite(sl)), (M, dist)
+                for u in (0.0, 2.0**-24, 0.5, 1.0 - 2.0**-24, 1.0):
+                    assert np.isfinite(_tab_eval(v, xi, sl, u)), (M, dist, u)
