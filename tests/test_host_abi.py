@@ -135,3 +135,22 @@ def test_batch_pair_plan_rule():
     assert _lib.batch_pair_plan(2**20) == (256, 8, 7, 2048)
     # 2^22 ions: the tile-pair matrix (206 GB) exceeds the 32 GiB budget -> directed pairs
     assert _lib.batch_pair_plan(2**22)[2] == 5
+
+
+def test_config_device_bytes_budget_rules():
+    # host arithmetic only: the tile-pair matrices od_create would allocate by default
+    from opendust_gb300 import build_simulation, workloads
+
+    def gb(builder, N):
+        plasma, sim, grains, dist, ext = builder(N=N, n=4)
+        holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, trap=np.zeros(15), **ext)
+        return _lib.config_device_bytes(holder) / 1e9
+
+    # cutoff: 512-ion tiles while the dense matrix fits 64 GiB (2^19: 12.9 GB, 2^20: 51.5 GB),
+    # the cell stencil beyond (no matrix)
+    assert 12.9 < gb(workloads.field_chain, 2**19) < 13.3
+    assert 51.5 < gb(workloads.field_chain, 2**20) < 52.2
+    assert gb(workloads.field_chain, 2**21) < 1.0
+    # all pairs: 2048-ion tiles at 2^20 (12.9 GB), no matrix below 2^15
+    assert 12.9 < gb(workloads.full_plain, 2**20) < 13.3
+    assert gb(workloads.small_plain, 2**14) < 0.1
