@@ -259,6 +259,7 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
     p->mfp_inv = (float)(1.0 / mfp_h);
     p->vmax_mfp = (float)vmax;
     p->Pmax_mfp = 1.0 - exp(-vmax / mfp_h);
+    p->mfp_inv_d = 1.0 / mfp_h;
   }
   p->p_t = c->p_top; p->p_s = c->p_side; p->p_b = c->p_bottom;
   for (int t = 0; t < OD_NTAB; t++) {

@@ -38,7 +38,7 @@ struct od_dparams {
   // FP64 exact-flag constants (identical doubles in the CPU oracle)
   double gx[OD_MAX_GRAINS], gy[OD_MAX_GRAINS], gz[OD_MAX_GRAINS], gr2[OD_MAX_GRAINS];
   double Rh2, Hh_half_d;
-  double p_coll, Pmax_mfp, p_t, p_s, p_b;
+  double p_coll, Pmax_mfp, mfp_inv_d, p_t, p_s, p_b;
   // injection tables (lambda/d_t units for v and slope)
   int32_t tn[OD_NTAB];
   float tv[OD_NTAB][OD_MAX_TABLE];

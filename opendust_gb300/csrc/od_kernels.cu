@@ -395,17 +395,20 @@ __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint3
       if (c2) v.z = p.vT * gz;
     }
   } else if (p.coll == OD_COLL_MFP) {
-    // null collision: candidate with probability Pmax, real with probability |v|/vmax
+    // null collision: candidate with probability Pmax = 1 - exp(-vmax/mfp), real with
+    // probability |v|/vmax; an ion faster than the majorant vmax (accelerated by a grain or the
+    // field) collides with its own probability 1 - exp(-|v| d_t/mfp) instead of being capped
     od_u4 w = od_draw(p, ion, step, OD_RNG_MFP_TEST);
-    if ((double)od_u01(w.x) < p.Pmax_mfp) {
-      float sp = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-      if (od_u01(w.y) * p.vmax_mfp < sp) {
-        od_u4 g = od_draw(p, ion, step, OD_RNG_MFP_GAUSS);
-        float gx, gy, gz, dummy;
-        od_gauss2(g.x, g.y, gx, gy);
-        od_gauss2(g.z, g.w, gz, dummy);
-        v.x = p.vT * gx; v.y = p.vT * gy; v.z = p.vT * gz;
-      }
+    const float sp = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    const bool hit = sp <= p.vmax_mfp
+                         ? (double)od_u01(w.x) < p.Pmax_mfp && od_u01(w.y) * p.vmax_mfp < sp
+                         : (double)od_u01(w.z) < 1.0 - exp(-(double)sp * p.mfp_inv_d);
+    if (hit) {
+      od_u4 g = od_draw(p, ion, step, OD_RNG_MFP_GAUSS);
+      float gx, gy, gz, dummy;
+      od_gauss2(g.x, g.y, gx, gy);
+      od_gauss2(g.z, g.w, gz, dummy);
+      v.x = p.vT * gx; v.y = p.vT * gy; v.z = p.vT * gz;
     }
   }
 }

@@ -365,16 +365,18 @@ static void collide(const odo_par* p, uint32_t ion, uint32_t step, double* v) {
       if (c2) v[2] = p->vT * gz;
     }
   } else if (p->coll == OD_COLL_MFP) {
+    /* null collision against the majorant speed vmax; an ion faster than vmax collides with
+       its own probability 1 - exp(-|v| d_t / mfp) */
     draw(p->seed, ion, step, OD_RNG_MFP_TEST, p->sim, w);
-    if (u01(w[0]) < p->Pmax_mfp) {
-      double sp = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-      if (u01(w[1]) * p->vmax_mfp < sp) {
-        double gx, gy, gz, dummy;
-        draw(p->seed, ion, step, OD_RNG_MFP_GAUSS, p->sim, g);
-        gauss2(g[0], g[1], &gx, &gy);
-        gauss2(g[2], g[3], &gz, &dummy);
-        v[0] = p->vT * gx; v[1] = p->vT * gy; v[2] = p->vT * gz;
-      }
+    double sp = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    int hit = sp <= p->vmax_mfp ? (u01(w[0]) < p->Pmax_mfp && u01(w[1]) * p->vmax_mfp < sp)
+                                : u01(w[2]) < 1.0 - exp(-sp / p->mfp_h);
+    if (hit) {
+      double gx, gy, gz, dummy;
+      draw(p->seed, ion, step, OD_RNG_MFP_GAUSS, p->sim, g);
+      gauss2(g[0], g[1], &gx, &gy);
+      gauss2(g[2], g[3], &gz, &dummy);
+      v[0] = p->vT * gx; v[1] = p->vT * gy; v[2] = p->vT * gz;
     }
   }
 }

@@ -242,3 +242,27 @@ def test_two_ion_cutoff_switching():
         np.testing.assert_allclose(f[0, 0], -mag, rtol=1e-6, atol=1e-12 * abs(mag) + 1e-300)
         if d > 2.0:
             assert f[1, 0] == 0.0
+
+
+def test_mfp_collisions_of_ions_faster_than_the_majorant():
+    # constant mean free path (null collision with the majorant vmax = 3|v_fl| + 10 v_T): an ion
+    # faster than vmax collides with its own probability 1 - exp(-|v| d_t / mfp), not the
+    # majorant's. Ions at 2 vmax, mfp chosen so that vmax d_t / mfp = 0.5: 1 - e^-1 = 0.632
+    # collide in one step (a capped rate would give 1 - e^-0.5 = 0.393).
+    plasma0, sim0, *_ = workloads.small_plain(N=2, n=4)
+    vmax = 3 * abs(plasma0.v_fl) + 10 * plasma0.v_T
+    mfp = 2 * vmax * sim0.d_t
+    N = 4000
+    holder, plasma, sim, grains = _cfg(N=N, collisions="mfp", mean_free_path=mfp)
+    rng = np.random.default_rng(4)
+    lam = plasma.r_D_e
+    r = 2.5 * lam * np.sqrt(rng.uniform(0, 1, N))
+    th = rng.uniform(0, 2 * np.pi, N)
+    pos = np.stack([r * np.cos(th), r * np.sin(th), rng.uniform(-2.5, -1.5, N) * lam], 1)
+    d = rng.normal(size=(N, 3))
+    vel = 2 * vmax * d / np.linalg.norm(d, axis=1, keepdims=True)
+    out = oracle.run(holder, pos, vel, 0, 1, round32=False)
+    collided = np.linalg.norm(out["vel"], axis=1) < vmax
+    p = collided.mean()
+    expect = 1 - math.exp(-1.0)
+    assert abs(p - expect) < 4 * math.sqrt(expect * (1 - expect) / N), (p, expect)
