@@ -284,6 +284,13 @@ od_status od_get_pair_plan(const od_handle* h, int32_t* plan5);
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured by a short probe
  * kernel: the denominator of the all-pairs kernel's roofline. */
 od_status od_probe_fp32_peak(int32_t device, double* tflops);
+/* Self test of the bounded device waits (no counterpart in the reference, whose OpenMM waits
+ * are unbounded). One thread on `device` arms an mbarrier and waits on it with the same wait
+ * routine the step kernels use, but with `limit` polls (1 to 2^26) instead of 2^26. With
+ * arrive = 0 nothing arrives, the wait runs out, the kernel records it in a device error word
+ * and returns, and the call returns OD_ERR_TIMEOUT with the context still usable; with
+ * arrive != 0 the thread arrives first and the call returns OD_OK. */
+od_status od_selftest_wait(int32_t device, uint32_t limit, int32_t arrive);
 
 /* Index of the next step (number of steps taken so far). */
 int64_t od_step_index(const od_handle* h);
@@ -394,7 +401,11 @@ od_status od_read_restart(const char* path, int64_t n, double* pos_nm, double* v
  * device and on `stream` (a cudaStream_t, NULL for the default stream) and returns after the
  * stream has finished it. The first call on each device looks up the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture. All calls share
- * the array: calls that overlap on the GPU (other streams, other host threads) race. */
+ * the array: calls that overlap on the GPU (other streams, other host threads) race. r_0 must
+ * be at least 1e-9 r_D_e (each ion's own pair has r = 0 and would overflow FP32 below that);
+ * smaller values return OD_ERR_INVALID. The device address is cached per device ordinal for
+ * the primary context: only the primary context is supported, and the cache is not cleared
+ * by cudaDeviceReset, so do not call this after resetting a device in the same process. */
 od_status od_ion_forces_static(const double* pos_dev, int64_t n, double r_D_e, double r_0,
                                double kq_sq_s, double* force_dev, void* stream);
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint32, c_uint64, c_void_p
 
 import numpy as np
 
@@ -151,6 +151,7 @@ def load(path: str | None = None):
         "od_set_graph": (c_int32, [H, c_int32]),
         "od_get_cutoff_pairs": (c_int32, [H, POINTER(c_int64)]),
         "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
+        "od_selftest_wait": (c_int32, [c_int32, c_uint32, c_int32]),
         "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
         "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
         "od_autotune": (c_int32, [H, c_int32, _DP]),

@@ -1131,6 +1131,26 @@ extern "C" od_status od_probe_fp32_peak(int32_t device, double* tflops) {
   return OD_OK;
 }
 
+extern "C" od_status od_selftest_wait(int32_t device, uint32_t limit, int32_t arrive) {
+  if (od_device_count() <= device || device < 0)
+    return fail(nullptr, OD_ERR_UNSUPPORTED, "no CUDA device with that index");
+  if (limit < 1 || limit > OD_WAIT_LIMIT)
+    return fail(nullptr, OD_ERR_INVALID, "limit must be 1 to 2^26 polls");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  uint32_t* d_err = nullptr;
+  e = cudaMalloc(&d_err, sizeof(uint32_t));
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc(error word)");
+  uint32_t err = 0;
+  e = cudaMemset(d_err, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = od_launch_wait_selftest(d_err, limit, arrive ? 1 : 0, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, sizeof(err), cudaMemcpyDeviceToHost);
+  cudaFree(d_err);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "wait self test");
+  if (err & OD_DERR_TIMEOUT) return fail(nullptr, OD_ERR_TIMEOUT, "a bounded device wait ran out");
+  return OD_OK;
+}
+
 extern "C" int64_t od_step_index(const od_handle* h) { return h ? h->step : -1; }
 
 extern "C" od_status od_get_series(od_handle* h, int64_t first, int64_t count, double* q,
@@ -1322,8 +1342,11 @@ extern "C" od_status od_ion_forces_static(const double* pos_dev, int64_t n, doub
     return fail(nullptr, OD_ERR_INVALID,
                 "od_ion_forces_static takes 2 to 32768 ions (its scratch array is sized for "
                 "32768); use od_force_snapshot for larger systems");
-  if (!(r_D_e > 0) || !(r_0 >= 0))
-    return fail(nullptr, OD_ERR_INVALID, "r_D_e must be positive and r_0 non-negative");
+  // Every ion is also a source, so its own pair enters with r = 0 and 1/(r + r_0) = 1/r_0;
+  // below r_0 = 1e-9 r_D_e the FP32 pair magnitude overflows there and turns the ion's force
+  // into NaN. The reference's own r_0 is 1e-3 r_D_e.
+  if (!(r_D_e > 0) || !(r_0 >= 1e-9 * r_D_e))
+    return fail(nullptr, OD_ERR_INVALID, "r_D_e must be positive and r_0 at least 1e-9 r_D_e");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDevice");

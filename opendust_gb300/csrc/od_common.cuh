@@ -317,10 +317,10 @@ __device__ __forceinline__ void od_bulk_g2s(void* dst, const void* src, uint32_t
       "l"(src), "r"(bytes), "r"(od_smem_addr(bar))
       : "memory");
 }
-// Wait for phase `parity` of the barrier; gives up after OD_WAIT_LIMIT polls and returns false.
-__device__ __forceinline__ bool od_mbar_wait(uint64_t* bar, uint32_t parity) {
+// Wait for phase `parity` of the barrier; gives up after `limit` polls and returns false.
+__device__ __forceinline__ bool od_mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t limit) {
   uint32_t addr = od_smem_addr(bar);
-  for (uint32_t it = 0; it < OD_WAIT_LIMIT; it++) {
+  for (uint32_t it = 0; it < limit; it++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -330,4 +330,11 @@ __device__ __forceinline__ bool od_mbar_wait(uint64_t* bar, uint32_t parity) {
     if (done) return true;
   }
   return false;
+}
+// The production wait: OD_WAIT_LIMIT polls (seconds on a GB300) before it gives up.
+__device__ __forceinline__ bool od_mbar_wait(uint64_t* bar, uint32_t parity) {
+  return od_mbar_wait_n(bar, parity, OD_WAIT_LIMIT);
+}
+__device__ __forceinline__ void od_mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(od_smem_addr(bar)) : "memory");
 }

@@ -178,6 +178,8 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
                                 int N, int Npad, int P, const od_force_ctx& fc, int nrec,
                                 cudaStream_t s);
 cudaError_t od_run_fp32_probe(int device, double* tflops);
+// one-thread mbarrier wait that gives up after `limit` polls unless `arrive` (self test)
+cudaError_t od_launch_wait_selftest(uint32_t* err, uint32_t limit, int arrive, cudaStream_t s);
 cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,
                                      uint32_t* flags, int32_t* list, int32_t* list_bits,
                                      double* counts, cudaStream_t s);

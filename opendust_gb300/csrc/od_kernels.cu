@@ -398,11 +398,16 @@ __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint3
     // null collision: candidate with probability Pmax = 1 - exp(-vmax/mfp), real with
     // probability |v|/vmax; an ion faster than the majorant vmax (accelerated by a grain or the
     // field) collides with its own probability 1 - exp(-|v| d_t/mfp) instead of being capped
+    // The branch and the acceptance test are decided in FP64 against the FP32 majorant, the
+    // same way the oracle decides them: the squares of FP32 components are exact in FP64, so
+    // the sum (x^2 + y^2) + z^2 rounds identically with or without FMA contraction.
     od_u4 w = od_draw(p, ion, step, OD_RNG_MFP_TEST);
-    const float sp = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
-    const bool hit = sp <= p.vmax_mfp
-                         ? (double)od_u01(w.x) < p.Pmax_mfp && od_u01(w.y) * p.vmax_mfp < sp
-                         : (double)od_u01(w.z) < 1.0 - exp(-(double)sp * p.mfp_inv_d);
+    const double sp2 = (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z;
+    const double vm = (double)p.vmax_mfp;
+    const double sp = sqrt(sp2);
+    const bool hit = sp2 <= vm * vm
+                         ? (double)od_u01(w.x) < p.Pmax_mfp && (double)od_u01(w.y) * vm < sp
+                         : (double)od_u01(w.z) < 1.0 - exp(-sp * p.mfp_inv_d);
     if (hit) {
       od_u4 g = od_draw(p, ion, step, OD_RNG_MFP_GAUSS);
       float gx, gy, gz, dummy;
@@ -1190,12 +1195,17 @@ cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& 
 }
 
 // FP32 FMA throughput probe: 8 independent FMA chains per thread, 8 blocks of 256 per SM.
+// The body is unrolled 16 times (128 FMAs per loop trip), so the loop counter and branch cost
+// about 2 % of the issue slots.
 __global__ void k_ffma_probe(float* out, float a, float b, int iters) {
   float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
         x6 = x0 + 6, x7 = x0 + 7;
-  for (int i = 0; i < iters; i++) {
-    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
-    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  for (int i = 0; i < iters; i += 16) {
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+      x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+    }
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
@@ -1411,5 +1421,25 @@ cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s) {
   k_b_collect_inject<<<v.nsims, kCT, 0, s>>>(v.sims);
   k_b_correct_orbit<<<v.nblk_corr, kBlk, 0, s>>>(v.sims, v.blk_corr);
   k_b_tail<<<v.nsims, kBlk, 0, s>>>(v.sims);
+  return cudaGetLastError();
+}
+
+// Bounded-wait self test. One thread arms an mbarrier that expects one arrival; with arrive = 0
+// nothing ever arrives, so od_mbar_wait_n gives up after `limit` polls and the kernel records
+// OD_DERR_TIMEOUT in *err and returns, the same path every production wait takes when its
+// limit runs out. No copy is in flight, so nothing else has to drain before the return.
+__global__ void k_wait_selftest(uint32_t* err, uint32_t limit, int arrive) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    od_mbar_init(&bar, 1);
+    od_fence_barrier_init();
+    if (arrive) od_mbar_arrive(&bar);
+    if (!od_mbar_wait_n(&bar, 0, limit)) atomicOr(err, OD_DERR_TIMEOUT);
+    od_mbar_inval(&bar);
+  }
+}
+
+cudaError_t od_launch_wait_selftest(uint32_t* err, uint32_t limit, int arrive, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(err, limit, arrive);
   return cudaGetLastError();
 }

@@ -203,8 +203,103 @@ static double pair_factor(const odo_par* p, double r2) {
   return f / r;
 }
 
+/* Cell list for the cutoff method: bins of side >= rc/2 over the ions' bounding box (a target
+ * visits the 5 x 5 x 5 bins around its own),
+ * ions of a bin listed in increasing index order (stable counting sort). Only the cost of the
+ * oracle changes: pair_factor is still applied to every pair of neighbouring bins and returns
+ * 0 beyond rc, so the set of pairs and their terms equal the plain double loop's (the order
+ * of the FP64 sum differs). */
+typedef struct {
+  int nc[3];
+  double lo[3], inv[3];
+  int64_t* start; /* nc0*nc1*nc2 + 1 */
+  int64_t* list;  /* n */
+} odo_cells;
+
+static int cell_coord(const odo_cells* cl, int d, double v) {
+  int c = (int)floor((v - cl->lo[d]) * cl->inv[d]);
+  return c < 0 ? 0 : (c >= cl->nc[d] ? cl->nc[d] - 1 : c);
+}
+
+static int cells_build(const odo_par* p, int64_t n, const double* x, odo_cells* cl) {
+  for (int d = 0; d < 3; d++) { cl->lo[d] = INFINITY; }
+  double hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++) {
+      double v = x[3 * i + d];
+      if (v < cl->lo[d]) cl->lo[d] = v;
+      if (v > hi[d]) hi[d] = v;
+    }
+  int64_t total = 1;
+  for (int d = 0; d < 3; d++) {
+    double ext = hi[d] - cl->lo[d];
+    int m = (int)floor(2.0 * ext / p->rc);
+    if (m < 1) m = 1;
+    if (m > 512) m = 512;
+    cl->nc[d] = m;
+    cl->inv[d] = ext > 0 ? m / ext : 0.0; /* bin side ext/m >= rc/2 */
+    total *= m;
+  }
+  cl->start = (int64_t*)calloc((size_t)total + 1, sizeof(int64_t));
+  cl->list = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+  int64_t* cid = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+  if (!cl->start || !cl->list || !cid) { free(cl->start); free(cl->list); free(cid); return 1; }
+  for (int64_t i = 0; i < n; i++) {
+    int cx = cell_coord(cl, 0, x[3 * i]), cy = cell_coord(cl, 1, x[3 * i + 1]);
+    int cz = cell_coord(cl, 2, x[3 * i + 2]);
+    cid[i] = ((int64_t)cz * cl->nc[1] + cy) * cl->nc[0] + cx;
+    cl->start[cid[i] + 1]++;
+  }
+  for (int64_t c = 0; c < total; c++) cl->start[c + 1] += cl->start[c];
+  int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)total);
+  if (!fill) { free(cl->start); free(cl->list); free(cid); return 1; }
+  memcpy(fill, cl->start, sizeof(int64_t) * (size_t)total);
+  for (int64_t i = 0; i < n; i++) cl->list[fill[cid[i]]++] = i;
+  free(fill); free(cid);
+  return 0;
+}
+
+static void cells_free(odo_cells* cl) { free(cl->start); free(cl->list); }
+
+/* G_i for one target i over the bins around it */
+static void ionion_cells_one(const odo_par* p, const odo_cells* cl, const double* x, int64_t i,
+                             double* g) {
+  double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+  int c0 = cell_coord(cl, 0, xi), c1 = cell_coord(cl, 1, yi), c2 = cell_coord(cl, 2, zi);
+  /* pairs with r^2 above rc^2 (1 + 1e-12) have r > rc, where pair_factor is 0: skipped */
+  const double r2max = p->rc * p->rc * (1.0 + 1e-12);
+  double gx = 0, gy = 0, gz = 0;
+  for (int bz = c2 - 2; bz <= c2 + 2; bz++) {
+    if (bz < 0 || bz >= cl->nc[2]) continue;
+    for (int by = c1 - 2; by <= c1 + 2; by++) {
+      if (by < 0 || by >= cl->nc[1]) continue;
+      for (int bx = c0 - 2; bx <= c0 + 2; bx++) {
+        if (bx < 0 || bx >= cl->nc[0]) continue;
+        int64_t c = ((int64_t)bz * cl->nc[1] + by) * cl->nc[0] + bx;
+        for (int64_t k = cl->start[c]; k < cl->start[c + 1]; k++) {
+          int64_t j = cl->list[k];
+          if (j == i) continue;
+          double dx = xi - x[3 * j], dy = yi - x[3 * j + 1], dz = zi - x[3 * j + 2];
+          double r2 = dx * dx + dy * dy + dz * dz;
+          if (r2 > r2max) continue;
+          double cc = pair_factor(p, r2);
+          gx += cc * dx; gy += cc * dy; gz += cc * dz;
+        }
+      }
+    }
+  }
+  g[0] = gx; g[1] = gy; g[2] = gz;
+}
+
 /* G_i = sum_{j != i} c(r_ij) (x_i - x_j), lambda units */
 static void ionion(const odo_par* p, int64_t n, const double* x, double* G) {
+  odo_cells cl;
+  if (p->method == OD_FORCE_CUTOFF && n > 4096 && !cells_build(p, n, x, &cl)) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; i++) ionion_cells_one(p, &cl, x, i, G + 3 * i);
+    cells_free(&cl);
+    return;
+  }
 #pragma omp parallel for schedule(dynamic, 16)
   for (int64_t i = 0; i < n; i++) {
     double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
@@ -367,10 +462,13 @@ static void collide(const odo_par* p, uint32_t ion, uint32_t step, double* v) {
   } else if (p->coll == OD_COLL_MFP) {
     /* null collision against the majorant speed vmax; an ion faster than vmax collides with
        its own probability 1 - exp(-|v| d_t / mfp) */
+    /* the branch compares against the majorant rounded to FP32, as the CUDA path stores it */
     draw(p->seed, ion, step, OD_RNG_MFP_TEST, p->sim, w);
-    double sp = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    int hit = sp <= p->vmax_mfp ? (u01(w[0]) < p->Pmax_mfp && u01(w[1]) * p->vmax_mfp < sp)
-                                : u01(w[2]) < 1.0 - exp(-sp / p->mfp_h);
+    double sp2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double vm = (double)(float)p->vmax_mfp;
+    double sp = sqrt(sp2);
+    int hit = sp2 <= vm * vm ? (u01(w[0]) < p->Pmax_mfp && u01(w[1]) * vm < sp)
+                             : u01(w[2]) < 1.0 - exp(-sp / p->mfp_h);
     if (hit) {
       double gx, gy, gz, dummy;
       draw(p->seed, ion, step, OD_RNG_MFP_GAUSS, p->sim, g);
@@ -676,6 +774,18 @@ int odo_force_targets(const od_config* c, const double* pos, int64_t n, int roun
   double* xh = (double*)malloc(sizeof(double) * 3 * n);
   to_hat(p, pos, n, round32, xh);
   double F = p->k * p->q_s * p->q_s / (p->lam * p->lam);
+  odo_cells cl;
+  if (p->method == OD_FORCE_CUTOFF && n > 4096 && !cells_build(p, n, xh, &cl)) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t t = 0; t < m; t++) {
+      double g[3];
+      ionion_cells_one(p, &cl, xh, idx[t], g);
+      force[3 * t] = F * g[0]; force[3 * t + 1] = F * g[1]; force[3 * t + 2] = F * g[2];
+    }
+    cells_free(&cl);
+    free(xh); free(p);
+    return 0;
+  }
 #pragma omp parallel for schedule(dynamic, 4)
   for (int64_t t = 0; t < m; t++) {
     int64_t i = idx[t];

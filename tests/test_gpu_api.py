@@ -59,3 +59,21 @@ def test_simulate_field_driven_and_cutoff(gpu_lib, tmp_path):
     d = od.dustParticles[0]
     assert np.allclose(d.forceExternalField[:, 2], d.q * p.E)
     assert np.isfinite(d.forceIonsOrbit).all() and np.isfinite(d.forceIonsCollect).all()
+
+
+def test_bounded_wait_runs_out_and_context_survives(gpu_lib):
+    # a wait that nothing completes gives up after its (test-only, short) poll limit and the
+    # call reports OD_ERR_TIMEOUT; an armed-and-arrived wait returns OD_OK; the context is
+    # still usable afterwards (a later engine steps normally)
+    from opendust_gb300 import _lib as L
+    lib = L.load()
+    assert lib.od_selftest_wait(0, 1000, 0) == 5          # OD_ERR_TIMEOUT
+    assert b"ran out" in lib.od_last_error(None)
+    assert lib.od_selftest_wait(0, 1000, 1) == 0
+    assert lib.od_selftest_wait(0, 0, 0) == 1          # OD_ERR_INVALID: limit out of range
+    from tests._util import case
+    holder, pos, vel, *_ = case(N=1024, n=2, seed=3)
+    with L.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        eng.step(2)
+        assert np.isfinite(eng.series()["q"]).all()

@@ -227,27 +227,3 @@ def test_autotune_picks_a_correct_plan(gpu_lib):
     idx = np.arange(0, 2**16, 64)
     ref = oracle.force_targets(holder, pos, idx, round32=True)
     assert rel_err_per_ion(f[idx], ref).max() <= 1e-5
-
-
-def test_force_snapshots_along_full_size_run(gpu_lib):
-    # C2 physics at full size (2^20 ions, mfp collisions): 10 states taken every 2 steps of a
-    # running simulation (initial state sampled on the device), each checked against the FP64
-    # oracle on 1024 random target ions x all sources (10240 targets in total)
-    from opendust_gb300 import build_simulation, workloads
-
-    plasma, sim, grains, dist, ext = workloads.full_plain(n=24)
-    holder, _ = build_simulation(plasma, sim, grains, dist, seed=13, **ext)
-    N = int(sim.N)
-    worst = 0.0
-    with _lib.Engine(holder) as eng:
-        eng.init_state()
-        for k in range(10):
-            eng.step(2)
-            pos, _ = eng.get_state()
-            f = eng.force_snapshot(pos)
-            idx = np.sort(np.random.default_rng(100 + k).choice(N, 1024, replace=False))
-            ref = oracle.force_targets(holder, pos, idx, round32=True)
-            err = rel_err_per_ion(f[idx], ref)
-            worst = max(worst, float(err.max()))
-            assert err.max() <= 1e-5, (k, err.max())
-    print(f"10 snapshots of a 2^20-ion run: worst per-ion rel err {worst:.3e}")

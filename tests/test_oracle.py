@@ -266,3 +266,21 @@ def test_mfp_collisions_of_ions_faster_than_the_majorant():
     p = collided.mean()
     expect = 1 - math.exp(-1.0)
     assert abs(p - expect) < 4 * math.sqrt(expect * (1 - expect) / N), (p, expect)
+
+
+def test_cutoff_cell_list_equals_double_loop():
+    # Above 4096 ions the oracle's cutoff force walks a cell list; at or below it, a plain double
+    # loop. Only neighbours within r_c contribute, so the force on a target from all 8000 ions
+    # (cell list) must equal the force from the subset within r_c + 0.01 lambda (double loop).
+    holder, plasma, sim, grains = _cfg(N=8000, builder=workloads.field_chain)
+    lam = plasma.r_D_e
+    pos, _ = setup_host.initial_state(8000, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
+                                      plasma.v_fl, plasma.v_T, "fieldDriven", 5)
+    rc = holder.cfg.cutoff
+    for t in (17, 4711):
+        near = np.flatnonzero(np.linalg.norm(pos - pos[t], axis=1) < rc + 0.01 * lam)
+        assert 100 < len(near) <= 4096
+        f_all = oracle.force_targets(holder, pos, [t], round32=False)[0]
+        sub = pos[near]
+        f_sub = oracle.force_targets(holder, sub, [int(np.flatnonzero(near == t)[0])], round32=False)[0]
+        np.testing.assert_allclose(f_all, f_sub, rtol=1e-11, atol=1e-12 * np.linalg.norm(f_sub))
