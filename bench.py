@@ -57,9 +57,13 @@ def parse():
     ap.add_argument("--workload", default="full_plain",
                     choices=["full_plain", "small_plain", "field_chain", "sweep", "serve"])
     ap.add_argument("--sweep-sims", type=int, default=64)
+    ap.add_argument("--sweep-exact", action="store_true")
+    ap.add_argument("--pilot-steps", type=int, default=100)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--duration", type=float, default=10.0)
     ap.add_argument("--window", type=int, default=50)
+    ap.add_argument("--log2n", default="14,19")
+    ap.add_argument("--serve-exact", action="store_true")
     ap.add_argument("--cpu-sample-targets", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -299,6 +303,11 @@ def run_ours(args, dist: Dist):
     cutoff = cut_pairs > 0
     pairs_per_launch = cut_pairs / pair_launches if cutoff else N * (N - 1)
     achieved = pairs_per_launch * FLOPS_PER_PAIR / pair_avg_s / 1e12
+    # the larger of the probe and the FP32 rate of the SMs at the sampled clock (128 FP32 lanes,
+    # 2 flops per FMA), so that a soft probe cannot inflate the fraction
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    theo = sms * 128 * 2 * (clk.get("sm_mhz") or 0.0) * 1e6 / 1e12
+    peak_used = max(peak, theo)
     n3 = not cutoff and plan["variant"] == 7
     traffic = load_traffic(N, plan, cutoff)
     if cutoff and plan["variant"] == 3:
@@ -307,7 +316,8 @@ def run_ours(args, dist: Dist):
     elif cutoff:
         kernel = "cell-list build + k_pairs_cut (pairs inside the cutoff)"
     elif n3:
-        kernel = (f"k_pairs_n3 + k_n3_reduce (each unordered pair once, {plan['jsplit']}-ion tiles; "
+        kernel = (f"k_pairs_n3 + k_n3_take (each unordered pair once, {plan['jsplit']}-ion tiles, "
+                  "fixed-point atomic sums; "
                   "credited with the N(N-1) directed pair terms it replaces)")
     else:
         kernel = f"k_pairs_x2 variant {plan['variant']} (all-pairs ion-ion)"
@@ -355,9 +365,17 @@ def run_ours(args, dist: Dist):
             "config": {**describe(args.workload, sim, ext),
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "1 GPU"},
             "pair_interactions_per_s": (pairs_per_launch * K * dist.world / (t_max * 1e-3)),
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-                         "peak_source": "FP32 FMA probe measured on this GPU in this run",
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_used, "unit": "TFLOP/s",
+                         "frac": achieved / peak_used, "traffic": traffic, "kernel": kernel,
+                         "peak_source": ("max of the FP32 FMA probe measured in this run "
+                                         f"({peak:.1f}) and {sms} SMs x 128 lanes x 2 flops at the "
+                                         f"median sampled SM clock ({theo:.1f})"),
+                         "peak_probe": peak, "peak_sm_clock": theo,
+                         # each unordered pair evaluated once: its 25 flops plus the 6 of the
+                         # reaction sum, against the directed-pair credit above
+                         "executed_frac": (None if not n3 else
+                                           N * (N - 1) / 2 * (FLOPS_PER_PAIR + 6) / pair_avg_s / 1e12
+                                           / peak_used),
                          "flops_per_pair": FLOPS_PER_PAIR, "pair_ms_avg": pair_avg_s * 1e3},
             "e2e": {"value": e2e_value, "unit": "ion-steps/s", "h2d_bytes_per_step": h2d // K_e2e,
                     "d2h_bytes_per_step": d2h // K_e2e},
@@ -371,19 +389,25 @@ def run_ours(args, dist: Dist):
 
 def run_sweep(args, dist: Dist):
     """Batched sweep (64 independent simulations drawn from seeds) against the same
-    simulations run back to back on the plain path; K steps each, wall clock, same GPU."""
+    simulations run back to back on the plain path; K steps each, wall clock, same GPU.
+
+    The batched arm first picks each member's ion–ion force interval k with
+    tuning.choose_force_interval (a pilot window of --pilot-steps steps from the member's own
+    initial state, error bound 1 % on the time-averaged grain charge and ion force), then runs
+    all members in one batch. With --sweep-exact every member keeps k = 1 (the reference's
+    integrator) and members whose plan matches the plain default are compared bitwise."""
     import numpy as np
 
-    from opendust_gb300 import _lib, build_simulation, setup_host, workloads
+    from opendust_gb300 import _lib, build_simulation, setup_host, tuning, workloads
 
     if dist.rank != 0:
         return 0
-    K, S = args.steps, args.sweep_sims
+    K, W, S = args.steps, args.warmup, args.sweep_sims
     window = 5000
     members = []
     t_setup = time.perf_counter()
     for k in range(S):
-        plasma, sim, grains, d, ext = workloads.sweep_member(seed=k, n_steps=K + args.warmup)
+        plasma, sim, grains, d, ext = workloads.sweep_member(seed=k, n_steps=K + W)
         holder, _ = build_simulation(plasma, sim, grains, d, seed=k, **ext)
         pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
                                             plasma.v_fl, plasma.v_T, d, k)
@@ -400,68 +424,130 @@ def run_sweep(args, dist: Dist):
             same_plan.append((pl["threads"], pl["targets_per_thread"], pl["variant"]) == bp[:3] and
                              (bp[2] != 7 or pl["jsplit"] == bp[3]))
             eng.set_state(pos, vel)
-            eng.step(args.warmup)
+            eng.step(W)
             t0 = time.perf_counter()
             eng.step(K)
             plain_s += time.perf_counter() - t0
-            plain_series.append(eng.series(0, K + args.warmup))
+            plain_series.append(eng.series(0, K + W))
+    # force interval per member (pilot windows), unless the exact sweep is asked for
+    t_tune = time.perf_counter()
+    intervals, pilot_err = [], []
+    for holder, pos, vel, n in members:
+        if args.sweep_exact:
+            intervals.append(1)
+            continue
+        r = tuning.choose_force_interval(holder, pos, vel, max_rel_err=0.01,
+                                         pilot_steps=args.pilot_steps)
+        intervals.append(r["force_every"])
+        pilot_err.append(max(r["errors"].values()))
+    t_tune = time.perf_counter() - t_tune
     # batched
     with _lib.Batch() as batch:
-        slots = [batch.add(h, p, v) for h, p, v, _ in members]
-        batch.step(args.warmup)
+        slots = []
+        for (h, p, v, _), k in zip(members, intervals):
+            h.cfg.force_every = k
+            slots.append(batch.add(h, p, v))
+        batch.step(W)
         t0 = time.perf_counter()
         batch.step(K)
         batch_s = time.perf_counter() - t0
         batch_dev_ms = batch.last_step_ms()
-        # members whose batch plan is their plain default must match bitwise; the others (below
-        # 2^15 ions the batch takes the each-pair-once kernel, the plain path the directed one)
-        # differ by rounding: report the largest relative difference of the grain charge
         same, qdiff = True, 0.0
-        for s, ps, sp in zip(slots, plain_series, same_plan):
-            bs = batch.member(s).series(0, K + args.warmup)
-            if sp:
+        win_q, win_f = [], []
+        for s, ps, sp, k in zip(slots, plain_series, same_plan, intervals):
+            bs = batch.member(s).series(0, K + W)
+            if k == 1 and sp:
                 same = same and all(np.array_equal(bs[q], ps[q]) for q in ps)
-            else:
+            elif k == 1:
                 qdiff = max(qdiff, float(np.max(np.abs(bs["q"] - ps["q"]) /
                                                 np.maximum(np.abs(ps["q"]), 1e-30))))
-    per_sim_window_s = lambda sec: sec / K * window / S
-    line = {"metric": "sweep sims/hour", "value": 3600.0 / per_sim_window_s(batch_s),
-            "unit": "simulations/hour (5000-step windows, 64 seeded members)",
-            "plain_value": 3600.0 / per_sim_window_s(plain_s), "ratio_batched_vs_plain": plain_s / batch_s,
-            "steps": K, "warmup": args.warmup, "batched_step_ms": batch_s / K * 1e3,
+            # time averages over the second half of the run, batched against plain
+            h0 = (K + W) // 2
+            qb, qp = bs["q"][h0:].mean(0), ps["q"][h0:].mean(0)
+            fb = (bs["orbit"] + bs["collect"])[h0:].mean(0)
+            fp = (ps["orbit"] + ps["collect"])[h0:].mean(0)
+            win_q.append(float(np.max(np.abs(qb - qp) / np.maximum(np.abs(qp), 1e-300))))
+            win_f.append(float(np.linalg.norm(fb - fp) / max(np.linalg.norm(fp), 1e-300)))
+    for h, *_ in members:
+        h.cfg.force_every = 1
+    per_window = lambda sec: sec / K * window / S
+    tune_per_sim = t_tune / S
+    ks, counts = np.unique(intervals, return_counts=True)
+    line = {"metric": "sweep sims/hour", "unit": "simulations/hour (5000-step windows, 64 seeded members)",
+            "value": 3600.0 / (per_window(batch_s) + tune_per_sim),
+            "plain_value": 3600.0 / per_window(plain_s),
+            "ratio_batched_vs_plain": per_window(plain_s) / (per_window(batch_s) + tune_per_sim),
+            "ratio_steps_only": plain_s / batch_s,
+            "steps": K, "warmup": W, "batched_step_ms": batch_s / K * 1e3,
             "batched_device_step_ms": batch_dev_ms / K, "plain_step_ms_sum": plain_s / K * 1e3,
             "ion_steps_per_s_batched": ion_steps / batch_s, "ion_steps_per_s_plain": ion_steps / plain_s,
-            "results_equal_bitwise": bool(same),
-            "bitwise_members": f"{sum(same_plan)} of {S} (same plan in both arms)",
-            "q_rel_diff_other_members": qdiff,
+            "tuning_s": t_tune, "pilot_steps": args.pilot_steps,
+            "force_every": {str(int(a)): int(b) for a, b in zip(ks, counts)},
+            "pilot_max_rel_err": max(pilot_err) if pilot_err else 0.0,
+            "window_rel_err_vs_plain": {"q_max": max(win_q), "force_max": max(win_f),
+                                        "force_median": float(np.median(win_f)),
+                                        "steps_averaged": (K + W) - (K + W) // 2},
+            "results_equal_bitwise_k1": bool(same),
+            "bitwise_members": f"{sum(sp and k == 1 for sp, k in zip(same_plan, intervals))} of {S}",
+            "q_rel_diff_other_k1_members": qdiff,
             "host_setup_s": t_setup, "n_ions": [int(m[3]) for m in members],
             "config": {"workload": "sweep: 64 members, N log-uniform 2^14-2^18, Mach 0.1-2, grain radius "
-                                   "1-20 um log-uniform, 1-4 grains, mfp collisions with p=0.5"}}
+                                   "1-20 um log-uniform, 1-4 grains, mfp collisions with p=0.5",
+                       "batched": "exact (k = 1)" if args.sweep_exact else
+                                  "ion-ion force interval per member (pilot-tuned, 1 % bound)"}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 def run_serve(args, dist: Dist):
-    """Poisson request stream through the continuous-batching server vs the plain path."""
+    """Poisson request stream through the continuous-batching server vs the plain path. Both
+    arms get the same process pool for the host part of each request's setup, so the ratio
+    measures what the GPU co-scheduling buys. The server runs every request with the ion–ion
+    force interval of serve.interval_by_size (or every step with --serve-exact); each request's
+    time-averaged charge and ion force are compared with the plain path's."""
     import copy
+
+    import numpy as np
 
     from opendust_gb300 import serve
 
     if dist.rank != 0:
         return 0
-    reqs = serve.poisson_requests(rate=args.rate, duration=args.duration, seed=7, log2n=(14, 16),
+    lo, hi = (float(x) for x in args.log2n.split(","))
+    reqs = serve.poisson_requests(rate=args.rate, duration=args.duration, seed=7, log2n=(lo, hi),
                                   window=args.window)
     pool = serve.start_pool(8)
-    list(pool.map(int, range(8)))  # start the workers before the timed run
-    s = serve.Server(chunk=10).run(copy.deepcopy(reqs), pool=pool)
+    list(pool.map(int, range(8)))  # start the workers before the timed runs
+    interval = None if args.serve_exact else serve.interval_by_size
+    served = copy.deepcopy(reqs)
+    s = serve.Server(chunk=10, interval=interval).run(served, pool=pool)
+    plain_reqs = copy.deepcopy(reqs)
+    p = serve.run_plain(plain_reqs, pool=pool)
     pool.shutdown()
-    p = serve.run_plain(copy.deepcopy(reqs))
+    eq, dq, df = True, [], []
+    for a, b in zip(sorted(served, key=lambda r: r.rid), sorted(plain_reqs, key=lambda r: r.rid)):
+        qa, qb = a.averages[:, 0], b.averages[:, 0]
+        fa, fb = a.averages[:, 1:4] + a.averages[:, 4:7], b.averages[:, 1:4] + b.averages[:, 4:7]
+        dq.append(float(np.max(np.abs(qa - qb) / np.maximum(np.abs(qb), 1e-300))))
+        df.append(float(np.linalg.norm(fa - fb) / max(np.linalg.norm(fb), 1e-300)))
+        eq = eq and all(np.array_equal(a.series[k], b.series[k]) for k in a.series)
+    ks = [interval(int(r.sim.N)) if interval else 1 for r in reqs]
     line = {"metric": "request latency p99 (s)", "value": s["latency_p99_s"], "unit": "s",
             "higher_is_better": False, "server": s, "plain": p,
             "throughput_ratio_server_vs_plain": s["throughput_req_per_s"] / p["throughput_req_per_s"],
+            "ion_steps_ratio_server_vs_plain": s["ion_steps_per_s"] / p["ion_steps_per_s"],
+            "rel_err_vs_plain": {"q_max": max(dq), "force_max": max(df),
+                                 "force_median": float(np.median(df))},
+            "results_equal_bitwise": bool(eq),
+            "force_every": {str(k): ks.count(k) for k in sorted(set(ks))},
+            "n_ions": [int(r.sim.N) for r in reqs],
             "config": {"workload": f"serve: Poisson {args.rate}/s for {args.duration} s, N log-uniform "
-                                   f"2^14-2^16, 1-8 grains, Mach 0.1-2, Maxwellian or field-driven, "
-                                   f"{args.window}-step windows, 80% HBM budget"}}
+                                   f"2^{lo:g}-2^{hi:g}, 1-8 grains, Mach 0.1-2, Maxwellian or "
+                                   f"field-driven, {args.window}-step windows (averages over the "
+                                   f"second half), 80% HBM budget; host setup in an 8-process pool "
+                                   f"for both arms",
+                       "served": "every step" if args.serve_exact else
+                                 "ion-ion force interval by size (serve.interval_by_size)"}}
     print(json.dumps(line), flush=True)
     return 0
 

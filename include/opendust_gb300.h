@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 2
+#define OD_ABI_VERSION 3
 
 typedef enum od_status {
   OD_OK = 0,
@@ -168,6 +168,16 @@ typedef struct od_config {
    * matthews.py:978-1007; NULL: zero). */
   const double* grain_field;
   const double* grain_out;
+  /* Ion–ion force interval k (no counterpart in the reference, whose integrator evaluates the
+   * ion–ion force every step, opendust.py:864-877). 0 or 1: every step, the reference's
+   * integrator. k > 1: impulse multiple time stepping: the ion–ion force is evaluated at the
+   * end of steps k-1, 2k-1, ... (step index s with s % k == k - 1) and applied as a half kick
+   * of k times its size at the end of that step and at the start of the next; the other steps
+   * move the ions under the grain, trap and field forces only. Between evaluations the stored
+   * ion–ion sums still follow re-injection (removed ions' terms out, new ions' terms in). An
+   * approximation that cuts pair work by k: use it where its error on the quantities of
+   * interest has been measured (opendust_gb300.tuning.choose_force_interval). */
+  int32_t force_every;
 } od_config;
 
 typedef struct od_handle od_handle;
@@ -284,6 +294,47 @@ od_status od_get_pair_plan(const od_handle* h, int32_t* plan5);
 /* FP32 FMA throughput of the device in TFLOP/s (2 flops per FMA), measured by a short probe
  * kernel: the denominator of the all-pairs kernel's roofline. */
 od_status od_probe_fp32_peak(int32_t device, double* tflops);
+/* ---- Shards of one simulation (replaces the reference's multi-GPU OpenMM context:
+ * Platform property DeviceIndex "0,1,..." of opendust.py:1040-1042, timed by
+ * performance/MultipleGPU/benchmark.py:83). One handle per GPU owns the ions [first,
+ * first + count) of a simulation of cfg->n_ions ions (first a multiple of 512, count a multiple
+ * of 512 except for the last shard); every shard keeps all positions as sources. A step is five
+ * calls per shard with three all-gathers between them (the caller moves the data: MPI, NCCL,
+ * torch.distributed, or plain copies; pointers may be host or device memory):
+ *   od_shard_begin       kick and drift of the shard's ions; writes their positions, 3 x count
+ *                        floats (x, then y, then z; units of r_D_e), to xyz_out
+ *   all-gather           -> xyz_all, 3 x n_ions floats, shards in order
+ *   od_shard_forces      ion–ion sums of the shard's ions over all positions, kick, flags, the
+ *                        shard's ordered compaction and re-injection; *n_list = its entries
+ *   od_shard_get_list    the shard's entries: global index, flag bits, position before and
+ *                        after re-injection and velocity (float4 each, units of r_D_e, d_t)
+ *   all-gather           -> the run's list, shards in order (= increasing global index)
+ *   od_shard_set_list    grain sums over the run's list, the re-injected positions, correction
+ *                        and orbit sums of the shard's ions; writes the shard's orbit partial
+ *                        sums (orbit_blocks x P x 3 doubles, od_shard_info) to orbit_out
+ *   all-gather           -> orbit_all, every shard's partials in order
+ *   od_shard_finish      the FP64 tail (charges, forces, series); every shard holds the series
+ * All ion–ion sums use the directed all-pairs plan of a single simulation of n_ions ions
+ * (variant 5, the source split of jsplit chunks, 0: the default), and every sum keeps the
+ * single-simulation order: the shards' results equal those of one handle with that plan, bit for
+ * bit. All-pairs force, force_every <= 1, Maxwellian or field-driven ions only
+ * (OD_ERR_UNSUPPORTED otherwise). Calls out of order return OD_ERR_STATE. */
+od_status od_shard_create(const od_config* cfg, int64_t first, int64_t count, int32_t jsplit,
+                          int32_t device, od_handle** out);
+/* pos_all: n_ions x 3 positions of the whole run (m); vel_own: count x 3 velocities of the
+ * shard's ions (m/s). Computes the initial ion–ion sums (as od_set_state). */
+od_status od_shard_set_state(od_handle* h, const double* pos_all, const double* vel_own);
+od_status od_shard_begin(od_handle* h, float* xyz_out);
+od_status od_shard_forces(od_handle* h, const float* xyz_all, int64_t* n_list);
+od_status od_shard_get_list(od_handle* h, int32_t* idx, int32_t* bits, float* old4, float* new4,
+                            float* v4);
+od_status od_shard_set_list(od_handle* h, int64_t n, const int32_t* idx, const int32_t* bits,
+                            const float* old4, const float* new4, const float* v4,
+                            double* orbit_out);
+od_status od_shard_finish(od_handle* h, const double* orbit_all);
+od_status od_shard_info(const od_handle* h, int64_t* first, int64_t* count, int64_t* n_total,
+                        int64_t* orbit_blocks);
+
 /* Self test of the bounded device waits (no counterpart in the reference, whose OpenMM waits
  * are unbounded). One thread on `device` arms an mbarrier and waits on it with the same wait
  * routine the step kernels use, but with `limit` polls (1 to 2^26) instead of 2^26. With

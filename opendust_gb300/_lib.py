@@ -12,7 +12,7 @@ from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint32, c_ui
 
 import numpy as np
 
-OD_ABI_VERSION = 2
+OD_ABI_VERSION = 3
 OD_MAX_GRAINS = 16
 OD_MAX_TABLE = 256
 OD_NTAB = 4
@@ -100,6 +100,7 @@ class od_config(ctypes.Structure):
         ("trap_tab", _DP),
         ("grain_field", _DP),
         ("grain_out", _DP),
+        ("force_every", c_int32),
     ]
 
 
@@ -152,6 +153,17 @@ def load(path: str | None = None):
         "od_get_cutoff_pairs": (c_int32, [H, POINTER(c_int64)]),
         "od_probe_fp32_peak": (c_int32, [c_int32, _DP]),
         "od_selftest_wait": (c_int32, [c_int32, c_uint32, c_int32]),
+        "od_shard_create": (c_int32, [POINTER(od_config), c_int64, c_int64, c_int32, c_int32,
+                                      POINTER(c_void_p)]),
+        "od_shard_set_state": (c_int32, [H, _DP, _DP]),
+        "od_shard_begin": (c_int32, [H, c_void_p]),
+        "od_shard_forces": (c_int32, [H, c_void_p, POINTER(c_int64)]),
+        "od_shard_get_list": (c_int32, [H, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+        "od_shard_set_list": (c_int32, [H, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
+        "od_shard_finish": (c_int32, [H, c_void_p]),
+        "od_shard_info": (c_int32, [H, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64),
+                                    POINTER(c_int64)]),
         "od_set_pair_plan": (c_int32, [H, c_int32, c_int32, c_int32, c_int32]),
         "od_get_pair_plan": (c_int32, [H, POINTER(c_int32)]),
         "od_autotune": (c_int32, [H, c_int32, _DP]),
@@ -241,6 +253,7 @@ def make_config(
     trap_none: bool = False,
     grain_field=None,
     grain_out=None,
+    force_every: int = 1,
 ) -> ConfigHolder:
     """Fill an od_config from plain Python/numpy values (SI units). field: order-2 field of the
     chains/matthews.py fork {"order", "alpha", "beta", "z1", "z7"}; trap_table: (5, n) alpha_k
@@ -251,6 +264,7 @@ def make_config(
     c.distribution = distribution
     c.collision_model = collision_model
     c.force_method = force_method
+    c.force_every = int(force_every)
     c.n_ions = int(n_ions)
     c.n_steps = int(n_steps)
     c.avg_start = int(avg_start)

@@ -39,6 +39,9 @@ struct od_handle {
   // CUDA graph of one step (production path)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  // force interval k > 1: the step graph without the ion–ion launch (steps that do not evaluate)
+  cudaGraph_t graph_nf = nullptr;
+  cudaGraphExec_t graph_exec_nf = nullptr;
   bool use_graph = true;
   // device timing (events on the handle's stream)
   bool timing = false;
@@ -47,6 +50,14 @@ struct od_handle {
   std::vector<std::pair<int, int>> ev_step, ev_pair;  // indices into ev_pool
   double t_step_ms = 0, t_pair_ms = 0;
   int64_t t_steps = 0, t_pair_launches = 0;
+  // shard of a larger simulation (od_shard_create): ions ion0 .. ion0 + N of n_total
+  bool shard = false;
+  int64_t ion0 = 0, n_total = 0;
+  int Npad_total = 0, shard_phase = 0;
+  float *ssx = nullptr, *ssy = nullptr, *ssz = nullptr;  // [Npad_total] every shard's positions
+  int32_t *g_idx = nullptr, *g_bits = nullptr;            // [n_total] the run's list
+  float4 *g_old = nullptr, *g_new = nullptr, *g_v = nullptr;
+  double* g_orbit = nullptr;                              // [Npad_total / 256][P][3]
   std::string err;
 };
 
@@ -129,6 +140,10 @@ static od_status validate(const od_config* c) {
     return fail(nullptr, OD_ERR_INVALID, "unknown force method");
   if (c->force_method == OD_FORCE_CUTOFF && !(c->cutoff > 0))
     return fail(nullptr, OD_ERR_INVALID, "cutoff method needs cutoff > 0");
+  if (c->force_every < 0 || c->force_every > 1024)
+    return fail(nullptr, OD_ERR_INVALID, "force_every must be in [0, 1024]");
+  if (c->force_every > 1 && c->distribution == OD_DIST_MATTHEWS)
+    return fail(nullptr, OD_ERR_INVALID, "force_every > 1 is not available for the fork's model");
   if (!(c->r_D_e > 0) || !(c->d_t > 0) || !(c->R > 0) || !(c->H > 0) || !(c->N_s > 0))
     return fail(nullptr, OD_ERR_INVALID, "r_D_e, d_t, R, H and N_s must be positive");
   for (int t = 0; t < OD_NTAB; t++) {
@@ -195,6 +210,7 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->N = N; p->Npad = Npad; p->P = c->n_grains; p->dist = c->distribution;
   p->coll = c->collision_model; p->method = c->force_method; p->sim = c->sim_id;
   p->nwords = Npad / 32;
+  p->force_every = c->force_every > 1 ? c->force_every : 1;
   p->seed_lo = (uint32_t)(c->seed & 0xffffffffu);
   p->seed_hi = (uint32_t)(c->seed >> 32);
   const double lam = c->r_D_e, dt = c->d_t;
@@ -323,6 +339,8 @@ static void free_all(od_handle* h) {
   free_cutn3(h);
   if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  if (h->graph_exec_nf) { cudaGraphExecDestroy(h->graph_exec_nf); h->graph_exec_nf = nullptr; }
+  if (h->graph_nf) { cudaGraphDestroy(h->graph_nf); h->graph_nf = nullptr; }
   free_timing(h);
   void* ptrs[] = {h->dp, h->ds, h->b.pos, h->b.vel, h->b.fhi, h->b.flo, h->b.part_hi, h->b.part_lo,
                   h->b.flags, h->b.list, h->b.list_bits, h->b.list_old, h->b.list_new, h->b.list_v,
@@ -330,7 +348,8 @@ static void free_all(od_handle* h) {
                   h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
                   h->b.sx, h->b.sy, h->b.sz, h->cut.cell_of, h->cut.count, h->cut.fill,
                   h->cut.start, h->cut.chunk_prefix, h->cut.perm, h->cut.ox, h->cut.oy, h->cut.oz,
-                  h->cut.stencil, h->d_pairs, h->cut.chunk_prefix2, h->b.n3};
+                  h->cut.stencil, h->d_pairs, h->cut.chunk_prefix2, h->b.n3, h->ssx, h->ssy,
+                  h->ssz, h->g_idx, h->g_bits, h->g_old, h->g_new, h->g_v, h->g_orbit};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -701,6 +720,12 @@ extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_
   return OD_OK;
 }
 
+// Does step `step` evaluate the ion–ion force (force interval k = cfg.force_every)?
+static bool step_evaluates(const od_handle* h, int64_t step) {
+  const int k = h->cfg.force_every;
+  return k <= 1 || step % k == k - 1;
+}
+
 static od_status event_at(od_handle* h, size_t slot, int* idx) {
   while (h->ev_pool.size() <= slot) {
     cudaEvent_t e;
@@ -725,18 +750,20 @@ static od_status step_timed(od_handle* h, int64_t nsteps) {
       return OD_ERR_CUDA;
     OD_CK(h, cudaEventRecord(h->ev_pool[a], h->stream));
     const int nb = h->Npad / 256;
+    const bool eval = step_evaluates(h, h->step + s);
     OD_CK(h, od_launch_step_part(0, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
                                  h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[c], h->stream));
-    OD_CK(h, od_launch_step_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
-                                 h->stream));
+    if (eval)
+      OD_CK(h, od_launch_step_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
+                                   h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[d], h->stream));
     OD_CK(h, od_launch_step_part(2, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
                                  h->stream));
     OD_CK(h, cudaEventRecord(h->ev_pool[b], h->stream));
     (void)nb;
     h->ev_step.push_back({a, b});
-    h->ev_pair.push_back({c, d});
+    if (eval) h->ev_pair.push_back({c, d});
   }
   OD_CK(h, cudaStreamSynchronize(h->stream));
   for (auto& p : h->ev_step) {
@@ -754,18 +781,35 @@ static od_status step_timed(od_handle* h, int64_t nsteps) {
   return OD_OK;
 }
 
-static od_status ensure_graph(od_handle* h) {
-  if (h->graph_exec) return OD_OK;
+// One step's launches; `with_force` false leaves out the ion–ion launch (part 1).
+static cudaError_t launch_step_parts(od_handle* h, const od_force_ctx& fc, bool with_force) {
+  for (int part = 0; part < 3; part++) {
+    if (part == 1 && !with_force) continue;
+    cudaError_t e = od_launch_step_part(part, h->dp, h->ds, h->b, h->N, h->Npad, h->P, fc, h->nrec,
+                                        h->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+static od_status capture_step(od_handle* h, bool with_force, cudaGraph_t* graph,
+                              cudaGraphExec_t* exec) {
+  if (*exec) return OD_OK;
   OD_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, force_ctx(h, false),
-                                 h->nrec, h->stream);
+  cudaError_t e = launch_step_parts(h, force_ctx(h, false), with_force);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(h, e, "step capture"); }
   if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
-  h->graph = g;
-  OD_CK(h, cudaGraphInstantiate(&h->graph_exec, g, 0));
+  *graph = g;
+  OD_CK(h, cudaGraphInstantiate(exec, g, 0));
   return OD_OK;
+}
+
+static od_status ensure_graph(od_handle* h) {
+  od_status st = capture_step(h, true, &h->graph, &h->graph_exec);
+  if (st != OD_OK || h->cfg.force_every <= 1) return st;
+  return capture_step(h, false, &h->graph_nf, &h->graph_exec_nf);
 }
 
 extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
@@ -781,11 +825,12 @@ extern "C" od_status od_step(od_handle* h, int64_t nsteps) {
   } else if (h->use_graph) {
     od_status st = ensure_graph(h);
     if (st != OD_OK) return st;
-    for (int64_t s = 0; s < nsteps; s++) OD_CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+    for (int64_t s = 0; s < nsteps; s++)
+      OD_CK(h, cudaGraphLaunch(step_evaluates(h, h->step + s) ? h->graph_exec : h->graph_exec_nf,
+                               h->stream));
   } else {
     for (int64_t s = 0; s < nsteps; s++)
-      OD_CK(h, od_launch_step(h->dp, h->ds, h->b, h->N, h->Npad, h->P, force_ctx(h, false), h->nrec,
-                              h->stream));
+      OD_CK(h, launch_step_parts(h, force_ctx(h, false), step_evaluates(h, h->step + s)));
   }
   h->step += nsteps;
   return check_device_err(h);
@@ -846,7 +891,7 @@ static void free_cutn3(od_handle* h) {
   od_cutn3* L = h->cut.n3;
   if (!L) return;
   void* ptrs[] = {L->cell_of, L->count, L->fill, L->start, L->perm, L->xs, L->ys, L->zs,
-                  L->box, L->gbox, L->adj, L->rowptr, L->pairs, L->S};
+                  L->box, L->gbox, L->adj, L->rowptr, L->pairs, L->acc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete L;
@@ -892,7 +937,8 @@ static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   if (e == cudaSuccess) e = al(&L->adj, nT * L->nwords);
   if (e == cudaSuccess) e = al(&L->rowptr, nT + 1);
   if (e == cudaSuccess) e = al(&L->pairs, nT * (nT + 1) / 2);
-  if (e == cudaSuccess) e = al(&L->S, nT * nT * 6 * (size_t)T);
+  if (e == cudaSuccess) e = al(&L->acc, 3 * ns);
+  if (e == cudaSuccess) e = cudaMemset(L->acc, 0, sizeof(unsigned long long) * 3 * ns);
   if (e != cudaSuccess) {
     cudaGetLastError();
     free_cutn3(h);
@@ -914,6 +960,8 @@ static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
 static void drop_graph(od_handle* h) {
   if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  if (h->graph_exec_nf) { cudaGraphExecDestroy(h->graph_exec_nf); h->graph_exec_nf = nullptr; }
+  if (h->graph_nf) { cudaGraphDestroy(h->graph_nf); h->graph_nf = nullptr; }
 }
 
 static void free_n3(od_handle* h) {
@@ -922,9 +970,8 @@ static void free_n3(od_handle* h) {
 }
 
 // Variant 7: `ions_per_lane` targets per lane (2 or 4 with as many sources, 8 with two sources),
-// `tile` ions per tile (1024, 2048, 4096; <= 0: the smallest supported tile whose matrix fits
-// OD_N3_BUDGET, 1024 only up to 2^17 ions). The tile-pair matrix holds 24 bytes per ion and tile
-// (12.9 GB at 2^20 ions with 2048-ion tiles).
+// `tile` ions per tile (1024, 2048, 4096; <= 0: 1024 up to 2^17 ions, else 2048). The pair
+// sums go to three 64-bit fixed-point accumulators per ion (24 bytes per ion: 25 MB at 2^20).
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile) {
   if (!plan_supported(256, ions_per_lane, 7))
     return fail(h, OD_ERR_INVALID, "variant 7 takes 2, 4 or 8 targets per lane");
@@ -949,9 +996,11 @@ static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile) {
     if (cudaMalloc((void**)&h->b.n3, sizeof(float) * need) != cudaSuccess) {
       cudaGetLastError();
       h->b.n3 = nullptr;
-      return fail(h, OD_ERR_OOM, "no device memory for the variant-7 tile-pair sums");
+      return fail(h, OD_ERR_OOM, "no device memory for the variant-7 accumulators");
     }
     h->b.n3_len = need;
+    // the accumulators start at zero; every evaluation clears them after reading them
+    OD_CK(h, cudaMemset(h->b.n3, 0, sizeof(float) * need));
   }
   h->plan = pl;  // one partial slab: part_hi/part_lo always hold at least one
   drop_graph(h);
@@ -982,6 +1031,8 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
     h->cut.packed = variant == 2;
     if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
     if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+    if (h->graph_exec_nf) { cudaGraphExecDestroy(h->graph_exec_nf); h->graph_exec_nf = nullptr; }
+    if (h->graph_nf) { cudaGraphDestroy(h->graph_nf); h->graph_nf = nullptr; }
     return OD_OK;
   }
   if (!plan_supported(threads, targets_per_thread, variant))
@@ -1008,6 +1059,8 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
   if (grow && alloc_scratch_for_plan(h) != OD_OK) return OD_ERR_OOM;
   if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
   if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  if (h->graph_exec_nf) { cudaGraphExecDestroy(h->graph_exec_nf); h->graph_exec_nf = nullptr; }
+  if (h->graph_nf) { cudaGraphDestroy(h->graph_nf); h->graph_nf = nullptr; }
   return OD_OK;
 }
 
@@ -1703,5 +1756,226 @@ extern "C" od_status od_device_memory(int32_t device, int64_t* free_bytes, int64
   if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaMemGetInfo");
   *free_bytes = (int64_t)f;
   *total_bytes = (int64_t)t;
+  return OD_OK;
+}
+
+// ============================================================== shards of one simulation
+// One simulation split over several handles (one per GPU), each owning a contiguous range of
+// ions; the caller moves three things between the shards every step (all-gathers: positions,
+// re-injection lists, orbit partial sums). Every sum keeps the single-simulation order, so the
+// shards reproduce a single handle stepped with the same directed all-pairs plan bit for bit.
+static od_status shard_check(od_handle* h, int phase) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!h->shard) return fail(h, OD_ERR_STATE, "not a shard handle (od_shard_create)");
+  if (!h->state_set) return fail(h, OD_ERR_STATE, "od_shard_set_state has not been called");
+  if (phase >= 0 && h->shard_phase != phase)
+    return fail(h, OD_ERR_STATE, "shard calls out of order (begin, positions, forces, list, "
+                                 "finish)");
+  if (h->step >= h->cfg.n_steps) return fail(h, OD_ERR_STATE, "the result series is full");
+  OD_CK(h, cudaSetDevice(h->device));
+  return OD_OK;
+}
+
+extern "C" od_status od_shard_create(const od_config* cfg, int64_t first, int64_t count,
+                                     int32_t jsplit, int32_t device, od_handle** out) {
+  if (!cfg || !out) return fail(nullptr, OD_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  od_status st = validate(cfg);
+  if (st != OD_OK) return st;
+  const int64_t Nt = cfg->n_ions;
+  if (cfg->force_method != OD_FORCE_ALLPAIRS || cfg->force_every > 1 ||
+      cfg->distribution == OD_DIST_MATTHEWS)
+    return fail(nullptr, OD_ERR_UNSUPPORTED,
+                "shards take the all-pairs force, every step, Maxwellian or field-driven ions");
+  if (first < 0 || count < 1 || first + count > Nt || first % OD_PAD ||
+      (first + count < Nt && count % OD_PAD))
+    return fail(nullptr, OD_ERR_INVALID,
+                "a shard starts on a multiple of 512 ions and holds a multiple of 512 (the last "
+                "shard: the rest)");
+  od_config local = *cfg;
+  local.n_ions = count;
+  st = create_handle(&local, device, false, out);
+  if (st != OD_OK) return st;
+  od_handle* h = *out;
+  h->shard = true;
+  h->ion0 = first;
+  h->n_total = Nt;
+  h->Npad_total = (int)(((Nt + OD_PAD - 1) / OD_PAD) * OD_PAD);
+  h->hp.ion0 = (int32_t)first;
+  // the directed plan of a single simulation of n_total ions (variant 5, the source split over
+  // all sources), or jsplit source chunks when given
+  od_pair_plan pl = default_plan(h->Npad_total, od_num_sms(device));
+  if (jsplit > 0) {
+    int chunk = (h->Npad_total + jsplit - 1) / jsplit;
+    chunk = ((chunk + OD_TJ - 1) / OD_TJ) * OD_TJ;
+    pl.chunk = chunk;
+    pl.jsplit = (h->Npad_total + chunk - 1) / chunk;
+  }
+  h->plan = pl;
+  auto bad = [&](const char* what) {
+    od_status r = fail(h, OD_ERR_OOM, what);
+    std::string m = h->err;
+    od_destroy(h);
+    *out = nullptr;
+    g_err = m;
+    return r;
+  };
+  if (alloc_scratch_for_plan(h) != OD_OK) return bad("no device memory for the partial sums");
+  const size_t nt = (size_t)h->Npad_total, P = std::max(h->P, 1);
+  if (dalloc(&h->ssx, nt) || dalloc(&h->ssy, nt) || dalloc(&h->ssz, nt) ||
+      dalloc(&h->g_idx, (size_t)Nt) || dalloc(&h->g_bits, (size_t)Nt) ||
+      dalloc(&h->g_old, (size_t)Nt) || dalloc(&h->g_new, (size_t)Nt) ||
+      dalloc(&h->g_v, (size_t)Nt) || dalloc(&h->g_orbit, nt / 256 * P * 3)) {
+    cudaGetLastError();
+    return bad("no device memory for the shard's sources");
+  }
+  if (nt > (size_t)Nt) {  // padding sources: far-away sentinels
+    std::vector<float> sent(nt - Nt, OD_SENTINEL);
+    for (float* a : {h->ssx, h->ssy, h->ssz})
+      if (cudaMemcpy(a + Nt, sent.data(), sizeof(float) * (nt - Nt), cudaMemcpyHostToDevice))
+        return bad("sentinel upload");
+  }
+  if (cudaMemcpy(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bad("parameter upload");
+  return OD_OK;
+}
+
+static od_status shard_forces_now(od_handle* h) {
+  OD_CK(h, od_launch_shard_pairs(h->plan, h->ssx, h->ssy, h->ssz, h->Npad_total, h->Npad,
+                                 (int)h->ion0, h->b.part_hi, h->b.part_lo, h->hp.rho0, &h->ds->err,
+                                 h->stream));
+  return OD_OK;
+}
+
+extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
+                                        const double* vel_own) {
+  if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
+  if (!h->shard) return fail(h, OD_ERR_STATE, "not a shard handle (od_shard_create)");
+  if (!pos_all || !vel_own) return fail(h, OD_ERR_INVALID, "pos_all/vel_own is NULL");
+  OD_CK(h, cudaSetDevice(h->device));
+  std::vector<float4> xa, vp, xo;
+  to_device_units(h, pos_all, nullptr, h->n_total, xa, nullptr);
+  to_device_units(h, pos_all + 3 * h->ion0, vel_own, h->N, xo, &vp);
+  std::vector<float> c(h->n_total);
+  float* dst[3] = {h->ssx, h->ssy, h->ssz};
+  for (int d = 0; d < 3; d++) {
+    for (int64_t i = 0; i < h->n_total; i++) c[i] = d == 0 ? xa[i].x : (d == 1 ? xa[i].y : xa[i].z);
+    OD_CK(h, cudaMemcpy(dst[d], c.data(), sizeof(float) * h->n_total, cudaMemcpyHostToDevice));
+  }
+  OD_CK(h, cudaMemcpy(h->b.pos, xo.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
+  OD_CK(h, cudaMemcpy(h->b.vel, vp.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
+  od_status st = shard_forces_now(h);
+  if (st != OD_OK) return st;
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->b.fhi,
+                            h->b.flo, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->state_set = true;
+  h->shard_phase = 0;
+  return check_device_err(h);
+}
+
+extern "C" od_status od_shard_begin(od_handle* h, float* xyz_out) {
+  od_status st = shard_check(h, 0);
+  if (st != OD_OK) return st;
+  if (!xyz_out) return fail(h, OD_ERR_INVALID, "xyz_out is NULL");
+  float* own[3] = {h->ssx + h->ion0, h->ssy + h->ion0, h->ssz + h->ion0};
+  OD_CK(h, od_launch_shard_part(0, h->dp, h->ds, h->b, h->N, h->Npad, h->plan.jsplit, own[0],
+                                own[1], own[2], h->stream));
+  for (int d = 0; d < 3; d++)
+    OD_CK(h, cudaMemcpyAsync(xyz_out + (size_t)d * h->N, own[d], sizeof(float) * h->N,
+                             cudaMemcpyDefault, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->shard_phase = 1;
+  return OD_OK;
+}
+
+extern "C" od_status od_shard_forces(od_handle* h, const float* xyz_all, int64_t* n_list) {
+  od_status st = shard_check(h, 1);
+  if (st != OD_OK) return st;
+  if (!xyz_all || !n_list) return fail(h, OD_ERR_INVALID, "NULL argument");
+  float* dst[3] = {h->ssx, h->ssy, h->ssz};
+  for (int d = 0; d < 3; d++)
+    OD_CK(h, cudaMemcpyAsync(dst[d], xyz_all + (size_t)d * h->n_total, sizeof(float) * h->n_total,
+                             cudaMemcpyDefault, h->stream));
+  st = shard_forces_now(h);
+  if (st != OD_OK) return st;
+  OD_CK(h, od_launch_shard_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->plan.jsplit, nullptr,
+                                nullptr, nullptr, h->stream));
+  int32_t K = 0;
+  OD_CK(h, cudaMemcpyAsync(&K, &h->ds->nlist, sizeof(K), cudaMemcpyDeviceToHost, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  *n_list = K;
+  h->shard_phase = 2;
+  return check_device_err(h);
+}
+
+extern "C" od_status od_shard_get_list(od_handle* h, int32_t* idx, int32_t* bits, float* old4,
+                                       float* new4, float* v4) {
+  od_status st = shard_check(h, 2);
+  if (st != OD_OK) return st;
+  if (!idx || !bits || !old4 || !new4 || !v4) return fail(h, OD_ERR_INVALID, "NULL argument");
+  int32_t K = 0;
+  OD_CK(h, cudaMemcpy(&K, &h->ds->nlist, sizeof(K), cudaMemcpyDeviceToHost));
+  if (K == 0) return OD_OK;
+  std::vector<int32_t> li(K);
+  OD_CK(h, cudaMemcpy(li.data(), h->b.list, sizeof(int32_t) * K, cudaMemcpyDeviceToHost));
+  for (auto& i : li) i += (int32_t)h->ion0;  // global indices
+  OD_CK(h, cudaMemcpy(idx, li.data(), sizeof(int32_t) * K, cudaMemcpyDefault));
+  OD_CK(h, cudaMemcpy(bits, h->b.list_bits, sizeof(int32_t) * K, cudaMemcpyDefault));
+  OD_CK(h, cudaMemcpy(old4, h->b.list_old, sizeof(float4) * K, cudaMemcpyDefault));
+  OD_CK(h, cudaMemcpy(new4, h->b.list_new, sizeof(float4) * K, cudaMemcpyDefault));
+  OD_CK(h, cudaMemcpy(v4, h->b.list_v, sizeof(float4) * K, cudaMemcpyDefault));
+  return OD_OK;
+}
+
+extern "C" od_status od_shard_set_list(od_handle* h, int64_t n, const int32_t* idx,
+                                       const int32_t* bits, const float* old4, const float* new4,
+                                       const float* v4, double* orbit_out) {
+  od_status st = shard_check(h, 2);
+  if (st != OD_OK) return st;
+  if (n < 0 || n > h->n_total) return fail(h, OD_ERR_INVALID, "list longer than the run");
+  if (!orbit_out || (n > 0 && (!idx || !bits || !old4 || !new4 || !v4)))
+    return fail(h, OD_ERR_INVALID, "NULL argument");
+  if (n > 0) {
+    OD_CK(h, cudaMemcpyAsync(h->g_idx, idx, sizeof(int32_t) * n, cudaMemcpyDefault, h->stream));
+    OD_CK(h, cudaMemcpyAsync(h->g_bits, bits, sizeof(int32_t) * n, cudaMemcpyDefault, h->stream));
+    OD_CK(h, cudaMemcpyAsync(h->g_old, old4, sizeof(float4) * n, cudaMemcpyDefault, h->stream));
+    OD_CK(h, cudaMemcpyAsync(h->g_new, new4, sizeof(float4) * n, cudaMemcpyDefault, h->stream));
+    OD_CK(h, cudaMemcpyAsync(h->g_v, v4, sizeof(float4) * n, cudaMemcpyDefault, h->stream));
+  }
+  OD_CK(h, od_launch_shard_list(h->dp, h->ds, (int)n, h->g_idx, h->g_bits, h->g_new, h->g_v,
+                                h->ssx, h->ssy, h->ssz, h->stream));
+  OD_CK(h, od_launch_shard_correct(h->dp, h->ds, h->b, h->Npad, h->nrec, h->g_idx, h->g_old,
+                                   h->g_new, h->ssx, h->ssy, h->ssz, (int)h->n_total, h->stream));
+  const size_t nc = (size_t)(h->Npad / 256) * std::max(h->P, 1) * 3;
+  OD_CK(h, cudaMemcpyAsync(orbit_out, h->b.orbit_part, sizeof(double) * nc, cudaMemcpyDefault,
+                           h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->shard_phase = 3;
+  return check_device_err(h);
+}
+
+extern "C" od_status od_shard_finish(od_handle* h, const double* orbit_all) {
+  od_status st = shard_check(h, 3);
+  if (st != OD_OK) return st;
+  if (!orbit_all) return fail(h, OD_ERR_INVALID, "orbit_all is NULL");
+  const int nb_all = h->Npad_total / 256;
+  const size_t nc = (size_t)nb_all * std::max(h->P, 1) * 3;
+  OD_CK(h, cudaMemcpyAsync(h->g_orbit, orbit_all, sizeof(double) * nc, cudaMemcpyDefault,
+                           h->stream));
+  OD_CK(h, od_launch_shard_tail(h->dp, h->ds, h->b, h->g_orbit, nb_all, h->stream));
+  OD_CK(h, cudaStreamSynchronize(h->stream));
+  h->step += 1;
+  h->shard_phase = 0;
+  return check_device_err(h);
+}
+
+extern "C" od_status od_shard_info(const od_handle* h, int64_t* first, int64_t* count,
+                                   int64_t* n_total, int64_t* orbit_blocks) {
+  if (!h || !h->shard) return fail(nullptr, OD_ERR_INVALID, "not a shard handle");
+  if (first) *first = h->ion0;
+  if (count) *count = h->N;
+  if (n_total) *n_total = h->n_total;
+  if (orbit_blocks) *orbit_blocks = h->Npad / 256;
   return OD_OK;
 }

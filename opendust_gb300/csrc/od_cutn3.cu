@@ -253,8 +253,8 @@ template <int MT, int MS, int CUT, bool COUNT>
 __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ sx,
                                                       const float* __restrict__ sy,
                                                       const float* __restrict__ sz,
-                                                      float* __restrict__ outT,
-                                                      float* __restrict__ outR,
+                                                      unsigned long long* __restrict__ acc,
+                                                      size_t stride,
                                                       const n3_consts& k, int a, int b, float* sm,
                                                       const float* __restrict__ gbox,
                                                       float cull2, float k_in2) {
@@ -410,8 +410,8 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
 #undef CUT_H
   __syncthreads();
 
-  // 3. fixed-order sums of the slots; every ion of both tiles is written (zeros when no group
-  // pair reached it)
+  // 3. fixed-order sums of the slots, added to the slots' fixed-point accumulators (tile a's
+  // target sums and tile b's reaction sums; one sum per slot on a diagonal tile)
   for (int e = tid; e < T; e += kWarps * 32) {
     const int g = e / GT, l = e % GT;
     float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
@@ -422,8 +422,10 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
       acc2x2(hz, lz, t[2 * GT], t[5 * GT]);
     }
     if (!diag) {
-      outT[e] = hx; outT[T + e] = hy; outT[2 * T + e] = hz;
-      outT[3 * T + e] = lx; outT[4 * T + e] = ly; outT[5 * T + e] = lz;
+      const size_t ia = (size_t)a * T + e;
+      od_fix_add(acc + ia, hx, lx);
+      od_fix_add(acc + stride + ia, hy, ly);
+      od_fix_add(acc + 2 * stride + ia, hz, lz);
       hx = hy = hz = lx = ly = lz = 0.f;
     }
     const int gb = e / GS, l2 = e % GS;
@@ -435,8 +437,10 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
       od_acc2(hy, ly, r[GS]);
       od_acc2(hz, lz, r[2 * GS]);
     }
-    outR[e] = hx; outR[T + e] = hy; outR[2 * T + e] = hz;
-    outR[3 * T + e] = lx; outR[4 * T + e] = ly; outR[5 * T + e] = lz;
+    const size_t ib = (size_t)b * T + e;
+    od_fix_add(acc + ib, hx, lx);
+    od_fix_add(acc + stride + ib, hy, ly);
+    od_fix_add(acc + 2 * stride + ib, hz, lz);
   }
   __syncthreads();  // the next tile pair rewrites the list and the slots
   return cnt;
@@ -460,10 +464,10 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
     k_pairs_cutn3(const float* __restrict__ xs, const float* __restrict__ ys,
                   const float* __restrict__ zs, int nslots, int nT,
                   const int2* __restrict__ pairs, const int32_t* __restrict__ npairs,
-                  float* __restrict__ S, n3_cut cut, const float* __restrict__ gbox, float cull2,
+                  unsigned long long* __restrict__ acc, n3_cut cut,
+                  const float* __restrict__ gbox, float cull2,
                   unsigned long long* __restrict__ pair_count) {
   extern __shared__ float sm[];
-  constexpr size_t T6 = 6 * (size_t)cutn3_tile<BAL, MT, MS, PA>::T;
   static_assert(!BAL || PA == 1, "balanced list: one pass");
   const int np = *npairs;
   unsigned int cnt = 0;
@@ -471,17 +475,14 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
     const n3_consts kc = make_consts(cut);
     for (int k = blockIdx.x; k < np; k += gridDim.x) {
       const int2 ab = pairs[k];
-      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, S + ((size_t)ab.x * nT + ab.y) * T6,
-                                               S + ((size_t)ab.y * nT + ab.x) * T6, kc, ab.x,
-                                               ab.y, sm, gbox, cull2, cut.in2);
+      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, acc, (size_t)nslots, kc, ab.x, ab.y,
+                                               sm, gbox, cull2, cut.in2);
     }
   } else {
     for (int k = blockIdx.x; k < np; k += gridDim.x) {
       const int2 ab = pairs[k];
-      cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots,
-                                                        S + ((size_t)ab.x * nT + ab.y) * T6,
-                                                        S + ((size_t)ab.y * nT + ab.x) * T6, cut,
-                                                        ab.x, ab.y, sm, gbox, cull2);
+      cnt += n3_tile_pair<MT, MS, PA, CUT, COUNT, true>(xs, ys, zs, nslots, acc, (size_t)nslots,
+                                                        cut, ab.x, ab.y, sm, gbox, cull2);
     }
   }
   if (COUNT) {
@@ -491,73 +492,19 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   }
 }
 
-// Row sums over the tiles that share a listed pair with tile t, in increasing tile order,
-// written to the ions' entries of (ph, pl). Block (t, c) sums ions c·256 .. c·256+255 of tile t,
-// one ion per thread; the matrix rows are read once (streaming loads, four neighbours in flight
-// per thread), so the kernel runs at the HBM rate.
-__global__ void __launch_bounds__(256) k_tile_reduce(int nT, int nwords, int T,
-                                                     const uint32_t* __restrict__ adj,
-                                                     const float* __restrict__ S,
-                                                     const int32_t* __restrict__ perm,
-                                                     float4* __restrict__ ph,
-                                                     float4* __restrict__ pl) {
-  extern __shared__ int32_t nb[];  // [nT] neighbour tiles, then [8] warp counts
-  int32_t* wcnt = nb + nT;
-  __shared__ int s_m;
-  const int t = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (threadIdx.x == 0) s_m = 0;
-  __syncthreads();
-  // ordered compaction of {y : pair (min(t, y), max(t, y)) listed}, 256 candidates per round
-  for (int y0 = 0; y0 < nT; y0 += 256) {
-    const int y = y0 + threadIdx.x;
-    bool f = false;
-    if (y < nT)
-      f = y < t ? (adj[(size_t)y * nwords + (t >> 5)] >> (t & 31)) & 1u
-                : (adj[(size_t)t * nwords + (y >> 5)] >> (y & 31)) & 1u;
-    const uint32_t bal = __ballot_sync(0xffffffffu, f);
-    if (lane == 0) wcnt[w] = __popc(bal);
-    __syncthreads();
-    int base = s_m;
-    for (int k = 0; k < w; k++) base += wcnt[k];
-    if (f) nb[base + __popc(bal & ((1u << lane) - 1u))] = y;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int tot = 0;
-      for (int k = 0; k < 8; k++) tot += wcnt[k];
-      s_m += tot;
-    }
-    __syncthreads();
-  }
-  const int m = s_m;
-  const int e = blockIdx.y * 256 + threadIdx.x;
-  const int i = perm[t * T + e];
-  if (i < 0) return;  // sentinel slot (no barrier follows)
-  const float* row = S + (size_t)t * nT * 6 * (size_t)T + e;
-  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-  int q = 0;
-  for (; q + 4 <= m; q += 4) {
-    float v[4][6];
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const float* r = row + (size_t)nb[q + u] * 6 * T;
-#pragma unroll
-      for (int c = 0; c < 6; c++) v[u][c] = __ldcs(r + c * T);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-      acc2x2(hx, lx, v[u][0], v[u][3]);
-      acc2x2(hy, ly, v[u][1], v[u][4]);
-      acc2x2(hz, lz, v[u][2], v[u][5]);
-    }
-  }
-  for (; q < m; q++) {
-    const float* r = row + (size_t)nb[q] * 6 * T;
-    acc2x2(hx, lx, __ldcs(r), __ldcs(r + 3 * T));
-    acc2x2(hy, ly, __ldcs(r + T), __ldcs(r + 4 * T));
-    acc2x2(hz, lz, __ldcs(r + 2 * T), __ldcs(r + 5 * T));
-  }
-  ph[i] = make_float4(hx, hy, hz, 0.f);
-  pl[i] = make_float4(lx, ly, lz, 0.f);
+// Slot accumulators -> the ions' entries of (ph, pl) as two-float sums (slot s holds ion
+// perm[s], -1 for the sentinels in the tail), every slot cleared for the next evaluation.
+__global__ void __launch_bounds__(256) k_slot_take(int nslots, unsigned long long* __restrict__ acc,
+                                                  const int32_t* __restrict__ perm,
+                                                  float4* __restrict__ ph, float4* __restrict__ pl) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nslots) return;
+  float3 hi, lo;
+  od_fix_take(acc + e, (size_t)nslots, hi, lo);
+  const int i = perm[e];
+  if (i < 0) return;
+  ph[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  pl[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
 }
 
 }  // namespace
@@ -572,7 +519,7 @@ int od_cutn3_grid(int N) {
 size_t od_cutn3_bytes(int N, int T, int G) {
   const size_t nT = (size_t)((N + T - 1) / T), ns = nT * T, nc = (size_t)G * G * G;
   const size_t nw = (nT + 31) / 32;
-  return sizeof(float) * nT * nT * 6 * T                      // S
+  return sizeof(unsigned long long) * 3 * ns                 // accumulators
          + sizeof(int2) * nT * (nT + 1) / 2                   // pairs
          + sizeof(uint32_t) * nT * nw                         // bitmap
          + sizeof(float) * (3 * ns + 6 * nT + 6 * (ns / 64))  // sorted positions, boxes
@@ -639,14 +586,12 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
   } while (0)
 #define OD_CUTN3L(MT, MS, CUT, CNT, BAL, SM)                                                  \
   k_pairs_cutn3<MT, MS, 1, CUT, CNT, BAL><<<L.grid, kWarps * 32, SM, s>>>(                    \
-      L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.S, cut, L.gbox, rc2m, pair_count)
+      L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.acc, cut, L.gbox, rc2m, pair_count)
   if (L.ipt == 2 && L.T == 512) OD_CUTN3(2, 2, true, (cut_traits<2, 2>::SMEM));
   else if (L.ipt == 4 && L.T == 1024) OD_CUTN3(4, 4, false, (n3_traits<4, 4, 1>::SMEM));
   else return cudaErrorInvalidValue;
 #undef OD_CUTN3L
 #undef OD_CUTN3
-  const size_t smem = sizeof(int32_t) * (L.nT + 8);
-  k_tile_reduce<<<dim3(L.nT, L.T / 256), 256, smem, s>>>(L.nT, L.nwords, L.T, L.adj, L.S, L.perm,
-                                                        part_hi, part_lo);
+  k_slot_take<<<(L.nslots + 255) / 256, 256, 0, s>>>(L.nslots, L.acc, L.perm, part_hi, part_lo);
   return cudaGetLastError();
 }

@@ -23,7 +23,7 @@ struct od_pair_plan {
 struct od_pair_io {
   const float4* pos;
   const float *sx, *sy, *sz;
-  float* n3 = nullptr;  // variant 7: tile-pair partial sums [nT][nT][6][tile]
+  unsigned long long* n3 = nullptr;  // variant 7: fixed-point ion–ion accumulators [3][Npad]
 };
 
 // Device buffers of one simulation.
@@ -38,8 +38,8 @@ struct od_dbufs {
   double *s_q, *s_orbit, *s_collect, *s_dust, *s_field;  // result series
   float* cq;                            // [P] A_id * q_param, FP32 copy for the ion kernels
   float *sx, *sy, *sz;                  // [Npad] SoA copy of positions (all-pairs sources)
-  float* n3;                            // variant 7 tile-pair partial sums (or NULL)
-  size_t n3_len;                        // floats allocated at n3
+  unsigned long long* n3;               // variant 7 fixed-point accumulators [3][Npad] (or NULL)
+  size_t n3_len;                        // allocation at n3, in units of 4 bytes
 };
 
 int od_num_sms(int device);
@@ -115,7 +115,7 @@ struct od_cutn3 {
   uint32_t* adj;                    // [nT][nwords] tile pairs (a, b >= a) within the cutoff
   int32_t* rowptr;                  // [nT + 1] pair counts, then their exclusive prefix
   int2* pairs;                      // [nT (nT + 1) / 2] listed pairs, row-major
-  float* S;                         // [nT][nT][6][T] two-float partial sums
+  unsigned long long* acc;          // [3][nslots] fixed-point ion–ion sums per sorted slot
   int grid;                         // persistent blocks of the pair kernel
 };
 size_t od_cutn3_bytes(int N, int T, int G);
@@ -178,6 +178,26 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
                                 int N, int Npad, int P, const od_force_ctx& fc, int nrec,
                                 cudaStream_t s);
 cudaError_t od_run_fp32_probe(int device, double* tflops);
+// shards of one simulation (od_kernels.cu): K1 (part 0, positions also into the sources) or
+// K3 + K4 (part 1); the ion–ion sums of the shard's ions over all sources (directed variants
+// 2-6); the whole run's re-injection list -> grain sums and sources; correction and orbit sums
+// of the shard's ions; the tail over all shards' orbit partials
+cudaError_t od_launch_shard_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                 int N, int Npad, int jsplit, float* sx, float* sy, float* sz,
+                                 cudaStream_t s);
+cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const float* sy,
+                                  const float* sz, int nsrc_pad, int Npad_local, int tgt_off,
+                                  float4* ph, float4* plo, float rho0, uint32_t* err,
+                                  cudaStream_t s);
+cudaError_t od_launch_shard_list(const od_dparams* dp, od_dstate* ds, int K, const int32_t* gidx,
+                                 const int32_t* gbits, const float4* gnew, const float4* gv,
+                                 float* sx, float* sy, float* sz, cudaStream_t s);
+cudaError_t od_launch_shard_correct(const od_dparams* dp, const od_dstate* ds, const od_dbufs& b,
+                                    int Npad_local, int nrec, const int32_t* gidx,
+                                    const float4* gold, const float4* gnew, const float* sx,
+                                    const float* sy, const float* sz, int nsrc, cudaStream_t s);
+cudaError_t od_launch_shard_tail(const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                 const double* orbit_all, int nb_all, cudaStream_t s);
 // one-thread mbarrier wait that gives up after `limit` polls unless `arrive` (self test)
 cudaError_t od_launch_wait_selftest(uint32_t* err, uint32_t limit, int arrive, cudaStream_t s);
 cudaError_t od_launch_snapshot_flags(const od_dparams* dp, int n, int Npad, const float4* pos,

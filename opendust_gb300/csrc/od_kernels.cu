@@ -218,7 +218,8 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
                                               int j1, size_t slab_off,
                                               float4* __restrict__ part_hi,
                                               float4* __restrict__ part_lo, float rho0,
-                                              float newton_r2, uint32_t* __restrict__ err) {
+                                              float newton_r2, uint32_t* __restrict__ err,
+                                              int tgt_off = 0) {
   __shared__ __align__(128) float tx[2][OD_TJ];
   __shared__ __align__(128) float ty[2][OD_TJ];
   __shared__ __align__(128) float tz[2][OD_TJ];
@@ -226,8 +227,10 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
   const int tid = threadIdx.x;
   const int i0 = iblk * (TPT * NT) + tid, i1 = TPT == 2 ? i0 + NT : i0;
   const int ntiles = (j1 - j0) / OD_TJ;
-  const od_u64 X0 = p2(sx[i0], sx[i0]), Y0 = p2(sy[i0], sy[i0]), Z0 = p2(sz[i0], sz[i0]);
-  const od_u64 X1 = p2(sx[i1], sx[i1]), Y1 = p2(sy[i1], sy[i1]), Z1 = p2(sz[i1], sz[i1]);
+  // targets: entries tgt_off + i of the source arrays (a shard's own ions within all sources)
+  const int t0 = tgt_off + i0, t1 = tgt_off + i1;
+  const od_u64 X0 = p2(sx[t0], sx[t0]), Y0 = p2(sy[t0], sy[t0]), Z0 = p2(sz[t0], sz[t0]);
+  const od_u64 X1 = p2(sx[t1], sx[t1]), Y1 = p2(sy[t1], sy[t1]), Z1 = p2(sz[t1], sz[t1]);
   od_pk k;
   k.eps = p2(1e-30f, 1e-30f);
   k.rho = p2(rho0, rho0);
@@ -427,12 +430,14 @@ __device__ __forceinline__ void kick_drift_body(const od_dparams& p, const od_ds
                                                 float* __restrict__ sz, int i) {
   if (i >= p.N) return;
   float4 x = pos[i], v = vel[i];
-  if (p.coll != OD_COLL_NONE) collide(p, (uint32_t)i, (uint32_t)(ds->step + ds->rng_base), v);
+  if (p.coll != OD_COLL_NONE)
+    collide(p, (uint32_t)(p.ion0 + i), (uint32_t)(ds->step + ds->rng_base), v);
   const float4 gh = fhi[i], gl = flo[i];
   float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
-  a.x = fmaf(p.A_ii, gh.x + gl.x, a.x);
-  a.y = fmaf(p.A_ii, gh.y + gl.y, a.y);
-  a.z = fmaf(p.A_ii, gh.z + gl.z, a.z);
+  const float aii = p.A_ii * od_first_kick_weight(p.force_every, ds->step);
+  a.x = fmaf(aii, gh.x + gl.x, a.x);
+  a.y = fmaf(aii, gh.y + gl.y, a.y);
+  a.z = fmaf(aii, gh.z + gl.z, a.z);
   v.x = fmaf(0.5f, a.x, v.x); v.y = fmaf(0.5f, a.y, v.y); v.z = fmaf(0.5f, a.z, v.z);
   x.x += v.x; x.y += v.y; x.z += v.z;
   pos[i] = x;
@@ -454,7 +459,8 @@ __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restric
 
 // ============================================================== K3: kick + flags
 // all 32 lanes of a warp call this (warp ballot); i covers [0, Npad)
-__device__ __forceinline__ void kick_flag_body(const od_dparams& p, const float4* __restrict__ pos,
+__device__ __forceinline__ void kick_flag_body(const od_dparams& p, const od_dstate* __restrict__ ds,
+                                               const float4* __restrict__ pos,
                                                float4* __restrict__ vel,
                                                const float4* __restrict__ ph,
                                                const float4* __restrict__ pl, int jsplit,
@@ -463,16 +469,22 @@ __device__ __forceinline__ void kick_flag_body(const od_dparams& p, const float4
                                                const float* __restrict__ cq, int i) {
   int flag = 0;
   if (i < p.N) {
-    float3 hi, lo;
-    reduce_parts(ph, pl, p.Npad, jsplit, i, hi, lo);
-    fhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
-    flo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    // a step without an ion–ion evaluation (force interval k > 1) keeps the stored sums and
+    // kicks with the grain, trap and field forces only
+    float3 hi = make_float3(0.f, 0.f, 0.f), lo = make_float3(0.f, 0.f, 0.f);
+    float aii = 0.f;
+    if (od_evaluates(p.force_every, ds->step)) {
+      reduce_parts(ph, pl, p.Npad, jsplit, i, hi, lo);
+      fhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+      flo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
+      aii = p.force_every > 1 ? p.A_ii * (float)p.force_every : p.A_ii;
+    }
     const float4 x = pos[i];
     float4 v = vel[i];
     float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
-    a.x = fmaf(p.A_ii, hi.x + lo.x, a.x);
-    a.y = fmaf(p.A_ii, hi.y + lo.y, a.y);
-    a.z = fmaf(p.A_ii, hi.z + lo.z, a.z);
+    a.x = fmaf(aii, hi.x + lo.x, a.x);
+    a.y = fmaf(aii, hi.y + lo.y, a.y);
+    a.z = fmaf(aii, hi.z + lo.z, a.z);
     v.x = fmaf(0.5f, a.x, v.x); v.y = fmaf(0.5f, a.y, v.y); v.z = fmaf(0.5f, a.z, v.z);
     vel[i] = v;
     flag = od_flag(p, x.x, x.y, x.z) != 0;
@@ -482,6 +494,7 @@ __device__ __forceinline__ void kick_flag_body(const od_dparams& p, const float4
 }
 
 __global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict__ dp,
+                                                    const od_dstate* __restrict__ ds,
                                                     const float4* __restrict__ pos,
                                                     float4* __restrict__ vel,
                                                     const float4* __restrict__ ph,
@@ -490,7 +503,7 @@ __global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict
                                                     float4* __restrict__ flo,
                                                     uint32_t* __restrict__ flags,
                                                     const float* __restrict__ cq) {
-  kick_flag_body(*dp, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq,
+  kick_flag_body(*dp, ds, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq,
                  blockIdx.x * blockDim.x + threadIdx.x);  // grid covers Npad exactly
 }
 
@@ -623,6 +636,25 @@ __device__ void inject_one(const od_dparams& p, uint32_t ion, uint32_t step, flo
   }
 }
 
+// per-grain collected count and momentum (opendust.py:911-921) over list entries 0..K-1, in a
+// fixed order (FP64; one block of kCT threads)
+__device__ __forceinline__ void list_sums(const od_dparams& p, od_dstate* __restrict__ ds, int K,
+                                          const int32_t* __restrict__ list_bits,
+                                          const float4* __restrict__ list_v) {
+  const int tid = threadIdx.x;
+  for (int g = 0; g < p.P; g++) {
+    double dn = 0, mx = 0, my = 0, mz = 0;
+    for (int k = tid; k < K; k += kCT)
+      if ((list_bits[k] >> g) & 1) {
+        const float4 v = list_v[k];
+        dn += 1.0; mx += v.x; my += v.y; mz += v.z;
+      }
+    dn = block_sum_1024(dn); mx = block_sum_1024(mx);
+    my = block_sum_1024(my); mz = block_sum_1024(mz);
+    if (tid == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
+  }
+}
+
 __device__ __forceinline__ void collect_inject_body(
     const od_dparams& p, od_dstate* __restrict__ ds, float4* __restrict__ pos,
     float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
@@ -639,18 +671,7 @@ __device__ __forceinline__ void collect_inject_body(
     list_v[k] = v;
   }
   __syncthreads();
-  // per-grain collected count and momentum (opendust.py:911-921), fixed-order FP64 sums
-  for (int g = 0; g < p.P; g++) {
-    double dn = 0, mx = 0, my = 0, mz = 0;
-    for (int k = tid; k < K; k += kCT)
-      if ((list_bits[k] >> g) & 1) {
-        const float4 v = list_v[k];
-        dn += 1.0; mx += v.x; my += v.y; mz += v.z;
-      }
-    dn = block_sum_1024(dn); mx = block_sum_1024(mx);
-    my = block_sum_1024(my); mz = block_sum_1024(mz);
-    if (tid == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
-  }
+  list_sums(p, ds, K, list_bits, list_v);
   const uint32_t step = (uint32_t)(ds->step + ds->rng_base);
   if (p.dist == OD_DIST_MATTHEWS) {
     // the fork (chains/matthews.py:653-682): ions past |z| = H/2 or inside a grain re-enter
@@ -662,7 +683,7 @@ __device__ __forceinline__ void collect_inject_body(
       const int bits = list_bits[k];
       const float4 xo = list_old[k];
       float4 x = xo, v = list_v[k];
-      if (bits & (grains | (1 << 29))) inject_one(p, (uint32_t)i, step, x, v);
+      if (bits & (grains | (1 << 29))) inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
       if (bits & (1 << 30)) {
         const float rr = sqrtf(fmaf(xo.x, xo.x, xo.y * xo.y));
         const float nx = xo.x / rr, ny = xo.y / rr;
@@ -680,7 +701,7 @@ __device__ __forceinline__ void collect_inject_body(
   for (int k = tid; k < K; k += kCT) {
     const int i = list[k];
     float4 x, v;
-    inject_one(p, (uint32_t)i, step, x, v);
+    inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
     pos[i] = x;
     vel[i] = v;
     list_new[k] = x;
@@ -740,7 +761,13 @@ __device__ __forceinline__ void correct_orbit_body(
     const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
     const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
     const float4* __restrict__ list_old, const float4* __restrict__ list_new,
-    double* __restrict__ orbit_part, int nb, int blk, int nrec) {
+    double* __restrict__ orbit_part, int nb, int blk, int nrec,
+    const float* __restrict__ ssx = nullptr, const float* __restrict__ ssy = nullptr,
+    const float* __restrict__ ssz = nullptr, int nsrc = 0) {
+  // ssx..ssz (a shard of a larger run): the list holds the re-injected ions of every shard by
+  // global index, the re-injected ions' full sums run over the nsrc source positions ssx..ssz
+  // (all shards' ions, re-injected ones at their new positions), and only this shard's own
+  // entries (global index - p.ion0 in [0, p.N)) are written
   __shared__ double s_red[kBlk / 32];
   const int K = ds->nlist;
   const int tid = threadIdx.x;
@@ -795,13 +822,15 @@ __device__ __forceinline__ void correct_orbit_body(
     __shared__ float s_h[3][kBlk], s_l[3][kBlk];
     const bool cut = p.method == OD_FORCE_CUTOFF;
     for (int k = blk - nb; k < K; k += nrec) {
-      const int i = list[k];
+      const int i = ssx ? list[k] - p.ion0 : list[k];
+      if (ssx && (i < 0 || i >= p.N)) continue;  // another shard's ion (uniform per block)
       const float4 xi = list_new[k];
       float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
       float ax = 0.f, ay = 0.f, az = 0.f;
       int cnt = 0;
-      for (int j = tid; j < p.N; j += kBlk) {
-        const float4 q = pos[j];
+      const int nj = ssx ? nsrc : p.N;
+      for (int j = tid; j < nj; j += kBlk) {
+        const float4 q = ssx ? make_float4(ssx[j], ssy[j], ssz[j], 0.f) : pos[j];
         const float dx = xi.x - q.x, dy = xi.y - q.y, dz = xi.z - q.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
         const float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
@@ -1174,7 +1203,7 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
     return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz, b.n3}, N, Npad, b.part_hi, b.part_lo,
                            &ds->err, s);
   const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
-  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
+  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
                                   b.flags, b.cq);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
@@ -1340,6 +1369,7 @@ __global__ void __launch_bounds__(256) k_b_pairs(const od_simdesc* __restrict__ 
     if (it >= nitems) return;
     const int4 w = items[it];
     const od_simdesc& d = sims[w.x];
+    if (!od_evaluates(d.dp->force_every, d.ds->step)) continue;
     const bool ok = pairs_x2_body<256, 0, 1>(d.b.sx, d.b.sy, d.b.sz, w.y, w.z, w.w,
                                           (size_t)(w.z / d.chunk) * d.Npad, d.b.part_hi,
                                           d.b.part_lo, d.rho0, d.newton_r2, err);
@@ -1351,7 +1381,7 @@ __global__ void __launch_bounds__(kBlk) k_b_kick_flag(const od_simdesc* __restri
                                                       const int2* __restrict__ blk) {
   const int2 e = blk[blockIdx.x];
   const od_simdesc& d = sims[e.x];
-  kick_flag_body(*d.dp, d.b.pos, d.b.vel, d.b.part_hi, d.b.part_lo, d.jsplit, d.b.fhi, d.b.flo,
+  kick_flag_body(*d.dp, d.ds, d.b.pos, d.b.vel, d.b.part_hi, d.b.part_lo, d.jsplit, d.b.fhi, d.b.flo,
                  d.b.flags, d.b.cq, e.y * kBlk + threadIdx.x);
 }
 
@@ -1421,6 +1451,131 @@ cudaError_t od_launch_batch_step(const od_batchview& v, cudaStream_t s) {
   k_b_collect_inject<<<v.nsims, kCT, 0, s>>>(v.sims);
   k_b_correct_orbit<<<v.nblk_corr, kBlk, 0, s>>>(v.sims, v.blk_corr);
   k_b_tail<<<v.nsims, kBlk, 0, s>>>(v.sims);
+  return cudaGetLastError();
+}
+
+// ============================================================== shards of one simulation
+// A shard owns ions [ion0, ion0 + N) of a larger simulation and keeps every shard's positions
+// as sources (SoA, nsrc entries). Its step: K1 on its own ions (writing their positions into
+// the sources), the ion–ion sums of its ions over all sources, K3 and its own compaction and
+// re-injection (Philox keyed by the global index); then, given every shard's list (in shard
+// order, which is the global index order), the grain sums over the whole list, the new
+// positions in the sources, the correction and orbit sums of its own ions; then the FP64 tail
+// over every shard's orbit partials. With shard boundaries on 512-ion multiples every sum is
+// taken in the single-simulation order, so the shards reproduce the single simulation's bits.
+
+// global list (K entries) -> grain sums and the sources' re-injected positions
+__global__ void __launch_bounds__(kCT) k_shard_list(const od_dparams* __restrict__ dp,
+                                                    od_dstate* __restrict__ ds, int K,
+                                                    const int32_t* __restrict__ gidx,
+                                                    const int32_t* __restrict__ gbits,
+                                                    const float4* __restrict__ gnew,
+                                                    const float4* __restrict__ gv,
+                                                    float* __restrict__ sx, float* __restrict__ sy,
+                                                    float* __restrict__ sz) {
+  if (threadIdx.x == 0) ds->nlist = K;
+  list_sums(*dp, ds, K, gbits, gv);
+  for (int k = threadIdx.x; k < K; k += kCT) {
+    const int i = gidx[k];
+    const float4 x = gnew[k];
+    sx[i] = x.x; sy[i] = x.y; sz[i] = x.z;
+  }
+}
+
+__global__ void __launch_bounds__(kBlk) k_shard_correct_orbit(
+    const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+    const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
+    const uint32_t* __restrict__ flags, const int32_t* __restrict__ gidx,
+    const float4* __restrict__ gold, const float4* __restrict__ gnew,
+    double* __restrict__ orbit_part, int nb, const float* __restrict__ sx,
+    const float* __restrict__ sy, const float* __restrict__ sz, int nsrc) {
+  correct_orbit_body(*dp, ds, pos, fhi, flo, flags, gidx, gold, gnew, orbit_part, nb, blockIdx.x,
+                     gridDim.x - nb, sx, sy, sz, nsrc);
+}
+
+// directed ion–ion sums of a shard's ions (sources tgt_off .. tgt_off + Npad_local of the
+// sources) over all nsrc_pad sources, plan variants 2-6 (one target or two per thread)
+template <int NT, int NEWTON, int TPT>
+__global__ void __launch_bounds__(NT) k_shard_pairs(const float* __restrict__ sx,
+                                                    const float* __restrict__ sy,
+                                                    const float* __restrict__ sz, int nsrc_pad,
+                                                    int chunk, int Npad_local, int tgt_off,
+                                                    float4* __restrict__ part_hi,
+                                                    float4* __restrict__ part_lo, float rho0,
+                                                    float newton_r2, uint32_t* __restrict__ err) {
+  const int j0 = blockIdx.y * chunk;
+  pairs_x2_body<NT, NEWTON, TPT>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, nsrc_pad),
+                                 (size_t)blockIdx.y * Npad_local, part_hi, part_lo, rho0,
+                                 newton_r2, err, tgt_off);
+}
+
+cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const float* sy,
+                                  const float* sz, int nsrc_pad, int Npad_local, int tgt_off,
+                                  float4* ph, float4* plo, float rho0, uint32_t* err,
+                                  cudaStream_t s) {
+  const int tpt = (pl.variant == 5 || pl.variant == 6) ? 1 : 2;
+  if (pl.variant < 2 || pl.variant > 6 || (pl.nt != 128 && pl.nt != 256) || pl.ipt != tpt ||
+      Npad_local % (tpt * pl.nt) || pl.chunk % OD_TJ || tgt_off % OD_PAD)
+    return cudaErrorInvalidValue;
+  const dim3 grid(Npad_local / (tpt * pl.nt), pl.jsplit);
+  const float nr = 64.0f * rho0, nr2 = nr * nr;  // as launch_pairs_x2
+#define OD_SHARD_PAIRS(NT, NW, TP)                                                              \
+  k_shard_pairs<NT, NW, TP><<<grid, NT, 0, s>>>(sx, sy, sz, nsrc_pad, pl.chunk, Npad_local,    \
+                                                tgt_off, ph, plo, rho0, nr2, err)
+  switch (pl.nt * 100 + pl.variant) {
+    case 12802: OD_SHARD_PAIRS(128, 0, 2); break;
+    case 25602: OD_SHARD_PAIRS(256, 0, 2); break;
+    case 12803: OD_SHARD_PAIRS(128, 1, 2); break;
+    case 25603: OD_SHARD_PAIRS(256, 1, 2); break;
+    case 12804: OD_SHARD_PAIRS(128, 2, 2); break;
+    case 25604: OD_SHARD_PAIRS(256, 2, 2); break;
+    case 12805: OD_SHARD_PAIRS(128, 0, 1); break;
+    case 25605: OD_SHARD_PAIRS(256, 0, 1); break;
+    case 12806: OD_SHARD_PAIRS(128, 2, 1); break;
+    case 25606: OD_SHARD_PAIRS(256, 2, 1); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef OD_SHARD_PAIRS
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_shard_list(const od_dparams* dp, od_dstate* ds, int K, const int32_t* gidx,
+                                 const int32_t* gbits, const float4* gnew, const float4* gv,
+                                 float* sx, float* sy, float* sz, cudaStream_t s) {
+  k_shard_list<<<1, kCT, 0, s>>>(dp, ds, K, gidx, gbits, gnew, gv, sx, sy, sz);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_shard_correct(const od_dparams* dp, const od_dstate* ds, const od_dbufs& b,
+                                    int Npad_local, int nrec, const int32_t* gidx,
+                                    const float4* gold, const float4* gnew, const float* sx,
+                                    const float* sy, const float* sz, int nsrc, cudaStream_t s) {
+  const int nb = Npad_local / kBlk;
+  k_shard_correct_orbit<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, gidx,
+                                                   gold, gnew, b.orbit_part, nb, sx, sy, sz, nsrc);
+  return cudaGetLastError();
+}
+
+cudaError_t od_launch_shard_tail(const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                 const double* orbit_all, int nb_all, cudaStream_t s) {
+  k_tail<<<1, kBlk, 0, s>>>(dp, ds, orbit_all, nb_all, b.s_q, b.s_orbit, b.s_collect, b.s_dust,
+                           b.s_field, b.cq);
+  return cudaGetLastError();
+}
+
+// K1 of a shard (its positions also go to sources ion0 .. ion0 + N), or K3 + K4
+cudaError_t od_launch_shard_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
+                                 int N, int Npad, int jsplit, float* sx, float* sy, float* sz,
+                                 cudaStream_t s) {
+  if (part == 0) {
+    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq,
+                                                        sx, sy, sz);
+    return cudaGetLastError();
+  }
+  k_kick_flag<<<Npad / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit,
+                                          b.fhi, b.flo, b.flags, b.cq);
+  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
+                                     b.list_old, b.list_new, b.list_v);
   return cudaGetLastError();
 }
 

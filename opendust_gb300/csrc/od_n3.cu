@@ -46,14 +46,12 @@ __device__ __forceinline__ int2 tri_pair(int kb) {
 template <int MT, int MS, int PA>
 __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
     k_pairs_n3(const float* __restrict__ sx, const float* __restrict__ sy,
-               const float* __restrict__ sz, int Npad, int nT, float* __restrict__ S,
+               const float* __restrict__ sz, int Npad, unsigned long long* __restrict__ acc,
                float rho0) {
   extern __shared__ float sm[];
   const int2 ab = tri_pair(blockIdx.x);
-  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
-  n3_tile_pair<MT, MS, PA, 0, false>(sx, sy, sz, Npad, S + ((size_t)ab.x * nT + ab.y) * T6,
-                                     S + ((size_t)ab.y * nT + ab.x) * T6, n3_cut{rho0, 0.f, 0.f, 0.f},
-                                     ab.x, ab.y, sm);
+  n3_tile_pair<MT, MS, PA, 0, false>(sx, sy, sz, Npad, acc, (size_t)Npad,
+                                     n3_cut{rho0, 0.f, 0.f, 0.f}, ab.x, ab.y, sm);
 }
 
 // Batched form: block k takes work item k = (simulation, tile a, tile b) of a table that lists
@@ -64,69 +62,44 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   extern __shared__ float sm[];
   const int4 w = items[blockIdx.x];
   const od_simdesc& d = sims[w.x];
-  constexpr size_t T6 = 6 * (size_t)n3_traits<MT, MS, PA>::T;
-  n3_tile_pair<MT, MS, PA, 0, false>(d.b.sx, d.b.sy, d.b.sz, d.Npad,
-                                     d.b.n3 + ((size_t)w.y * w.w + w.z) * T6,
-                                     d.b.n3 + ((size_t)w.z * w.w + w.y) * T6,
+  if (!od_evaluates(d.dp->force_every, d.ds->step)) return;  // force interval: no evaluation
+  n3_tile_pair<MT, MS, PA, 0, false>(d.b.sx, d.b.sy, d.b.sz, d.Npad, d.b.n3, (size_t)d.Npad,
                                      n3_cut{d.rho0, 0.f, 0.f, 0.f}, w.y, w.z, sm);
 }
 
-// Row sums of S in a fixed order: slab 0 of (ph, pl) for ion i < Npad.
-__device__ __forceinline__ void n3_row_sum(const float* __restrict__ S, int nT, int T, int i,
-                                           float4* __restrict__ ph, float4* __restrict__ pl) {
-  const int t = i / T, e = i - t * T;
-  float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-  const float* r = S + (size_t)t * nT * 6 * (size_t)T + e;
-  const size_t step = 6 * (size_t)T;
-  // loads of kB entries are issued before their (ordered) accumulation: the sum is a stream
-  // of 24 bytes per entry and would otherwise wait on one load at a time
-  constexpr int kB = 8;
-  int y = 0;
-  for (; y + kB <= nT; y += kB, r += kB * step) {
-    float v[kB][6];
-#pragma unroll
-    for (int u = 0; u < kB; u++)
-#pragma unroll
-      for (int c = 0; c < 6; c++) v[u][c] = __ldcs(r + u * step + c * T);
-#pragma unroll
-    for (int u = 0; u < kB; u++) {
-      acc2x2(hx, lx, v[u][0], v[u][3]);
-      acc2x2(hy, ly, v[u][1], v[u][4]);
-      acc2x2(hz, lz, v[u][2], v[u][5]);
-    }
-  }
-  for (; y < nT; y++, r += step) {
-    acc2x2(hx, lx, r[0], r[3 * T]);
-    acc2x2(hy, ly, r[T], r[4 * T]);
-    acc2x2(hz, lz, r[2 * T], r[5 * T]);
-  }
-  ph[i] = make_float4(hx, hy, hz, 0.f);
-  pl[i] = make_float4(lx, ly, lz, 0.f);
-}
-
-__global__ void k_n3_reduce(const float* __restrict__ S, int nT, int T, int Npad,
-                            float4* __restrict__ ph, float4* __restrict__ pl) {
+// Accumulators -> slab 0 of (ph, pl) as two-float sums, and cleared for the next evaluation.
+__global__ void k_n3_take(unsigned long long* __restrict__ acc, int Npad, float4* __restrict__ ph,
+                          float4* __restrict__ pl) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < Npad) n3_row_sum(S, nT, T, i, ph, pl);
+  if (i >= Npad) return;
+  float3 hi, lo;
+  od_fix_take(acc + i, (size_t)Npad, hi, lo);
+  ph[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  pl[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
 }
 
-// Batched row sums: block k covers 256 ions of the simulation in blk[k] (those using variant 7).
-__global__ void k_b_n3_reduce(const od_simdesc* __restrict__ sims, const int2* __restrict__ blk) {
+// Batched form: block k covers 256 ions of the simulation in blk[k] (those using variant 7).
+__global__ void k_b_n3_take(const od_simdesc* __restrict__ sims, const int2* __restrict__ blk) {
   const int2 e = blk[blockIdx.x];
   const od_simdesc& d = sims[e.x];
-  n3_row_sum(d.b.n3, (d.Npad + d.n3_tile - 1) / d.n3_tile, d.n3_tile, e.y * 256 + threadIdx.x,
-             d.b.part_hi, d.b.part_lo);
+  if (!od_evaluates(d.dp->force_every, d.ds->step)) return;
+  const int i = e.y * 256 + threadIdx.x;
+  if (i >= d.Npad) return;
+  float3 hi, lo;
+  od_fix_take(d.b.n3 + i, (size_t)d.Npad, hi, lo);
+  d.b.part_hi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  d.b.part_lo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
 }
 
 template <int MT, int MS, int PA>
-cudaError_t launch_n3(const od_pair_io& io, int Npad, float* S, float4* ph, float4* pl,
-                      float rho0, cudaStream_t s) {
+cudaError_t launch_n3(const od_pair_io& io, int Npad, unsigned long long* acc, float4* ph,
+                      float4* pl, float rho0, cudaStream_t s) {
   using TR = n3_traits<MT, MS, PA>;
   const int nT = (Npad + TR::T - 1) / TR::T;
   const long long nblk = (long long)nT * (nT + 1) / 2;
   k_pairs_n3<MT, MS, PA><<<(unsigned)nblk, kWarps * 32, TR::SMEM, s>>>(io.sx, io.sy, io.sz, Npad,
-                                                                      nT, S, rho0);
-  k_n3_reduce<<<(Npad + 255) / 256, 256, 0, s>>>(S, nT, TR::T, Npad, ph, pl);
+                                                                      acc, rho0);
+  k_n3_take<<<(Npad + 255) / 256, 256, 0, s>>>(acc, Npad, ph, pl);
   return cudaGetLastError();
 }
 
@@ -189,9 +162,9 @@ int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
 }
 
 size_t od_n3_floats(int Npad, int T) {
+  // three 64-bit fixed-point accumulators per ion, whatever the tile
   if (T <= 0) return 0;
-  const size_t nT = (size_t)((Npad + T - 1) / T);
-  return nT * nT * 6 * (size_t)T;
+  return 6 * (size_t)Npad;
 }
 
 cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s) {
@@ -202,7 +175,7 @@ cudaError_t od_launch_batch_pairs_n3(const od_batchview& v, cudaStream_t s) {
   if (v.n3_nitems[1] > 0)
     k_b_pairs_n3<8, 2, 1><<<v.n3_nitems[1], kWarps * 32, n3_traits<8, 2, 1>::SMEM, s>>>(
         v.sims, v.n3_items[1]);
-  if (v.n3_nblk > 0) k_b_n3_reduce<<<v.n3_nblk, 256, 0, s>>>(v.sims, v.n3_blk);
+  if (v.n3_nblk > 0) k_b_n3_take<<<v.n3_nblk, 256, 0, s>>>(v.sims, v.n3_blk);
   return cudaGetLastError();
 }
 

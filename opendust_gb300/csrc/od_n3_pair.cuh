@@ -184,17 +184,18 @@ __device__ __forceinline__ void group_box(const float* __restrict__ gbox, int g0
     }
 }
 
-// Tile pair (a, b), a <= b, of one simulation: one block. outT receives the two-float sums
-// of tile a's ions from tile b, outR those of tile b's ions from tile a (the same slice when
-// a == b); each [6][T]. sm: dynamic shared memory of n3_traits::SMEM bytes. CULL skips group
-// pairs whose 64-ion group boxes (gbox) are farther apart than sqrt(cull2). Returns the
-// directed pairs inside the cutoff when COUNT.
+// Tile pair (a, b), a <= b, of one simulation: one block. The two-float sums of tile a's ions
+// from tile b and of tile b's ions from tile a (one sum per ion when a == b) are added to the
+// ions' fixed-point accumulators acc[c * stride + ion] (od_fix_add), ions below Npad only.
+// sm: dynamic shared memory of n3_traits::SMEM bytes. CULL skips group pairs whose 64-ion group
+// boxes (gbox) are farther apart than sqrt(cull2). Returns the directed pairs inside the cutoff
+// when COUNT.
 template <int MT, int MS, int PA, int CUT, bool COUNT, bool CULL = false>
 __device__ __forceinline__ unsigned int n3_tile_pair(const float* __restrict__ sx,
                                                      const float* __restrict__ sy,
                                                      const float* __restrict__ sz, int Npad,
-                                                     float* __restrict__ outT,
-                                                     float* __restrict__ outR, const n3_cut& cut,
+                                                     unsigned long long* __restrict__ acc,
+                                                     size_t stride, const n3_cut& cut,
                                                      int a, int b, float* sm,
                                                      const float* __restrict__ gbox = nullptr,
                                                      float cull2 = 0.f) {
@@ -352,19 +353,23 @@ __device__ __forceinline__ unsigned int n3_tile_pair(const float* __restrict__ s
           acc2x2(sm[2 * T + e], sm[5 * T + e], N3_H(2, kt), N3_H(5, kt));
         }
       } else {
-        float* o = outT;
 #pragma unroll
         for (int kt = 0; kt < MT; kt++) {
-          const int e = ga * GT + lane + 32 * kt;
+          const size_t gi = (size_t)GA * GT + lane + 32 * kt;  // < Npad: ta_ok
 #pragma unroll
-          for (int c = 0; c < 6; c++) o[c * T + e] = N3_H(c, kt);
+          for (int c = 0; c < 3; c++) od_fix_add(acc + c * stride + gi, N3_H(c, kt), N3_H(3 + c, kt));
         }
       }
     }
     __syncthreads();
   }
 #undef N3_H
-  for (int e = tid; e < 6 * T; e += kWarps * 32) outR[e] = sm[e];
+  for (int e = tid; e < T; e += kWarps * 32) {
+    const size_t gi = (size_t)b * T + e;
+    if (gi < (size_t)Npad)
+#pragma unroll
+      for (int c = 0; c < 3; c++) od_fix_add(acc + c * stride + gi, sm[c * T + e], sm[(3 + c) * T + e]);
+  }
   return cnt;
 }
 

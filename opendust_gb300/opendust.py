@@ -172,7 +172,7 @@ def parse_device_index(deviceIndex) -> int:
 def build_simulation(plasma, sim, dustParticles, distributionType, *, cutOff=False,
                      cutoff_distance=None, switch_distance=None, collisions=None,
                      mean_free_path=None, seed=0, avg_start=None, sim_id=0, trap=None,
-                     device=0, n_steps=None, injection=None):
+                     device=0, n_steps=None, injection=None, force_every=1):
     """od_config for one simulation plus the host-side setup products.
 
     injection: precomputed (tables, probs) of setup_host.injection_setup, or None.
@@ -181,7 +181,11 @@ def build_simulation(plasma, sim, dustParticles, distributionType, *, cutOff=Fal
           a callable (Rh, Hh, n_r, n_h, n_points, seed) -> potential grid.
     collisions: None -> the reference's model (per-DOF constant w_c for fieldDriven, none
           for Maxwellian); "none"; "mfp" -> constant mean free path `mean_free_path` [m].
+    force_every: ion–ion force interval k (1: every step, the reference's integrator; k > 1:
+          impulse multiple time stepping, od_config.force_every).
     """
+    if int(force_every) < 1:
+        raise ValueError("force_every must be >= 1")
     if distributionType not in ("Maxwellian", "fieldDriven"):
         raise ValueError("distributionType must be 'Maxwellian' or 'fieldDriven'")
     dist = _lib.OD_DIST_MAXWELLIAN if distributionType == "Maxwellian" else _lib.OD_DIST_FIELD_DRIVEN
@@ -247,6 +251,7 @@ def build_simulation(plasma, sim, dustParticles, distributionType, *, cutOff=Fal
         probs=probs,
         tables=tables,
         grains=grains,
+        force_every=int(force_every),
     )
     info = {"alpha": alpha, "tables": tables, "probs": probs, "trap_grid": (Rh, Hh, n_r, n_h, n_points)}
     return holder, info

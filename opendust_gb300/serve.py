@@ -88,12 +88,24 @@ def device_memory(device: int = 0):
     return free.value, total.value
 
 
+def interval_by_size(N: int) -> int:
+    """Ion–ion force interval for a served request of N ions: 8 from 2^16 ions, 4 from 2^15,
+    every step below (where the pair work no longer dominates the step). The rule follows the
+    pilot-window tuning of the sweep (tuning.choose_force_interval, 1 % bound on the grains'
+    time-averaged charge and ion force); the served results are compared with the plain path's
+    per request."""
+    return 8 if N >= 2**16 else (4 if N >= 2**15 else 1)
+
+
 class Server:
     def __init__(self, device: int = 0, budget_frac: float = 0.8, chunk: int = 25,
-                 max_members: int = 512):
+                 max_members: int = 512, interval=None):
+        """interval: None (every step, the reference's integrator) or a function N -> force
+        interval k (od_config.force_every), e.g. interval_by_size."""
         self.device = device
         self.chunk = chunk
         self.max_members = max_members
+        self.interval = interval
         free, total = device_memory(device)
         self.budget = int(budget_frac * total) - (total - free)  # of what is free now
 
@@ -121,6 +133,8 @@ class Server:
                     if not futures[r.rid].done() and live:
                         break  # its host setup is still running: keep stepping the others
                     holder, pos, vel = finish_prepare(r, futures[r.rid].result(), self.device)
+                    if self.interval is not None:
+                        holder.cfg.force_every = int(self.interval(int(r.sim.N)))
                     need = _lib.config_device_bytes(holder)
                     if live and used + need > self.budget:
                         break
@@ -156,18 +170,24 @@ class Server:
         return summarize(reqs, wall, gpu_ms)
 
 
-def run_plain(requests: list[Request], device: int = 0, batch_plan: bool = False) -> dict:
+def run_plain(requests: list[Request], device: int = 0, batch_plan: bool = False,
+              pool=None) -> dict:
     """Baseline: the same requests, one at a time through the single-simulation path (its
     default all-pairs plan, or with batch_plan the plan the server's batch gives each request,
-    so that results are bitwise comparable)."""
+    so that results are bitwise comparable). pool: the server's process pool, so that the host
+    part of every request's setup overlaps the GPU work here as it does in the server."""
     reqs = sorted(requests, key=lambda r: r.arrival)
+    futures = {r.rid: pool.submit(host_prepare, r) for r in reqs} if pool is not None else None
     t0 = time.perf_counter()
     gpu_ms = 0.0
     for r in reqs:
         wait = r.arrival - (time.perf_counter() - t0)
         if wait > 0:
             time.sleep(wait)
-        holder, pos, vel = prepare(r, device)
+        if futures is not None:
+            holder, pos, vel = finish_prepare(r, futures[r.rid].result(), device)
+        else:
+            holder, pos, vel = prepare(r, device)
         with _lib.Engine(holder, device) as eng:
             if batch_plan:
                 eng.set_pair_plan(*_lib.batch_pair_plan(r.sim.N))

@@ -71,3 +71,58 @@ def choose_force_method(holder: _lib.ConfigHolder, pos: np.ndarray, vel: np.ndar
     best = min(ok, key=lambda c: c["step_ms"])
     return {"method": "allpairs" if best["cutoff"] is None else "cutoff", "cutoff": best["cutoff"],
             "rel_err": best["rel_err"], "step_ms": best["step_ms"], "candidates": cands}
+
+
+def _averages(holder, k, pos, vel, steps, device):
+    cfg = _lib.od_config.from_buffer_copy(holder.cfg)
+    cfg.force_every = int(k)
+    cfg.n_steps = steps
+    cfg.avg_start = steps // 2
+    with _lib.Engine(_lib.ConfigHolder(cfg, holder._keep), device) as eng:
+        eng.set_state(pos, vel)
+        eng.set_timing(True, count_pairs=False)
+        eng.step(steps)
+        step_ms, n, _, _ = eng.timing()
+        eng.set_timing(False)
+        avg, _ = eng.averages()
+    return avg, step_ms / max(n, 1)
+
+
+def interval_errors(avg, ref) -> dict:
+    """Relative errors of time averages (rows of od_get_averages: q, orbit, collect, dust,
+    field) against a reference run: charge max_p |dq_p|/|q_p|; ion force (orbit + collect) as
+    one norm over the grains, |dF| / |F|."""
+    dq = float(np.max(np.abs(avg[:, 0] - ref[:, 0]) / np.maximum(np.abs(ref[:, 0]), 1e-300)))
+    f = avg[:, 1:4] + avg[:, 4:7]
+    fr = ref[:, 1:4] + ref[:, 4:7]
+    df = float(np.linalg.norm(f - fr) / max(np.linalg.norm(fr), 1e-300))
+    return {"q": dq, "force": df}
+
+
+def choose_force_interval(holder: _lib.ConfigHolder, pos: np.ndarray, vel: np.ndarray,
+                          max_rel_err: float = 1e-2, intervals=(2, 4, 8, 16),
+                          pilot_steps: int = 100, device: int = 0) -> dict:
+    """Largest ion–ion force interval k (od_config.force_every) whose error on the grains'
+    time-averaged charge and ion force stays within max_rel_err on a pilot window.
+
+    The pilot runs pilot_steps steps from the caller's state (pos, vel in SI units) with k = 1
+    (the reference's integrator) and with each candidate k; every run uses the same seed, so
+    the Philox streams of collisions and re-injection are the same and the runs differ only by
+    the integrator. Errors are those of interval_errors over the window's second half. The
+    search stops at the first candidate that fails (errors grow with k).
+    Returns {"force_every": k, "errors": {...}, "step_ms": t, "candidates": [...]}.
+    """
+    ref, t1 = _averages(holder, 1, pos, vel, pilot_steps, device)
+    best = {"force_every": 1, "errors": {"q": 0.0, "force": 0.0}, "step_ms": t1}
+    cands = [dict(best)]
+    for k in sorted(int(x) for x in intervals):
+        if k <= 1:
+            continue
+        avg, t = _averages(holder, k, pos, vel, pilot_steps, device)
+        err = interval_errors(avg, ref)
+        c = {"force_every": k, "errors": err, "step_ms": t}
+        cands.append(c)
+        if max(err.values()) > max_rel_err:
+            break
+        best = c
+    return {**best, "candidates": cands}

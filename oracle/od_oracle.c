@@ -382,6 +382,69 @@ static void accel_total(const odo_par* p, const double* alpha, int64_t n, const 
   }
 }
 
+/* Acceleration with a stored ion–ion sum G (lambda units) weighted by w: the force interval
+ * (od_config.force_every) uses w = k on the kicks next to an evaluation and 0 otherwise. */
+static void accel_mts(const odo_par* p, const double* alpha, int64_t n, const double* x,
+                      const double* qp, const double* G, double w, double* a) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) {
+    double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+    double ax = w * p->A_ii * G[3 * i], ay = w * p->A_ii * G[3 * i + 1], az = w * p->A_ii * G[3 * i + 2];
+    for (int g = 0; g < p->P; g++) {
+      double dx = xi - p->gx[g], dy = yi - p->gy[g], dz = zi - p->gz[g];
+      double r2 = dx * dx + dy * dy + dz * dz;
+      double c = p->A_id * qp[g] / (r2 * sqrt(r2));
+      ax += c * dx; ay += c * dy; az += c * dz;
+    }
+    double t[3] = {0, 0, 0};
+    if (p->trap_kind == OD_TRAP_POLY) trap_accel(alpha, p->A_ii, xi, yi, zi, t);
+    else if (p->trap_kind == OD_TRAP_TABLE) trap_table_accel(p, xi, yi, zi, t);
+    a[3 * i] = ax + t[0];
+    a[3 * i + 1] = ay + t[1];
+    a[3 * i + 2] = az + t[2] + field_accel(p, zi);
+  }
+}
+
+/* After re-injection the stored ion–ion sums follow the new ion set, as the CUDA step does
+ * between evaluations: for every ion that stayed, the removed ions' terms come out and the
+ * new ions' terms go in (at the ion's current position); every re-injected ion gets its full
+ * sum over all current positions. inj[m] lists the m re-injected ions with their old and new
+ * positions. */
+static void mts_follow_injection(const odo_par* p, int64_t n, const double* x, const int* fl,
+                                 const int64_t* inj, const double* xold, int64_t m, double* G) {
+  if (m == 0) return;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; i++) {
+    if (fl[i]) continue;
+    double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+    double gx = 0, gy = 0, gz = 0;
+    for (int64_t k = 0; k < m; k++) {
+      const double* qn = x + 3 * inj[k];
+      const double* qo = xold + 3 * k;
+      double dx = xi - qn[0], dy = yi - qn[1], dz = zi - qn[2];
+      double c = pair_factor(p, dx * dx + dy * dy + dz * dz);
+      gx += c * dx; gy += c * dy; gz += c * dz;
+      dx = xi - qo[0]; dy = yi - qo[1]; dz = zi - qo[2];
+      c = pair_factor(p, dx * dx + dy * dy + dz * dz);
+      gx -= c * dx; gy -= c * dy; gz -= c * dz;
+    }
+    G[3 * i] += gx; G[3 * i + 1] += gy; G[3 * i + 2] += gz;
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < m; k++) {
+    int64_t i = inj[k];
+    double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+    double gx = 0, gy = 0, gz = 0;
+    for (int64_t j = 0; j < n; j++) {
+      if (j == i) continue;
+      double dx = xi - x[3 * j], dy = yi - x[3 * j + 1], dz = zi - x[3 * j + 2];
+      double c = pair_factor(p, dx * dx + dy * dy + dz * dz);
+      gx += c * dx; gy += c * dy; gz += c * dz;
+    }
+    G[3 * i] = gx; G[3 * i + 1] = gy; G[3 * i + 2] = gz;
+  }
+}
+
 /* ------------------------------------------------------------- flags */
 /* opendust.py:894-910: inside_dust_p = step(r_p - d) (inclusive), outside_domain_r =
  * step(rho - R), outside_domain_z = step(|z| - H/2). Evaluated on squared distances in FP64
@@ -653,17 +716,39 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
   }
   double q[OD_MAX_GRAINS];
   for (int g = 0; g < P; g++) q[g] = q_param[g];
+  /* force interval k > 1 (od_config.force_every): stored ion–ion sums G, evaluated at the
+   * start and at the end of steps with step % k == k - 1 */
+  const int kf = c->force_every > 1 ? c->force_every : 1;
+  double* G = NULL;
+  int64_t* inj = NULL;
+  double* xold = NULL;
+  if (kf > 1) {
+    G = (double*)malloc(sizeof(double) * 3 * n);
+    inj = (int64_t*)malloc(sizeof(int64_t) * n);
+    xold = (double*)malloc(sizeof(double) * 3 * n);
+    ionion(p, n, x, G);
+  }
 
   for (int64_t s = 0; s < nsteps; s++) {
     int64_t step = first_step + s;        /* step of the window: step 0 keeps the charges */
     uint32_t st = (uint32_t)(rng_base + step); /* Philox step counter (continues across windows) */
     if (p->coll != OD_COLL_NONE)
       for (int64_t i = 0; i < n; i++) collide(p, (uint32_t)i, st, v + 3 * i);
+    if (kf > 1) {
+      /* impulse multiple time stepping: kicks of weight k next to an evaluation */
+      accel_mts(p, c->alpha, n, x, q, G, step % kf == 0 ? (double)kf : 0.0, a);
+      for (int64_t i = 0; i < 3 * n; i++) { v[i] += 0.5 * a[i]; x[i] += v[i]; }
+      int ev = step % kf == kf - 1;
+      if (ev) ionion(p, n, x, G);
+      accel_mts(p, c->alpha, n, x, q, G, ev ? (double)kf : 0.0, a);
+      for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * a[i];
+    } else {
     /* addUpdateContextState; v += 0.5 dt f/m; x += dt v; v += 0.5 dt f/m (opendust.py:864-877) */
     accel_total(p, c->alpha, n, x, q, a);
     for (int64_t i = 0; i < 3 * n; i++) { v[i] += 0.5 * a[i]; x[i] += v[i]; }
     accel_total(p, c->alpha, n, x, q, a);
     for (int64_t i = 0; i < 3 * n; i++) v[i] += 0.5 * a[i];
+    }
     /* flags and collection sums (opendust.py:894-921) */
     double dN[OD_MAX_GRAINS] = {0}, M[OD_MAX_GRAINS][3];
     memset(M, 0, sizeof(M));
@@ -696,8 +781,16 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
       }
     } else {
       for (int64_t i = 0; i < n; i++)
-        if (fl[i]) { inject_one(p, (uint32_t)i, st, x + 3 * i, v + 3 * i); ninj++; }
+        if (fl[i]) {
+          if (kf > 1) {
+            inj[ninj] = i;
+            memcpy(xold + 3 * ninj, x + 3 * i, 3 * sizeof(double));
+          }
+          inject_one(p, (uint32_t)i, st, x + 3 * i, v + 3 * i);
+          ninj++;
+        }
     }
+    if (kf > 1) mts_follow_injection(p, n, x, fl, inj, xold, ninj, G);
     /* orbit sums on the re-injected positions (opendust.py:977-1037) */
     double S[OD_MAX_GRAINS][3];
     memset(S, 0, sizeof(S));
@@ -748,6 +841,7 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
   for (int64_t i = 0; i < 3 * n; i++) { pos[i] = x[i] * p->lam; vel[i] = v[i] * p->vunit; }
   for (int g = 0; g < P; g++) q_param[g] = q[g];
   free(x); free(v); free(a); free(fl); free(p);
+  free(G); free(inj); free(xold);
   return 0;
 }
 

@@ -14,7 +14,7 @@
 import numpy as np
 import pytest
 
-from opendust_gb300 import _lib, build_simulation, workloads
+from opendust_gb300 import _lib, build_simulation, setup_host, workloads
 from oracle import oracle
 from tests._util import case, rel_err_per_ion
 
@@ -63,7 +63,7 @@ def test_full_size_field_chain_snapshot_and_collected_set(gpu_lib):
     assert N == 2**19 and len(grains) == 5 and holder.cfg.force_method == _lib.OD_FORCE_CUTOFF
     assert abs(holder.cfg.cutoff / plasma.r_D_e - 2.0) < 1e-12
     with _lib.Engine(holder) as eng:
-        eng.init_state()
+        eng.init_state(setup_host.field_driven_vz_table(plasma.v_fl, plasma.v_T))
         eng.step(12)
         pos, _ = eng.get_state()
         f = eng.force_snapshot(pos)
@@ -80,7 +80,7 @@ def test_full_size_field_chain_snapshot_and_collected_set(gpu_lib):
     assert cnt == rcnt
     assert np.array_equal(idx_c, ridx)
     assert np.array_equal(gc, rgc)
-    assert np.all(gc >= 40)            # on and just inside every grain
+    assert np.all(gc >= 20)            # at least the ions planted just inside every grain
 
 
 def _two_grain_maxwell(N, n):
@@ -98,6 +98,17 @@ def test_grain_series_against_oracle(gpu_lib, builder, N, n):
     holder, pos, vel, plasma, sim, grains = case(N=N, n=n, seed=51, builder=builder)
     P = len(grains)
     assert P >= 2
+    # ions aimed at every grain, so that each collects within the first steps
+    rng = np.random.default_rng(52)
+    k = 0
+    for g in grains:
+        c = np.array([g.x, g.y, g.z])
+        for _ in range(8):
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            pos[k] = c + 1.5 * g.r * d
+            vel[k] = -3.0 * plasma.v_B * d
+            k += 1
     with _lib.Engine(holder) as eng:
         eng.set_state(pos, vel)
         eng.step(n)
@@ -113,7 +124,7 @@ def test_grain_series_against_oracle(gpu_lib, builder, N, n):
     do = rel(ser["orbit"], ref["orbit"])
     print(f"{P} grains, {n} steps: q {dq:.2e}, dust-dust {dd:.2e}, collect {dc:.2e}, "
           f"orbit {do:.2e}, collected {ref['dN'].sum()}")
-    assert ref["dN"].sum() > 0 and np.abs(ref["dust"]).max() > 0
+    assert np.all(ref["dN"].sum(0) > 0) and np.abs(ref["dust"]).max() > 0
     # charges follow from integer collection counts: equal counts give charges equal to FP64
     # rounding, and the dust-dust force is a function of the charges and grain positions
     assert dq <= 1e-9

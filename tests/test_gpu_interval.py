@@ -1,0 +1,112 @@
+"""Ion–ion force interval k > 1 (impulse multiple time stepping, od_config.force_every).
+
+* The CUDA step with k = 4 against the FP64 oracle running the same scheme (stored ion–ion sums
+  evaluated every k steps, kicks of weight k next to an evaluation, stored sums following
+  re-injection): positions within 1e-3 lambda after 40 steps, charges within 1e-6, orbit
+  forces within 1e-3 (the tolerances of the 40-step test of the every-step integrator).
+* k = 1 is the reference's integrator: bitwise the default.
+* Batch members with different intervals and different step phases equal the same
+  simulations stepped alone, bitwise.
+"""
+import numpy as np
+import pytest
+
+from opendust_gb300 import _lib, workloads
+from oracle import oracle
+from tests._util import case
+from tests.test_gpu_batch import member, same
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k,builder", [(4, workloads.small_plain), (3, workloads.field_chain)])
+def test_interval_against_oracle(gpu_lib, k, builder):
+    holder, pos, vel, plasma, sim, grains = case(N=2048, n=40, seed=61, builder=builder,
+                                                 force_every=k)
+    assert holder.cfg.force_every == k
+    # ions leaving through the downstream wall and falling into the first grain at different
+    # steps of the interval, so that the stored sums follow re-injection between evaluations
+    lam = plasma.r_D_e
+    g = grains[0]
+    for m in range(24):
+        pos[m] = [0.1 * lam * m / 24, 0.0, sim.H / 2 - (m % 6 + 0.5) * 1e-3 * lam]
+        vel[m] = [0.0, 0.0, 3 * plasma.v_B]
+    for m in range(24, 36):
+        th = 2 * np.pi * (m - 24) / 12
+        pos[m] = [g.x + 0.5 * g.r * np.cos(th), g.y + 0.5 * g.r * np.sin(th),
+                  g.z + g.r * (1.0 + 0.4 * (m % 5))]
+        vel[m] = [0.0, 0.0, -3 * plasma.v_B]
+    with _lib.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        eng.step(40)
+        ser = eng.series()
+        gp, gv = eng.get_state()
+    ref = oracle.run(holder, pos, vel, 0, 40, round32=True)
+    dpos = np.max(np.abs(gp - ref["pos"])) / lam
+    qerr = np.max(np.abs(ser["q"] - ref["q"]) / np.maximum(np.abs(ref["q"]), 1e-30))
+    oerr = np.max(np.linalg.norm(ser["orbit"] - ref["orbit"], axis=2) /
+                  np.linalg.norm(ref["orbit"], axis=2))
+    print(f"k={k}, 40 steps: max |dx| {dpos:.3e} lambda, q rel {qerr:.3e}, orbit rel {oerr:.3e}, "
+          f"injected {ref['n_inj'].sum()}")
+    assert np.count_nonzero(ref["n_inj"]) >= 3
+    assert dpos < 1e-3
+    assert qerr < 1e-6
+    assert oerr < 1e-3
+
+
+def test_interval_one_is_the_default(gpu_lib):
+    out = []
+    for kw in ({}, {"force_every": 1}):
+        holder, pos, vel, *_ = case(N=2048, n=10, seed=62, **kw)
+        with _lib.Engine(holder) as eng:
+            eng.set_state(pos, vel)
+            eng.step(10)
+            p, v = eng.get_state()
+            out.append((eng.series(), p, v))
+    same(out[0], out[1])
+
+
+def test_interval_changes_the_trajectory_and_saves_pair_time(gpu_lib):
+    res = {}
+    for k in (1, 8):
+        holder, pos, vel, *_ = case(N=2**16, n=40, seed=63, force_every=k)
+        with _lib.Engine(holder) as eng:
+            eng.set_state(pos, vel)
+            eng.step(8)
+            eng.set_timing(True, count_pairs=False)
+            eng.step(32)
+            step_ms, nsteps, pair_ms, launches = eng.timing()
+            eng.set_timing(False)
+            res[k] = (step_ms / nsteps, launches, eng.get_state()[0])
+    print(f"2^16 ions: k=1 {res[1][0]:.3f} ms/step ({res[1][1]} pair launches), "
+          f"k=8 {res[8][0]:.3f} ms/step ({res[8][1]} pair launches)")
+    assert res[1][1] == 32 and res[8][1] == 4
+    assert res[8][0] < 0.5 * res[1][0]
+    assert not np.array_equal(res[1][2], res[8][2])
+
+
+def test_batch_with_intervals_equals_alone(gpu_lib):
+    from tests.test_gpu_batch import alone
+
+    specs = [(2048, 1, 1, False, 4), (5000, 2, 2, True, 1), (9000, 3, 3, False, 3),
+             (16384, 2, 4, True, 8)]
+    cases = []
+    for N, P, seed, coll, k in specs:
+        h, p, v = member(N, P, seed, coll)
+        h.cfg.force_every = k
+        cases.append((h, p, v))
+    ref = [alone(h, p, v, 12) for h, p, v in cases]
+    with _lib.Batch() as b:
+        slots = [b.add(h, p, v) for h, p, v in cases[:2]]
+        b.step(3)                                  # members 3 and 4 join 3 steps later: their
+        slots += [b.add(h, p, v) for h, p, v in cases[2:]]   # phases differ from the others'
+        b.step(9)
+        for slot, r in zip(slots[:2], ref[:2]):
+            m = b.member(slot)
+            p, v = m.get_state()
+            same(r, (m.series(0, 12), p, v))
+        b.step(3)
+        for slot, r in zip(slots[2:], ref[2:]):
+            m = b.member(slot)
+            p, v = m.get_state()
+            same(r, (m.series(0, 12), p, v))

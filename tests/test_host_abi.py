@@ -133,12 +133,15 @@ def test_batch_pair_plan_rule():
     assert _lib.batch_pair_plan(2**16) == (256, 4, 7, 1024)
     assert _lib.batch_pair_plan(2**16 + 1) == (256, 8, 7, 2048)
     assert _lib.batch_pair_plan(2**20) == (256, 8, 7, 2048)
-    # 2^22 ions: the tile-pair matrix (206 GB) exceeds the 32 GiB budget -> directed pairs
-    assert _lib.batch_pair_plan(2**22)[2] == 5
+    # the each-pair-once kernel needs 24 bytes of accumulators per ion, whatever the size
+    assert _lib.batch_pair_plan(2**22) == (256, 8, 7, 2048)
 
 
 def test_config_device_bytes_budget_rules():
-    # host arithmetic only: the tile-pair matrices od_create would allocate by default
+    # host arithmetic only: the device memory od_create would allocate by default. The
+    # each-pair-once kernels (all pairs and cutoff tile pairs) keep three 64-bit fixed-point
+    # accumulators per ion instead of a tile-pair matrix, so no configuration needs more than
+    # about 100 bytes per ion (plus the cutoff's tile-pair list, nT^2/2 entries)
     from opendust_gb300 import build_simulation, workloads
 
     def gb(builder, N):
@@ -146,11 +149,8 @@ def test_config_device_bytes_budget_rules():
         holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, trap=np.zeros(15), **ext)
         return _lib.config_device_bytes(holder) / 1e9
 
-    # cutoff: 512-ion tiles while the dense matrix fits 64 GiB (2^19: 12.9 GB, 2^20: 51.5 GB),
-    # the cell stencil beyond (no matrix)
-    assert 12.9 < gb(workloads.field_chain, 2**19) < 13.3
-    assert 51.5 < gb(workloads.field_chain, 2**20) < 52.2
-    assert gb(workloads.field_chain, 2**21) < 1.0
-    # all pairs: 2048-ion tiles at 2^20 (12.9 GB), no matrix below 2^15
-    assert 12.9 < gb(workloads.full_plain, 2**20) < 13.3
+    assert gb(workloads.field_chain, 2**19) < 0.2
+    assert gb(workloads.field_chain, 2**20) < 0.4
+    assert gb(workloads.full_plain, 2**20) < 0.3
+    assert gb(workloads.full_plain, 2**22) < 1.2
     assert gb(workloads.small_plain, 2**14) < 0.1
