@@ -204,6 +204,59 @@ static void fill_trap_table(od_dparams* p, const double* tab, int n, double Hh, 
   }
 }
 
+// Out-of-domain trap force on a grain per unit grain charge [N/C] (opendust.py:1258-1321: the
+// gradient of the trap polynomial at the grain, times k q_s / r_D_e).
+static void out_domain_per_charge(const od_dparams& p, double x, double y, double z, double* f) {
+  const double* a = p.alpha;
+  const double L = p.lam, L2 = L * L, L4 = L2 * L2, L6 = L4 * L2, L8 = L4 * L4;
+  const double r = sqrt(x * x + y * y);
+  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r5 = r4 * r, r6 = r4 * r2, r7 = r6 * r;
+  const double z2 = z * z, z3 = z2 * z, z4 = z2 * z2, z5 = z4 * z, z6 = z4 * z2, z7 = z6 * z;
+  double fR = (-2 * a[1] * r) / L2;
+  fR += (-2 * a[3] * r * z2 - 4 * a[4] * r3) / L4;
+  fR += (-4 * a[6] * r3 * z2 - 2 * a[7] * r * z4 - 6 * a[8] * r5) / L6;
+  fR += (-4 * a[10] * r3 * z4 - 6 * a[11] * r5 * z2 - 2 * a[12] * r * z6 - 8 * a[13] * r7) / L8;
+  fR *= p.k * p.q_s / L;
+  double fH = (-2 * a[2] * z) / L2;
+  fH += (-2 * a[3] * r2 * z - 4 * a[5] * z3) / L4;
+  fH += (-2 * a[6] * r4 * z - 4 * a[7] * r2 * z3 - 6 * a[9] * z5) / L6;
+  fH += (-4 * a[10] * r4 * z3 - 2 * a[11] * r6 * z - 6 * a[12] * r2 * z5 - 8 * a[14] * z7) / L8;
+  fH *= p.k * p.q_s / L;
+  if (r == 0) { f[0] = 0; f[1] = 0; }
+  else { f[0] = fR * x / r; f[1] = fR * y / r; }
+  f[2] = fH;
+}
+
+// Per-grain constants of the FP64 tail (charge update, opendust.py:1117-1202; dust–dust force,
+// :1205-1235; out-of-domain force for the trap polynomial), so that the device tail evaluates one
+// exponential and a few products per grain and step (FP64 is slow on GB300). Needs the tail
+// constants and the grains of p; called again when grains move.
+static void tail_consts(od_dparams* p) {
+  const double pi = OD_PI_D;
+  for (int g = 0; g < p->P; g++) {
+    const double r = p->grs[g], S = r * r * 4.0 * pi;
+    // gamma_e dt S e with gamma_e = n_inf sqrt(T_e k_B / pi / m_e / 2) exp(-e k q / r / T_e / k_B)
+    p->ge_pref[g] = p->n_inf * sqrt(p->T_e * p->k_B / pi / p->m_e / 2.0) * p->dt * S * p->e;
+    p->ge_arg[g] = -p->e * p->k / r / p->T_e / p->k_B;
+    // OML: gamma_i dt S |e| with gamma_i = n_inf v_ti u/4 ((1 + 1/(2u*2) + chi/u^2) erf(u)
+    // + exp(-u^2)/(u sqrt(pi))), chi = e k q / r / T_n / k_B (the reference's literal 2*u*2)
+    const double u = p->v_fl_si / p->v_T_si / sqrt(2.0);
+    const double v_ti = p->v_T_si * sqrt(2.0);
+    const double c0 = p->n_inf * v_ti * u / 4.0 * p->dt * S * fabs(p->e);
+    p->oml_a[g] = c0 * ((1.0 + 1.0 / (2.0 * u * 2)) * erf(u) + 1.0 / u / sqrt(pi) * exp(-(u * u)));
+    p->oml_b[g] = c0 * erf(u) / (u * u) * (p->e * p->k / r / p->T_n / p->k_B);
+    for (int j = 0; j < p->P; j++) {
+      double* d = p->dd[g][j];
+      if (j == g) { d[0] = d[1] = d[2] = 0.0; continue; }
+      const double dx = p->gxs[g] - p->gxs[j], dy = p->gys[g] - p->gys[j], dz = p->gzs[g] - p->gzs[j];
+      const double rr = sqrt(dx * dx + dy * dy + dz * dz);
+      const double kk = p->k / (rr * rr * rr);
+      d[0] = kk * dx; d[1] = kk * dy; d[2] = kk * dz;
+    }
+    if (p->trap_kind == OD_TRAP_POLY) out_domain_per_charge(*p, p->gxs[g], p->gys[g], p->gzs[g], p->gout[g]);
+  }
+}
+
 static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   memset(p, 0, sizeof(*p));
   const double pi = OD_PI_D;
@@ -290,6 +343,7 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->n_inf = c->n_inf; p->T_e = c->T_e; p->T_n = c->T_n; p->k_B = c->k_B; p->m_e = c->m_e;
   p->e = c->e; p->E = c->E; p->v_T_si = c->v_T; p->v_fl_si = c->v_fl;
   p->n_steps = c->n_steps; p->avg_start = c->avg_start;
+  tail_consts(p);
 }
 
 // Default all-pairs plan: packed f32x2 arithmetic on SoA tiles with one target per thread
@@ -654,6 +708,7 @@ extern "C" od_status od_set_trap_table(od_handle* h, const double* trap_tab, int
   fill_trap_table(&h->hp, trap_tab, n, h->cfg.H / lam, A_ii);
   for (int g = 0; g < h->P; g++)
     for (int d = 0; d < 3; d++) h->hp.gout[g][d] = grain_out ? grain_out[3 * g + d] : 0.0;
+  tail_consts(&h->hp);
   h->cfg.trap_kind = h->hp.trap_kind;
   h->cfg.trap_n = n;
   OD_CK(h, cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
@@ -680,6 +735,7 @@ extern "C" od_status od_set_grains(od_handle* h, const double* x, const double* 
     if (grain_out)
       for (int d = 0; d < 3; d++) p.gout[g][d] = grain_out[3 * g + d];
   }
+  tail_consts(&p);
   OD_CK(h, cudaMemcpyAsync(h->dp, &h->hp, sizeof(od_dparams), cudaMemcpyHostToDevice, h->stream));
   OD_CK(h, cudaMemcpyAsync(reinterpret_cast<char*>(h->ds) + offsetof(od_dstate, q_param), q,
                            sizeof(double) * h->P, cudaMemcpyHostToDevice, h->stream));

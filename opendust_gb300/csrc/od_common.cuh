@@ -66,6 +66,11 @@ struct od_dparams {
   // charge [N/C] (OD_TRAP_TABLE)
   double gfield[OD_MAX_GRAINS];
   double gout[OD_MAX_GRAINS][3];
+  // per-grain constants of the FP64 tail, precomputed on the host (tail_consts): the electron
+  // term of the charge update is ge_pref exp(ge_arg q), the OML ion term oml_a + oml_b q; the
+  // dust–dust force on grain g is q_g sum_j q_j dd[g][j] (N/C^2)
+  double ge_pref[OD_MAX_GRAINS], ge_arg[OD_MAX_GRAINS], oml_a[OD_MAX_GRAINS], oml_b[OD_MAX_GRAINS];
+  double dd[OD_MAX_GRAINS][OD_MAX_GRAINS][3];
 };
 
 // Per-simulation FP64 accumulators and bookkeeping, resident in device memory.

@@ -874,97 +874,65 @@ __global__ void __launch_bounds__(kBlk) k_correct_orbit(
 // ============================================================== K6: FP64 host-tail on device
 // opendust.py:1117-1202 (charge), :1205-1235 (dust–dust), :1237-1331 (orbit + out-of-domain),
 // :1333-1365 (collect), :1367-1383 (field)
-__device__ double charge_update(const od_dparams& p, int g, double q_prev, double dN) {
-  const double r = p.grs[g];
-  const double phi = p.k * q_prev / r;
-  const double gamma_e = p.n_inf * pow(p.T_e * p.k_B / OD_PI_D / p.m_e / 2.0, 0.5) *
-                         exp(-p.e * phi / p.T_e / p.k_B);
-  const double S = r * r * 4.0 * OD_PI_D;
-  if (p.gmethod[g] == OD_CHARGE_CONSISTENT) return q_prev + (dN * p.q_s + gamma_e * p.dt * S * p.e);
-  if (p.gmethod[g] == OD_CHARGE_OML) {
-    const double u = p.v_fl_si / p.v_T_si / sqrt(2.0);
-    const double chi = p.e * phi / p.T_n / p.k_B;
-    const double v_ti = p.v_T_si * sqrt(2.0);
-    const double gamma_i = p.n_inf * v_ti * u / 4.0 *
-                           ((1.0 + 1.0 / (2.0 * u * 2) + chi / (u * u)) * erf(u) +
-                            1.0 / u / sqrt(OD_PI_D) * exp(-(u * u)));
-    return q_prev + (gamma_i * p.dt * S * fabs(p.e) + gamma_e * p.dt * S * p.e);
-  }
+// charge of grain g after a step with dN collected ions (opendust.py:1117-1202), from the
+// host-precomputed constants of tail_consts
+__device__ __forceinline__ double charge_update(const od_dparams& p, int g, double q_prev,
+                                                double dN) {
+  const double ge = p.ge_pref[g] * exp(p.ge_arg[g] * q_prev);
+  if (p.gmethod[g] == OD_CHARGE_CONSISTENT) return q_prev + (dN * p.q_s + ge);
+  if (p.gmethod[g] == OD_CHARGE_OML) return q_prev + (fma(p.oml_b[g], q_prev, p.oml_a[g]) + ge);
   return q_prev;
 }
 
-__device__ void out_domain_force(const od_dparams& p, double x, double y, double z, double q,
-                                 double* f) {
-  const double* a = p.alpha;
-  const double L = p.lam, L2 = L * L, L4 = L2 * L2, L6 = L4 * L2, L8 = L4 * L4;
-  const double r = sqrt(x * x + y * y);
-  const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r5 = r4 * r, r6 = r4 * r2, r7 = r6 * r;
-  const double z2 = z * z, z3 = z2 * z, z4 = z2 * z2, z5 = z4 * z, z6 = z4 * z2, z7 = z6 * z;
-  double fR = (-2 * a[1] * r) / L2;
-  fR += (-2 * a[3] * r * z2 - 4 * a[4] * r3) / L4;
-  fR += (-4 * a[6] * r3 * z2 - 2 * a[7] * r * z4 - 6 * a[8] * r5) / L6;
-  fR += (-4 * a[10] * r3 * z4 - 6 * a[11] * r5 * z2 - 2 * a[12] * r * z6 - 8 * a[13] * r7) / L8;
-  fR *= p.k * q * p.q_s / L;
-  double fH = (-2 * a[2] * z) / L2;
-  fH += (-2 * a[3] * r2 * z - 4 * a[5] * z3) / L4;
-  fH += (-2 * a[6] * r4 * z - 4 * a[7] * r2 * z3 - 6 * a[9] * z5) / L6;
-  fH += (-4 * a[10] * r4 * z3 - 2 * a[11] * r6 * z - 6 * a[12] * r2 * z5 - 8 * a[14] * z7) / L8;
-  fH *= p.k * q * p.q_s / L;
-  if (r == 0) { f[0] = 0; f[1] = 0; }
-  else { f[0] = fR * x / r; f[1] = fR * y / r; }
-  f[2] = fH;
-}
-
+// FP64 tail of one step (opendust.py:1117-1383): orbit sums over the blocks' partials in a fixed
+// order (all components at once), then one thread per grain for the charge update and the
+// grain forces, from the host-precomputed constants.
 __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __restrict__ ds,
                                           const double* __restrict__ orbit_part, int nb,
                                           double* __restrict__ s_q, double* __restrict__ s_orbit,
                                           double* __restrict__ s_collect,
                                           double* __restrict__ s_dust,
                                           double* __restrict__ s_field, float* __restrict__ cq) {
-  __shared__ double s_red[kBlk];
+  __shared__ double s_red[kBlk / 32][OD_MAX_GRAINS * 3];
   __shared__ double S[OD_MAX_GRAINS * 3];
-  const int tid = threadIdx.x;
-  const int nc = p.P * 3;
+  __shared__ double qn[OD_MAX_GRAINS];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int P = p.P, nc = P * 3;
   for (int c = 0; c < nc; c++) {
     double v = 0;
     for (int b = tid; b < nb; b += kBlk) v += orbit_part[(size_t)b * nc + c];
-    s_red[tid] = v;
-    __syncthreads();
-    for (int w = kBlk / 2; w > 0; w >>= 1) {
-      if (tid < w) s_red[tid] += s_red[tid + w];
-      __syncthreads();
-    }
-    if (tid == 0) S[c] = s_red[0];
-    __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[w][c] = v;
   }
-  if (tid != 0) return;
   const int64_t step = ds->step;
-  const int P = p.P;
-  double qn[OD_MAX_GRAINS];
-  for (int g = 0; g < P; g++)
-    qn[g] = step > 0 ? charge_update(p, g, ds->q_param[g], ds->dN[g]) : ds->q_param[g];
+  if (tid < P)
+    qn[tid] = step > 0 ? charge_update(p, tid, ds->q_param[tid], ds->dN[tid]) : ds->q_param[tid];
+  __syncthreads();
+  if (tid < nc) {
+    double v = 0;
+    for (int k = 0; k < kBlk / 32; k++) v += s_red[k][tid];
+    S[tid] = v;
+  }
+  __syncthreads();
   const bool avg = step >= p.avg_start;
-  for (int g = 0; g < P; g++) {
+  if (tid < P) {
+    const int g = tid;
     double fd[3] = {0, 0, 0};
     for (int j = 0; j < P; j++) {
       if (j == g) continue;
-      const double dx = p.gxs[g] - p.gxs[j], dy = p.gys[g] - p.gys[j], dz = p.gzs[g] - p.gzs[j];
-      const double r = sqrt(dx * dx + dy * dy + dz * dz);
-      const double kk = p.k * qn[g] * qn[j] / (r * r * r);
-      fd[0] += kk * dx; fd[1] += kk * dy; fd[2] += kk * dz;
+      fd[0] = fma(qn[j], p.dd[g][j][0], fd[0]);
+      fd[1] = fma(qn[j], p.dd[g][j][1], fd[1]);
+      fd[2] = fma(qn[j], p.dd[g][j][2], fd[2]);
     }
-    double fo[3] = {0, 0, 0};
-    if (p.trap_kind == OD_TRAP_POLY) out_domain_force(p, p.gxs[g], p.gys[g], p.gzs[g], qn[g], fo);
-    else if (p.trap_kind == OD_TRAP_TABLE)
-      for (int d = 0; d < 3; d++) fo[d] = qn[g] * p.gout[g][d];
     const double so = qn[g] * p.k * p.q_s / (p.lam * p.lam);
     const double sc = p.vunit * p.m_s / p.dt;
     double vals[13];
     vals[0] = qn[g];
     for (int d = 0; d < 3; d++) {
-      vals[1 + d] = S[g * 3 + d] * so + fo[d];
+      vals[1 + d] = S[g * 3 + d] * so + qn[g] * p.gout[g][d];
       vals[4 + d] = ds->M[g][d] * sc;
-      vals[7 + d] = fd[d];
+      vals[7 + d] = qn[g] * fd[d];
       vals[10 + d] = d == 2 ? qn[g] * p.gfield[g] : 0.0;
     }
     const size_t r = (size_t)step * P + g;
@@ -977,14 +945,15 @@ __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __rest
     }
     if (avg)
       for (int m = 0; m < 13; m++) ds->avg[g][m] += vals[m];
-  }
-  for (int g = 0; g < P; g++) {
     ds->q_param[g] = qn[g];
     cq[g] = (float)(p.A_id_d * qn[g]);
   }
-  if (avg) ds->n_avg += 1;
-  ds->n_inj_total += ds->nlist;
-  ds->step = step + 1;
+  __syncthreads();  // every grain has read ds->step
+  if (tid == 0) {
+    if (avg) ds->n_avg += 1;
+    ds->n_inj_total += ds->nlist;
+    ds->step = step + 1;
+  }
 }
 
 __global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp,
