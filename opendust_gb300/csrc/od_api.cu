@@ -100,6 +100,12 @@ static void split2(double d, float& hi, float& lo) {
   lo = (float)(d - (double)hi);
 }
 
+// Plans whose ion–ion sums go to the fixed-point accumulators b.n3 (directed packed variants
+// 2-6 and the each-pair-once variant 7; not the cutoff, not the scalar variants 0 and 1).
+static bool uses_acc(const od_handle* h) {
+  return !h->has_cut && h->b.n3 && h->plan.variant >= 2;
+}
+
 static od_force_ctx force_ctx(const od_handle* h, bool count_pairs) {
   od_force_ctx fc{};
   fc.plan = h->plan;
@@ -108,9 +114,13 @@ static od_force_ctx force_ctx(const od_handle* h, bool count_pairs) {
   fc.rc = h->hp.rc;
   fc.rs = h->hp.rs;
   fc.pair_count = (count_pairs && h->has_cut) ? h->d_pairs : nullptr;
+  fc.acc = uses_acc(h) ? h->b.n3 : nullptr;
   return fc;
 }
-static int force_jsplit(const od_handle* h) { return h->has_cut ? 1 : h->plan.jsplit; }
+// slabs that hold the ion–ion sums after od_launch_force with take = true
+static int force_jsplit(const od_handle* h) {
+  return h->has_cut || uses_acc(h) ? 1 : h->plan.jsplit;
+}
 
 static od_status validate(const od_config* c) {
   if (!c) return fail(nullptr, OD_ERR_INVALID, "config is NULL");
@@ -420,6 +430,7 @@ static od_status alloc_scratch_for_plan(od_handle* h) {
 static od_status create_handle(const od_config* cfg, int32_t device, bool n3_default,
                                od_handle** out);
 static od_status alloc_cutn3(od_handle* h, int ipt, int T);
+static od_status ensure_acc(od_handle* h);
 
 extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle** out) {
   return create_handle(cfg, device, true, out);
@@ -483,6 +494,7 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
   OD_CKC(dalloc(&h->b.sy, Np));
   OD_CKC(dalloc(&h->b.sz, Np));
   if (alloc_scratch_for_plan(h) != OD_OK) return bail(OD_ERR_OOM);
+  if (cfg->force_method != OD_FORCE_CUTOFF && ensure_acc(h) != OD_OK) return bail(OD_ERR_OOM);
   int n3_ipt = 0, n3_tile = 0;
   if (n3_default && cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default(h->Npad))
     n3_tile = od_n3_default(h->Npad, OD_N3_BUDGET, &n3_ipt);
@@ -1025,6 +1037,21 @@ static void free_n3(od_handle* h) {
   h->b.n3_len = 0;
 }
 
+// The fixed-point ion–ion accumulators (three 64-bit words per ion, zero between evaluations).
+static od_status ensure_acc(od_handle* h) {
+  const size_t need = od_n3_floats(h->Npad, 1);  // in units of 4 bytes
+  if (h->b.n3 && h->b.n3_len >= need) return OD_OK;
+  free_n3(h);
+  if (cudaMalloc((void**)&h->b.n3, sizeof(float) * need) != cudaSuccess) {
+    cudaGetLastError();
+    h->b.n3 = nullptr;
+    return fail(h, OD_ERR_OOM, "no device memory for the ion–ion accumulators");
+  }
+  h->b.n3_len = need;
+  OD_CK(h, cudaMemset(h->b.n3, 0, sizeof(float) * need));
+  return OD_OK;
+}
+
 // Variant 7: `ions_per_lane` targets per lane (2 or 4 with as many sources, 8 with two sources),
 // `tile` ions per tile (1024, 2048, 4096; <= 0: 1024 up to 2^17 ions, else 2048). The pair
 // sums go to three 64-bit fixed-point accumulators per ion (24 bytes per ion: 25 MB at 2^20).
@@ -1096,7 +1123,10 @@ extern "C" od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t tar
   if (variant == 7) return set_plan_n3(h, targets_per_thread, jsplit);
   if (h->Npad % (threads * targets_per_thread) != 0)
     return fail(h, OD_ERR_INVALID, "block does not divide the padded ion count");
-  free_n3(h);
+  if (variant >= 2) {
+    od_status st = ensure_acc(h);
+    if (st != OD_OK) return st;
+  }
   od_pair_plan pl{};
   pl.nt = threads; pl.ipt = targets_per_thread; pl.variant = variant;
   if (jsplit <= 0) {
@@ -1896,10 +1926,11 @@ extern "C" od_status od_shard_create(const od_config* cfg, int64_t first, int64_
   return OD_OK;
 }
 
-static od_status shard_forces_now(od_handle* h) {
+// take: into slab 0 of the partial sums (initial state); else left in the accumulators for K3
+static od_status shard_forces_now(od_handle* h, bool take) {
   OD_CK(h, od_launch_shard_pairs(h->plan, h->ssx, h->ssy, h->ssz, h->Npad_total, h->Npad,
                                  (int)h->ion0, h->b.part_hi, h->b.part_lo, h->hp.rho0, &h->ds->err,
-                                 h->stream));
+                                 h->b.n3, take, h->stream));
   return OD_OK;
 }
 
@@ -1920,10 +1951,10 @@ extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
   }
   OD_CK(h, cudaMemcpy(h->b.pos, xo.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
   OD_CK(h, cudaMemcpy(h->b.vel, vp.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
-  od_status st = shard_forces_now(h);
+  od_status st = shard_forces_now(h, true);
   if (st != OD_OK) return st;
-  OD_CK(h, od_launch_reduce(h->dp, h->Npad, h->plan.jsplit, h->b.part_hi, h->b.part_lo, h->b.fhi,
-                            h->b.flo, h->stream));
+  OD_CK(h, od_launch_reduce(h->dp, h->Npad, 1, h->b.part_hi, h->b.part_lo, h->b.fhi, h->b.flo,
+                            h->stream));
   OD_CK(h, cudaStreamSynchronize(h->stream));
   h->state_set = true;
   h->shard_phase = 0;
@@ -1953,7 +1984,7 @@ extern "C" od_status od_shard_forces(od_handle* h, const float* xyz_all, int64_t
   for (int d = 0; d < 3; d++)
     OD_CK(h, cudaMemcpyAsync(dst[d], xyz_all + (size_t)d * h->n_total, sizeof(float) * h->n_total,
                              cudaMemcpyDefault, h->stream));
-  st = shard_forces_now(h);
+  st = shard_forces_now(h, false);
   if (st != OD_OK) return st;
   OD_CK(h, od_launch_shard_part(1, h->dp, h->ds, h->b, h->N, h->Npad, h->plan.jsplit, nullptr,
                                 nullptr, nullptr, h->stream));

@@ -53,7 +53,7 @@ int od_n3_default(int Npad, size_t budget_bytes, int* ipt);
 size_t od_n3_floats(int Npad, int tile);
 cudaError_t od_n3_prepare(const od_pair_plan& pl);  // shared-memory opt-in, current device
 cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
-                               float4* pl_lo, float rho0, cudaStream_t s);
+                               float4* pl_lo, float rho0, cudaStream_t s, bool take = true);
 
 // One member of a batch, as the batched kernels see it.
 struct od_simdesc {
@@ -151,7 +151,8 @@ cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, 
                                     double r0, double scale, double* force, cudaStream_t s);
 
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* part_hi,
-                            float4* part_lo, float rho0, uint32_t* err, cudaStream_t s);
+                            float4* part_lo, float rho0, uint32_t* err, cudaStream_t s,
+                            bool take = true);
 // the same launch restricted to the first gridx_limit target blocks (autotuner probes)
 cudaError_t od_launch_pairs_probe(const od_pair_plan& pl, const od_pair_io& io, int Npad,
                                   int gridx_limit, float4* part_hi, float4* part_lo, float rho0,
@@ -169,9 +170,12 @@ struct od_force_ctx {
   const od_cutlist* cut;
   float rho0, rc, rs;
   unsigned long long* pair_count;  // pairs inside the cutoff (cutoff path, optional)
+  unsigned long long* acc;         // fixed-point ion–ion accumulators that K3 takes (or NULL)
 };
+// take: leave the ion–ion sums in slab 0 of (part_hi, part_lo) (false: in the accumulators)
 cudaError_t od_launch_force(const od_force_ctx& fc, const od_pair_io& io, int n, int Npad,
-                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s);
+                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s,
+                            bool take = true);
 cudaError_t od_launch_step(const od_dparams* dp, od_dstate* ds, const od_dbufs& b, int N, int Npad,
                            int P, const od_force_ctx& fc, int nrec, cudaStream_t s);
 cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, const od_dbufs& b,
@@ -188,7 +192,7 @@ cudaError_t od_launch_shard_part(int part, const od_dparams* dp, od_dstate* ds, 
 cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const float* sy,
                                   const float* sz, int nsrc_pad, int Npad_local, int tgt_off,
                                   float4* ph, float4* plo, float rho0, uint32_t* err,
-                                  cudaStream_t s);
+                                  unsigned long long* acc, bool take, cudaStream_t s);
 cudaError_t od_launch_shard_list(const od_dparams* dp, od_dstate* ds, int K, const int32_t* gidx,
                                  const int32_t* gbits, const float4* gnew, const float4* gv,
                                  float* sx, float* sy, float* sz, cudaStream_t s);

@@ -219,7 +219,9 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
                                               float4* __restrict__ part_hi,
                                               float4* __restrict__ part_lo, float rho0,
                                               float newton_r2, uint32_t* __restrict__ err,
-                                              int tgt_off = 0) {
+                                              int tgt_off = 0,
+                                              unsigned long long* __restrict__ acc = nullptr,
+                                              size_t acc_stride = 0) {
   __shared__ __align__(128) float tx[2][OD_TJ];
   __shared__ __align__(128) float ty[2][OD_TJ];
   __shared__ __align__(128) float tz[2][OD_TJ];
@@ -322,12 +324,24 @@ __device__ __forceinline__ bool pairs_x2_body(const float* __restrict__ sx,
     }
     return false;
   }
-  const size_t off = slab_off;
-  part_hi[off + i0] = make_float4(h0x, h0y, h0z, 0.f);
-  part_lo[off + i0] = make_float4(l0x, l0y, l0z, 0.f);
-  if (TPT == 2) {
-    part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
-    part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+  if (acc) {
+    // fixed-point accumulators: the source chunks of a target add up in any order
+    od_fix_add(acc + i0, h0x, l0x);
+    od_fix_add(acc + acc_stride + i0, h0y, l0y);
+    od_fix_add(acc + 2 * acc_stride + i0, h0z, l0z);
+    if (TPT == 2) {
+      od_fix_add(acc + i1, h1x, l1x);
+      od_fix_add(acc + acc_stride + i1, h1y, l1y);
+      od_fix_add(acc + 2 * acc_stride + i1, h1z, l1z);
+    }
+  } else {
+    const size_t off = slab_off;
+    part_hi[off + i0] = make_float4(h0x, h0y, h0z, 0.f);
+    part_lo[off + i0] = make_float4(l0x, l0y, l0z, 0.f);
+    if (TPT == 2) {
+      part_hi[off + i1] = make_float4(h1x, h1y, h1z, 0.f);
+      part_lo[off + i1] = make_float4(l1x, l1y, l1z, 0.f);
+    }
   }
   // release the barriers so that the next call of this body (persistent loop) can init them
   __syncthreads();
@@ -341,10 +355,24 @@ __global__ void __launch_bounds__(NT) k_pairs_x2(const float* __restrict__ sx,
                                                  const float* __restrict__ sz, int Npad, int chunk,
                                                  float4* __restrict__ part_hi,
                                                  float4* __restrict__ part_lo, float rho0,
-                                                 float newton_r2, uint32_t* __restrict__ err) {
+                                                 float newton_r2, uint32_t* __restrict__ err,
+                                                 unsigned long long* __restrict__ acc) {
   const int j0 = blockIdx.y * chunk;
   pairs_x2_body<NT, NEWTON, TPT>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, Npad),
-                                 (size_t)blockIdx.y * Npad, part_hi, part_lo, rho0, newton_r2, err);
+                                 (size_t)blockIdx.y * Npad, part_hi, part_lo, rho0, newton_r2, err,
+                                 0, acc, (size_t)Npad);
+}
+
+// Fixed-point accumulators -> slab 0 of (ph, pl) as two-float sums, cleared for the next
+// evaluation (the forms that read slabs: initial sums, snapshots, autotuner probes).
+__global__ void k_acc_take(unsigned long long* __restrict__ acc, int Npad, float4* __restrict__ ph,
+                           float4* __restrict__ pl) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= Npad) return;
+  float3 hi, lo;
+  od_fix_take(acc + i, (size_t)Npad, hi, lo);
+  ph[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
+  pl[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
 }
 
 __global__ void k_aos_to_soa(const float4* __restrict__ pos, int Npad, float* __restrict__ sx,
@@ -466,7 +494,8 @@ __device__ __forceinline__ void kick_flag_body(const od_dparams& p, const od_dst
                                                const float4* __restrict__ pl, int jsplit,
                                                float4* __restrict__ fhi, float4* __restrict__ flo,
                                                uint32_t* __restrict__ flags,
-                                               const float* __restrict__ cq, int i) {
+                                               const float* __restrict__ cq, int i,
+                                               unsigned long long* __restrict__ acc = nullptr) {
   int flag = 0;
   if (i < p.N) {
     // a step without an ion–ion evaluation (force interval k > 1) keeps the stored sums and
@@ -474,7 +503,9 @@ __device__ __forceinline__ void kick_flag_body(const od_dparams& p, const od_dst
     float3 hi = make_float3(0.f, 0.f, 0.f), lo = make_float3(0.f, 0.f, 0.f);
     float aii = 0.f;
     if (od_evaluates(p.force_every, ds->step)) {
-      reduce_parts(ph, pl, p.Npad, jsplit, i, hi, lo);
+      // from the fixed-point accumulators (and cleared), or from the partial slabs
+      if (acc) od_fix_take(acc + i, (size_t)p.Npad, hi, lo);
+      else reduce_parts(ph, pl, p.Npad, jsplit, i, hi, lo);
       fhi[i] = make_float4(hi.x, hi.y, hi.z, 0.f);
       flo[i] = make_float4(lo.x, lo.y, lo.z, 0.f);
       aii = p.force_every > 1 ? p.A_ii * (float)p.force_every : p.A_ii;
@@ -502,9 +533,10 @@ __global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict
                                                     float4* __restrict__ fhi,
                                                     float4* __restrict__ flo,
                                                     uint32_t* __restrict__ flags,
-                                                    const float* __restrict__ cq) {
+                                                    const float* __restrict__ cq,
+                                                    unsigned long long* __restrict__ acc) {
   kick_flag_body(*dp, ds, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq,
-                 blockIdx.x * blockDim.x + threadIdx.x);  // grid covers Npad exactly
+                 blockIdx.x * blockDim.x + threadIdx.x, acc);  // grid covers Npad exactly
 }
 
 __global__ void __launch_bounds__(kBlk) k_flags_only(const od_dparams* __restrict__ dp, int n,
@@ -1096,12 +1128,12 @@ static void launch_pairs_x2(const od_pair_plan& pl, const od_pair_io& io, int Np
   dim3 grid(gx_of(Npad / (NT * TPT)), pl.jsplit);
   const float nr = 64.0f * rho0;  // Newton (2 steps) keeps 1/s within 2^-24 for r > 64 r0
   k_pairs_x2<NT, NEWTON, TPT><<<grid, NT, 0, s>>>(io.sx, io.sy, io.sz, Npad, pl.chunk, ph, plo,
-                                                  rho0, nr * nr, err);
+                                                  rho0, nr * nr, err, io.n3);
 }
 
 cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
-                            float4* plo, float rho0, uint32_t* err, cudaStream_t s) {
-  if (pl.variant == 7) return od_launch_pairs_n3(pl, io, Npad, ph, plo, rho0, s);
+                            float4* plo, float rho0, uint32_t* err, cudaStream_t s, bool take) {
+  if (pl.variant == 7) return od_launch_pairs_n3(pl, io, Npad, ph, plo, rho0, s, take);
   const int key = pl.nt * 100 + pl.ipt * 10 + pl.variant;
   const float4* pos = io.pos;
   switch (key) {
@@ -1124,6 +1156,9 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Np
     case 25616: launch_pairs_x2<256, 2, 1>(pl, io, Npad, ph, plo, rho0, err, s); break;
     default: return cudaErrorInvalidValue;
   }
+  // variants 2-6 with accumulators (io.n3): into slab 0 unless the caller takes them itself
+  if (io.n3 && pl.variant >= 2 && take)
+    k_acc_take<<<(Npad + 255) / 256, 256, 0, s>>>(io.n3, Npad, ph, plo);
   return cudaGetLastError();
 }
 
@@ -1150,11 +1185,12 @@ cudaError_t od_launch_reduce(const od_dparams* dp, int Npad, int jsplit, const f
 }
 
 cudaError_t od_launch_force(const od_force_ctx& fc, const od_pair_io& io, int n, int Npad,
-                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s) {
+                            float4* part_hi, float4* part_lo, uint32_t* err, cudaStream_t s,
+                            bool take) {
   if (fc.cut)
     return od_launch_cutoff(*fc.cut, io.pos, n, Npad, part_hi, part_lo, fc.rho0, fc.rc, fc.rs, err,
                             fc.pair_count, s);
-  return od_launch_pairs(fc.plan, io, Npad, part_hi, part_lo, fc.rho0, err, s);
+  return od_launch_pairs(fc.plan, io, Npad, part_hi, part_lo, fc.rho0, err, s, take);
 }
 
 // part 0: K1 (kick/drift); part 1: K2 (ion–ion sums); part 2: K3..K6
@@ -1168,12 +1204,13 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
                                                         b.sx, b.sy, b.sz);
     return cudaGetLastError();
   }
+  // with accumulators (fc.acc) K3 takes the ion–ion sums from them
   if (part == 1)
     return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz, b.n3}, N, Npad, b.part_hi, b.part_lo,
-                           &ds->err, s);
+                           &ds->err, s, fc.acc == nullptr);
   const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
   k_kick_flag<<<nb, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
-                                  b.flags, b.cq);
+                                  b.flags, b.cq, fc.acc);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
   k_correct_orbit<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
@@ -1301,7 +1338,7 @@ cudaError_t od_launch_static_forces(const od_static_view& v, const double* pos, 
   const float nr = 64.0f * rho0;
   dim3 grid(Npad / 512, jsplit);
   k_pairs_x2<256, 0><<<grid, 256, 0, s>>>(v.sx, v.sy, v.sz, Npad, chunk, v.part_hi, v.part_lo,
-                                          rho0, nr * nr, v.err);
+                                          rho0, nr * nr, v.err, nullptr);  // partial slabs
   k_static_finish<<<(n + kBlk - 1) / kBlk, kBlk, 0, s>>>(v.part_hi, v.part_lo, n, Npad, jsplit,
                                                         scale, force);
   return cudaGetLastError();
@@ -1471,17 +1508,18 @@ __global__ void __launch_bounds__(NT) k_shard_pairs(const float* __restrict__ sx
                                                     int chunk, int Npad_local, int tgt_off,
                                                     float4* __restrict__ part_hi,
                                                     float4* __restrict__ part_lo, float rho0,
-                                                    float newton_r2, uint32_t* __restrict__ err) {
+                                                    float newton_r2, uint32_t* __restrict__ err,
+                                                    unsigned long long* __restrict__ acc) {
   const int j0 = blockIdx.y * chunk;
   pairs_x2_body<NT, NEWTON, TPT>(sx, sy, sz, blockIdx.x, j0, min(j0 + chunk, nsrc_pad),
                                  (size_t)blockIdx.y * Npad_local, part_hi, part_lo, rho0,
-                                 newton_r2, err, tgt_off);
+                                 newton_r2, err, tgt_off, acc, (size_t)Npad_local);
 }
 
 cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const float* sy,
                                   const float* sz, int nsrc_pad, int Npad_local, int tgt_off,
                                   float4* ph, float4* plo, float rho0, uint32_t* err,
-                                  cudaStream_t s) {
+                                  unsigned long long* acc, bool take, cudaStream_t s) {
   const int tpt = (pl.variant == 5 || pl.variant == 6) ? 1 : 2;
   if (pl.variant < 2 || pl.variant > 6 || (pl.nt != 128 && pl.nt != 256) || pl.ipt != tpt ||
       Npad_local % (tpt * pl.nt) || pl.chunk % OD_TJ || tgt_off % OD_PAD)
@@ -1490,7 +1528,7 @@ cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const
   const float nr = 64.0f * rho0, nr2 = nr * nr;  // as launch_pairs_x2
 #define OD_SHARD_PAIRS(NT, NW, TP)                                                              \
   k_shard_pairs<NT, NW, TP><<<grid, NT, 0, s>>>(sx, sy, sz, nsrc_pad, pl.chunk, Npad_local,    \
-                                                tgt_off, ph, plo, rho0, nr2, err)
+                                                tgt_off, ph, plo, rho0, nr2, err, acc)
   switch (pl.nt * 100 + pl.variant) {
     case 12802: OD_SHARD_PAIRS(128, 0, 2); break;
     case 25602: OD_SHARD_PAIRS(256, 0, 2); break;
@@ -1505,6 +1543,7 @@ cudaError_t od_launch_shard_pairs(const od_pair_plan& pl, const float* sx, const
     default: return cudaErrorInvalidValue;
   }
 #undef OD_SHARD_PAIRS
+  if (take) k_acc_take<<<(Npad_local + 255) / 256, 256, 0, s>>>(acc, Npad_local, ph, plo);
   return cudaGetLastError();
 }
 
@@ -1542,7 +1581,7 @@ cudaError_t od_launch_shard_part(int part, const od_dparams* dp, od_dstate* ds, 
     return cudaGetLastError();
   }
   k_kick_flag<<<Npad / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit,
-                                          b.fhi, b.flo, b.flags, b.cq);
+                                          b.fhi, b.flo, b.flags, b.cq, b.n3);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
   return cudaGetLastError();

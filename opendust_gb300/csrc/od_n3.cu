@@ -93,13 +93,13 @@ __global__ void k_b_n3_take(const od_simdesc* __restrict__ sims, const int2* __r
 
 template <int MT, int MS, int PA>
 cudaError_t launch_n3(const od_pair_io& io, int Npad, unsigned long long* acc, float4* ph,
-                      float4* pl, float rho0, cudaStream_t s) {
+                      float4* pl, float rho0, cudaStream_t s, bool take) {
   using TR = n3_traits<MT, MS, PA>;
   const int nT = (Npad + TR::T - 1) / TR::T;
   const long long nblk = (long long)nT * (nT + 1) / 2;
   k_pairs_n3<MT, MS, PA><<<(unsigned)nblk, kWarps * 32, TR::SMEM, s>>>(io.sx, io.sy, io.sz, Npad,
                                                                       acc, rho0);
-  k_n3_take<<<(Npad + 255) / 256, 256, 0, s>>>(acc, Npad, ph, pl);
+  if (take) k_n3_take<<<(Npad + 255) / 256, 256, 0, s>>>(acc, Npad, ph, pl);
   return cudaGetLastError();
 }
 
@@ -139,9 +139,9 @@ cudaError_t od_n3_prepare(const od_pair_plan& pl) {
 }
 
 cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int Npad, float4* ph,
-                               float4* plo, float rho0, cudaStream_t s) {
+                               float4* plo, float rho0, cudaStream_t s, bool take) {
   if (!io.n3) return cudaErrorInvalidValue;
-#define OD_N3_LAUNCH(a, b, c) launch_n3<a, b, c>(io, Npad, io.n3, ph, plo, rho0, s)
+#define OD_N3_LAUNCH(a, b, c) launch_n3<a, b, c>(io, Npad, io.n3, ph, plo, rho0, s, take)
   switch (pl.ipt * 10000 + pl.tile) { OD_N3_CASES(OD_N3_LAUNCH) }
 #undef OD_N3_LAUNCH
   return cudaErrorInvalidValue;
