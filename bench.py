@@ -41,11 +41,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = 25
-KERNELS_PER_STEP = 6          # all pairs: kick/drift, pairs, kick/flag, collect, correct, tail
-                              # (+ the tile-pair row sums with variant 7)
-KERNELS_PER_STEP_CUTOFF = 12  # + cell clear, count, scan, scatter, sort, chunk scan
-KERNELS_PER_STEP_CUTOFF_TILES = 16  # + clear, count, scan, scatter, sort, boxes, pairs,
-                                    # scan, list, tile-pair kernel, row sums (cutoff variant 3)
+KERNELS_PER_STEP = 5          # all pairs: kick/drift, pairs, kick/flag (takes the fixed-point
+                              # sums), collect/inject, correct/orbit (+ the FP64 tail in its
+                              # last block)
+KERNELS_PER_STEP_CUTOFF = 11  # + cell clear, count, scan, scatter, sort, chunk scan
+KERNELS_PER_STEP_CUTOFF_TILES = 15  # + clear, count, scan, scatter, sort, boxes, pairs,
+                                    # scan, list, tile-pair kernel, slot take (cutoff variant 3)
 
 
 def parse():
@@ -324,7 +325,7 @@ def run_ours(args, dist: Dist):
     if cutoff:
         launches = KERNELS_PER_STEP_CUTOFF_TILES if plan["variant"] == 3 else KERNELS_PER_STEP_CUTOFF
     else:
-        launches = KERNELS_PER_STEP + (1 if n3 else 0)
+        launches = KERNELS_PER_STEP
 
     # e2e through the C ABI with host buffers (the calls simulate() makes)
     eng.close()

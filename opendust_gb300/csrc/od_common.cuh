@@ -85,6 +85,7 @@ struct od_dstate {
   double avg[OD_MAX_GRAINS][13];      // running sums over the averaging window
   int64_t n_avg;
   int64_t n_inj_total;
+  uint32_t ticket;                    // orbit blocks of K5 done this step (0 between steps)
 };
 
 // ------------------------------------------------------------------ Philox4x32-10

@@ -673,17 +673,25 @@ __device__ void inject_one(const od_dparams& p, uint32_t ion, uint32_t step, flo
 __device__ __forceinline__ void list_sums(const od_dparams& p, od_dstate* __restrict__ ds, int K,
                                           const int32_t* __restrict__ list_bits,
                                           const float4* __restrict__ list_v) {
-  const int tid = threadIdx.x;
+  // one warp: lane l takes entries l, l + 32, ... in order, then a fixed shuffle tree (the list
+  // is short: K is the number of ions that left or hit a grain this step)
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
   for (int g = 0; g < p.P; g++) {
     double dn = 0, mx = 0, my = 0, mz = 0;
-    for (int k = tid; k < K; k += kCT)
+    for (int k = lane; k < K; k += 32)
       if ((list_bits[k] >> g) & 1) {
         const float4 v = list_v[k];
         dn += 1.0; mx += v.x; my += v.y; mz += v.z;
       }
-    dn = block_sum_1024(dn); mx = block_sum_1024(mx);
-    my = block_sum_1024(my); mz = block_sum_1024(mz);
-    if (tid == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dn += __shfl_xor_sync(0xffffffffu, dn, o);
+      mx += __shfl_xor_sync(0xffffffffu, mx, o);
+      my += __shfl_xor_sync(0xffffffffu, my, o);
+      mz += __shfl_xor_sync(0xffffffffu, mz, o);
+    }
+    if (lane == 0) { ds->dN[g] = dn; ds->M[g][0] = mx; ds->M[g][1] = my; ds->M[g][2] = mz; }
   }
 }
 
@@ -800,14 +808,16 @@ __device__ __forceinline__ void correct_orbit_body(
   // global index, the re-injected ions' full sums run over the nsrc source positions ssx..ssz
   // (all shards' ions, re-injected ones at their new positions), and only this shard's own
   // entries (global index - p.ion0 in [0, p.N)) are written
-  __shared__ double s_red[kBlk / 32];
   const int K = ds->nlist;
   const int tid = threadIdx.x;
   if (blk < nb) {
     const int i = blk * kBlk + tid;
     const bool live = i < p.N;
     const float4 x = live ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // orbit sums (opendust.py:977-1037): exp(-r)(x_p - x)(1/r^3 + 1/r^2), lambda units
+    // orbit sums (opendust.py:977-1037): exp(-r)(x_p - x)(1/r^3 + 1/r^2), lambda units; FP64
+    // warp trees for every component, then the 8 warps in order
+    __shared__ double s_orb[kBlk / 32][OD_MAX_GRAINS * 3];
+    const int lane = tid & 31, w = tid >> 5;
     for (int g = 0; g < p.P; g++) {
       float tx = 0.f, ty = 0.f, tz = 0.f;
       if (live) {
@@ -821,13 +831,20 @@ __device__ __forceinline__ void correct_orbit_body(
         const float t = e * ri * ri * (ri + 1.0f);
         tx = dx * t; ty = dy * t; tz = dz * t;
       }
-      double sx = block_sum_256(tx, s_red);
-      double sy = block_sum_256(ty, s_red);
-      double sz = block_sum_256(tz, s_red);
-      if (tid == 0) {
-        double* o = orbit_part + ((size_t)blk * p.P + g) * 3;
-        o[0] = sx; o[1] = sy; o[2] = sz;
+      double sx = tx, sy = ty, sz = tz;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
       }
+      if (lane == 0) { s_orb[w][3 * g] = sx; s_orb[w][3 * g + 1] = sy; s_orb[w][3 * g + 2] = sz; }
+    }
+    __syncthreads();
+    if (tid < 3 * p.P) {
+      double v = 0;
+      for (int k = 0; k < kBlk / 32; k++) v += s_orb[k][tid];
+      orbit_part[(size_t)blk * p.P * 3 + tid] = v;
     }
     // move the ion–ion sums of unflagged ions to the re-injected positions
     if (K > 0 && live && !((flags[i >> 5] >> (i & 31)) & 1u)) {
@@ -874,12 +891,26 @@ __device__ __forceinline__ void correct_orbit_body(
         }
       }
       od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
-      s_h[0][tid] = hx; s_h[1][tid] = hy; s_h[2][tid] = hz;
-      s_l[0][tid] = lx; s_l[1][tid] = ly; s_l[2][tid] = lz;
+      // two-float warp trees (fixed order), then the 8 warps in order
+      const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float t;
+        t = __shfl_xor_sync(0xffffffffu, hx, o); lx += __shfl_xor_sync(0xffffffffu, lx, o);
+        od_acc2(hx, lx, t);
+        t = __shfl_xor_sync(0xffffffffu, hy, o); ly += __shfl_xor_sync(0xffffffffu, ly, o);
+        od_acc2(hy, ly, t);
+        t = __shfl_xor_sync(0xffffffffu, hz, o); lz += __shfl_xor_sync(0xffffffffu, lz, o);
+        od_acc2(hz, lz, t);
+      }
+      if (lane == 0) {
+        s_h[0][w] = hx; s_h[1][w] = hy; s_h[2][w] = hz;
+        s_l[0][w] = lx; s_l[1][w] = ly; s_l[2][w] = lz;
+      }
       __syncthreads();
       if (tid < 3) {
         float h = 0.f, l = 0.f;
-        for (int u = 0; u < kBlk; u++) { od_acc2(h, l, s_h[tid][u]); l += s_l[tid][u]; }
+        for (int u = 0; u < kBlk / 32; u++) { od_acc2(h, l, s_h[tid][u]); l += s_l[tid][u]; }
         s_h[tid][0] = h;
         s_l[tid][0] = l;
       }
@@ -894,7 +925,7 @@ __device__ __forceinline__ void correct_orbit_body(
 }
 
 __global__ void __launch_bounds__(kBlk) k_correct_orbit(
-    const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
+    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds,
     const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
     const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
     const float4* __restrict__ list_old, const float4* __restrict__ list_new,
@@ -932,7 +963,8 @@ __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __rest
   const int P = p.P, nc = P * 3;
   for (int c = 0; c < nc; c++) {
     double v = 0;
-    for (int b = tid; b < nb; b += kBlk) v += orbit_part[(size_t)b * nc + c];
+    // L2 loads: the partials may come from other blocks of the same launch (fused tail)
+    for (int b = tid; b < nb; b += kBlk) v += __ldcg(orbit_part + (size_t)b * nc + c);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) s_red[w][c] = v;
@@ -997,6 +1029,33 @@ __global__ void __launch_bounds__(kBlk) k_tail(const od_dparams* __restrict__ dp
                                                double* __restrict__ s_field, float* __restrict__ cq) {
   tail_body(*dp, ds, orbit_part, nb, s_q, s_orbit, s_collect, s_dust, s_field, cq);
 }
+
+// K5 + K6: the last of the nb orbit blocks to finish (a ticket taken after its partials are
+// fenced) runs the FP64 tail over all partials, so the tail needs no launch of its own.
+__global__ void __launch_bounds__(kBlk) k_correct_orbit_tail(
+    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds,
+    const float4* __restrict__ pos, float4* __restrict__ fhi, float4* __restrict__ flo,
+    const uint32_t* __restrict__ flags, const int32_t* __restrict__ list,
+    const float4* __restrict__ list_old, const float4* __restrict__ list_new,
+    double* __restrict__ orbit_part, int nb, double* __restrict__ s_q,
+    double* __restrict__ s_orbit, double* __restrict__ s_collect, double* __restrict__ s_dust,
+    double* __restrict__ s_field, float* __restrict__ cq) {
+  correct_orbit_body(*dp, ds, pos, fhi, flo, flags, list, list_old, list_new, orbit_part, nb,
+                     blockIdx.x, gridDim.x - nb);
+  if ((int)blockIdx.x >= nb) return;  // re-injected ions' sums: the tail does not read them
+  __shared__ bool s_last;
+  __syncthreads();                    // this block's partials are written
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&ds->ticket, 1u) == (unsigned)nb - 1u;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  tail_body(*dp, ds, orbit_part, nb, s_q, s_orbit, s_collect, s_dust, s_field, cq);
+  if (threadIdx.x == 0) ds->ticket = 0u;
+}
+
 
 __global__ void k_set_charges(const od_dparams* __restrict__ dp, const od_dstate* __restrict__ ds,
                               float* __restrict__ cq, int P) {
@@ -1213,10 +1272,10 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
                                   b.flags, b.cq, fc.acc);
   k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
-  k_correct_orbit<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
-                                            b.list_old, b.list_new, b.orbit_part, nb);
-  k_tail<<<1, kBlk, 0, s>>>(dp, ds, b.orbit_part, nb, b.s_q, b.s_orbit, b.s_collect, b.s_dust,
-                           b.s_field, b.cq);
+  k_correct_orbit_tail<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
+                                                 b.list_old, b.list_new, b.orbit_part, nb, b.s_q,
+                                                 b.s_orbit, b.s_collect, b.s_dust, b.s_field,
+                                                 b.cq);
   return cudaGetLastError();
 }
 
