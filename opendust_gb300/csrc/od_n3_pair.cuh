@@ -15,6 +15,7 @@ constexpr int kWarps = 8;
 struct n3_consts {
   od_u64 eps, rho, nl2e, one, three, six, invw, nrsw, p30w;
   float rc2;
+  float skip2;  // cutoff forms: a pack whose pairs all lie beyond sqrt(skip2) contributes 0
 };
 struct n3_cut {
   float rho0, rc2, rs, inv_w;
@@ -31,6 +32,9 @@ __device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
   k.nrsw = p2(-c.rs * c.inv_w, -c.rs * c.inv_w);
   k.p30w = p2(30.f * c.inv_w, 30.f * c.inv_w);
   k.rc2 = c.rc2;
+  // (1 + 2e-5) rc^2: beyond it the clamped switching variable is 1 in FP32, so S = 0 and the
+  // switched term is exactly zero (the hard cutoff is exactly zero from rc^2 on)
+  k.skip2 = c.rc2 * 1.00002f;
   return k;
 }
 
@@ -46,6 +50,10 @@ __device__ __forceinline__ void n3_pair(const n3_consts& k, od_u64 X, od_u64 Y, 
   R2 = fma2(DY, DY, R2);
   R2 = fma2(DZ, DZ, R2);
   const float2 r2 = up2(R2);
+  // cutoff forms: when every pair of this pack across the warp lies beyond the cutoff (group
+  // pairs whose boxes come within r_c but whose ions do not), the terms are exactly zero and the
+  // reciprocal, exponential and switching work is skipped (warp-uniform branch)
+  if (CUT != 0 && __all_sync(0xffffffffu, fminf(r2.x, r2.y) >= k.skip2)) return;
   const od_u64 RI = p2(od_rsqrt(r2.x), od_rsqrt(r2.y));
   const od_u64 R = mul2(R2, RI);
   const float2 s = up2(add2(R, k.rho));
