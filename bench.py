@@ -432,11 +432,15 @@ def run_sweep(args, dist: Dist):
             plain_series.append(eng.series(0, K + W))
     # force interval per member (pilot windows), unless the exact sweep is asked for
     t_tune = time.perf_counter()
-    intervals, pilot_err = [], []
+    intervals, pilot_err, shapes = [], [], []
+    cache = tuning.PlanCache(os.path.join(tempfile.gettempdir(), f"od_plans_{os.getpid()}.json"))
     for holder, pos, vel, n in members:
         if args.sweep_exact:
             intervals.append(1)
+            shapes.append(None)
             continue
+        # each-pair-once shape per size bucket, measured once per bucket in this run
+        shapes.append(tuning.batch_plan_for(int(n), cache=cache))
         r = tuning.choose_force_interval(holder, pos, vel, max_rel_err=0.01,
                                          pilot_steps=args.pilot_steps)
         intervals.append(r["force_every"])
@@ -445,9 +449,11 @@ def run_sweep(args, dist: Dist):
     # batched
     with _lib.Batch() as batch:
         slots = []
-        for (h, p, v, _), k in zip(members, intervals):
+        for (h, p, v, _), k, sh in zip(members, intervals, shapes):
             h.cfg.force_every = k
             slots.append(batch.add(h, p, v))
+            if sh is not None:
+                batch.set_plan(slots[-1], *sh)
         batch.step(W)
         t0 = time.perf_counter()
         batch.step(K)
@@ -484,6 +490,8 @@ def run_sweep(args, dist: Dist):
             "ion_steps_per_s_batched": ion_steps / batch_s, "ion_steps_per_s_plain": ion_steps / plain_s,
             "tuning_s": t_tune, "pilot_steps": args.pilot_steps,
             "force_every": {str(int(a)): int(b) for a, b in zip(ks, counts)},
+            "batch_shapes": {f"{a}x{b}": sum(1 for sh in shapes if sh == (a, b))
+                             for a, b in tuning.BATCH_SHAPES},
             "pilot_max_rel_err": max(pilot_err) if pilot_err else 0.0,
             "window_rel_err_vs_plain": {"q_max": max(win_q), "force_max": max(win_f),
                                         "force_median": float(np.median(win_f)),

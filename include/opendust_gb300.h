@@ -396,6 +396,11 @@ od_status od_batch_create(int32_t device, od_batch** out);
  * receives its slot index. May be called between steps (continuous batching). */
 od_status od_batch_add(od_batch* b, const od_config* cfg, const double* pos, const double* vel,
                        int32_t* slot);
+/* Each-pair-once plan of a batch member (no counterpart in the reference): (ions per lane, tile)
+ * = (4, 1024) or (8, 2048), the two shapes the batched kernels run; od_batch_add gives the
+ * od_batch_pair_plan rule, opendust_gb300.tuning.batch_plan_for picks by measurement per size
+ * bucket. Results change by FP32 rounding only. */
+od_status od_batch_set_plan(od_batch* b, int32_t slot, int32_t ions_per_lane, int32_t tile);
 od_status od_batch_remove(od_batch* b, int32_t slot);
 od_handle* od_batch_member(od_batch* b, int32_t slot);
 int32_t od_batch_size(const od_batch* b);

@@ -170,6 +170,7 @@ def load(path: str | None = None):
         "od_batch_create": (c_int32, [c_int32, POINTER(c_void_p)]),
         "od_batch_add": (c_int32, [c_void_p, POINTER(od_config), _DP, _DP, POINTER(c_int32)]),
         "od_batch_remove": (c_int32, [c_void_p, c_int32]),
+        "od_batch_set_plan": (c_int32, [c_void_p, c_int32, c_int32, c_int32]),
         "od_batch_member": (c_void_p, [c_void_p, c_int32]),
         "od_batch_size": (c_int32, [c_void_p]),
         "od_batch_step": (c_int32, [c_void_p, c_int64]),
@@ -549,6 +550,11 @@ class Batch:
                                                ctypes.byref(slot)), self.b)
         self._holders[slot.value] = holder
         return slot.value
+
+    def set_plan(self, slot: int, ions_per_lane: int, tile: int):
+        """Each-pair-once shape of a member: (4, 1024) or (8, 2048)."""
+        self._check(self._lib.od_batch_set_plan(self.b, int(slot), int(ions_per_lane), int(tile)),
+                    self.b)
 
     def remove(self, slot: int):
         self._check(self._lib.od_batch_remove(self.b, int(slot)), self.b)

@@ -1613,6 +1613,19 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
   return OD_OK;
 }
 
+extern "C" od_status od_batch_set_plan(od_batch* b, int32_t slot, int32_t ions_per_lane,
+                                       int32_t tile) {
+  if (!b || slot < 0 || slot >= (int32_t)b->members.size() || !b->members[slot])
+    return bfail(b, OD_ERR_INVALID, "no batch member in that slot");
+  if (!((ions_per_lane == 4 && tile == 1024) || (ions_per_lane == 8 && tile == 2048)))
+    return bfail(b, OD_ERR_INVALID, "batch members take (4, 1024) or (8, 2048)");
+  od_handle* h = b->members[slot];
+  const od_status st = set_plan_n3(h, ions_per_lane, tile);
+  if (st != OD_OK) return bfail(b, st, h->err);
+  b->dirty = true;
+  return OD_OK;
+}
+
 extern "C" od_status od_batch_remove(od_batch* b, int32_t slot) {
   if (!b || slot < 0 || slot >= (int32_t)b->members.size() || !b->members[slot])
     return bfail(b, OD_ERR_INVALID, "no batch member in that slot");

@@ -126,3 +126,114 @@ def choose_force_interval(holder: _lib.ConfigHolder, pos: np.ndarray, vel: np.nd
             break
         best = c
     return {**best, "candidates": cands}
+
+
+# ---------------------------------------------------------------- persisted plan choices
+# Plans chosen by measurement are kept per (GPU model, size bucket) in a JSON file, so that a
+# later process (a sweep, a server) reuses them without timing again. The bucket of N ions is
+# round(2 log2 N) / 2: half-octave classes.
+
+def plan_cache_path() -> str:
+    import os
+
+    return os.environ.get("OD_PLAN_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "opendust_gb300", "plans.json")
+
+
+def size_bucket(n: int) -> float:
+    return round(2.0 * np.log2(max(int(n), 2))) / 2.0
+
+
+def gpu_model(device: int = 0) -> str:
+    try:
+        import torch
+
+        return torch.cuda.get_device_name(device)
+    except Exception:  # no torch / no device name: one class for every GPU
+        return "gpu"
+
+
+class PlanCache:
+    """{key: plan} in a JSON file; key = "<kind>|<GPU model>|<size bucket>"."""
+
+    def __init__(self, path: str | None = None):
+        import json
+        import os
+
+        self.path = path or plan_cache_path()
+        self.data = {}
+        if os.path.exists(self.path):
+            try:
+                with open(self.path) as f:
+                    self.data = json.load(f)
+            except (OSError, ValueError):
+                self.data = {}
+
+    @staticmethod
+    def key(kind: str, model: str, n: int) -> str:
+        return f"{kind}|{model}|{size_bucket(n):g}"
+
+    def get(self, kind, model, n):
+        v = self.data.get(self.key(kind, model, n))
+        return tuple(v) if v is not None else None
+
+    def put(self, kind, model, n, plan):
+        import json
+        import os
+
+        self.data[self.key(kind, model, n)] = list(plan)
+        os.makedirs(os.path.dirname(self.path) or ".", exist_ok=True)
+        tmp = self.path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(self.data, f, indent=1, sort_keys=True)
+        os.replace(tmp, self.path)
+
+
+def tuned_plan(eng: _lib.Engine, device: int = 0, cache: PlanCache | None = None) -> tuple:
+    """The autotuner's all-pairs plan for this engine's size, from the persisted cache or, on a
+    miss, by od_autotune on the engine's current positions (then stored). Applies it."""
+    cache = cache or PlanCache()
+    model = gpu_model(device)
+    plan = cache.get("single", model, eng.n)
+    if plan is None:
+        eng.autotune(use_cache=False)
+        p = eng.pair_plan()
+        plan = (p["threads"], p["targets_per_thread"], p["variant"], p["jsplit"])
+        cache.put("single", model, eng.n, plan)
+    eng.set_pair_plan(*plan)
+    return plan
+
+
+BATCH_SHAPES = ((4, 1024), (8, 2048))
+
+
+def batch_plan_for(n: int, device: int = 0, cache: PlanCache | None = None,
+                   time_plan=None) -> tuple:
+    """Each-pair-once shape (ions per lane, tile) for a batch member of n ions, chosen per size
+    bucket by timing both batch shapes on a member-sized simulation; persisted. time_plan(n,
+    shape) -> ms per evaluation (default: two timed steps of a small_plain simulation)."""
+    cache = cache or PlanCache()
+    model = gpu_model(device)
+    plan = cache.get("batch", model, n)
+    if plan is not None:
+        return plan
+    time_plan = time_plan or (lambda nn, sh: _time_batch_shape(nn, sh, device))
+    best = min(BATCH_SHAPES, key=lambda sh: time_plan(n, sh))
+    cache.put("batch", model, n, best)
+    return best
+
+
+def _time_batch_shape(n: int, shape, device: int) -> float:
+    from . import build_simulation, workloads
+
+    plasma, sim, grains, dist, ext = workloads.small_plain(N=int(n), n=8)
+    holder, _ = build_simulation(plasma, sim, grains, dist, seed=1, device=device, **ext)
+    with _lib.Engine(holder, device) as eng:
+        eng.set_pair_plan(256, shape[0], 7, shape[1])
+        eng.init_state()
+        eng.step(1)
+        eng.set_timing(True, count_pairs=False)
+        eng.step(3)
+        _, _, pair_ms, launches = eng.timing()
+        eng.set_timing(False)
+    return pair_ms / max(launches, 1)

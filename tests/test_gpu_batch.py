@@ -101,3 +101,23 @@ def test_batch_rejects_overflow_and_cutoff(gpu_lib):
         with pytest.raises(_lib.OpenDustError) as e:
             b.add(hc, p, v)
         assert e.value.status == 6
+
+
+def test_batch_member_plan_can_be_set(gpu_lib):
+    # a member moved to the other batch shape (8 x 2 with 2048-ion tiles below 2^16 ions)
+    # equals the same simulation stepped alone with that plan, bitwise
+    h, p, v = member(9000, 2, 5, True)
+    with _lib.Engine(h) as eng:
+        eng.set_pair_plan(256, 8, 7, 2048)
+        eng.set_state(p, v)
+        eng.step(8)
+        ref = (eng.series(0, 8), *eng.get_state())
+    with _lib.Batch() as b:
+        s = b.add(h, p, v)
+        b.set_plan(s, 8, 2048)
+        b.step(8)
+        m = b.member(s)
+        assert m.pair_plan()["targets_per_thread"] == 8
+        same(ref, (m.series(0, 8), *m.get_state()))
+        with pytest.raises(_lib.OpenDustError):
+            b.set_plan(s, 4, 2048)
