@@ -104,12 +104,14 @@ def test_batch_rejects_overflow_and_cutoff(gpu_lib):
 
 
 def test_batch_member_plan_can_be_set(gpu_lib):
-    # a member moved to the other batch shape (8 x 2 with 2048-ion tiles below 2^16 ions)
-    # equals the same simulation stepped alone with that plan, bitwise
+    # a member moved to the other batch shape (8 x 2 with 2048-ion tiles below 2^16 ions) after
+    # it joined equals the same simulation stepped alone with the same plan change, bitwise (its
+    # initial sums come from the plan it joined with)
     h, p, v = member(9000, 2, 5, True)
     with _lib.Engine(h) as eng:
-        eng.set_pair_plan(256, 8, 7, 2048)
+        eng.set_pair_plan(*_lib.batch_pair_plan(eng.n))
         eng.set_state(p, v)
+        eng.set_pair_plan(256, 8, 7, 2048)
         eng.step(8)
         ref = (eng.series(0, 8), *eng.get_state())
     with _lib.Batch() as b:
