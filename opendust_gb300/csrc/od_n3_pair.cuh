@@ -16,7 +16,6 @@ struct n3_consts {
   od_u64 eps, rho, nl2e, one, three, six, invw, nrsw, p30w;
   float rc2;
   float skip2;  // cutoff forms: a pack whose pairs all lie beyond sqrt(skip2) contributes 0
-  float in2;    // switching: a pack whose pairs all lie within sqrt(in2) takes the plain term
 };
 struct n3_cut {
   float rho0, rc2, rs, inv_w;
@@ -36,8 +35,6 @@ __device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
   // (1 + 2e-5) rc^2: beyond it the clamped switching variable is 1 in FP32, so S = 0 and the
   // switched term is exactly zero (the hard cutoff is exactly zero from rc^2 on)
   k.skip2 = c.rc2 * 1.00002f;
-  // (1 - 2e-5) r_s^2: inside it the switching variable clamps to 0, S = 1 and S' = 0
-  k.in2 = c.rs * c.rs * 0.99998f;
   return k;
 }
 
@@ -65,9 +62,6 @@ __device__ __forceinline__ void n3_pair(const n3_consts& k, od_u64 X, od_u64 Y, 
   const od_u64 EX = p2(od_ex2(ea.x), od_ex2(ea.y));
   od_u64 C;
   if (CUT == 0) {
-    C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
-  } else if (CUT == 1 && __all_sync(0xffffffffu, fmaxf(r2.x, r2.y) <= k.in2)) {
-    // every pair of the pack across the warp lies inside the switching radius: plain term
     C = mul2(mul2(EX, RI), fma2(SI, SI, SI));
   } else if (CUT == 1) {
     const float2 xx = up2(fma2(R, k.invw, k.nrsw));
