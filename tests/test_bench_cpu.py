@@ -32,7 +32,8 @@ def test_reference_arm_json_contract():
 def test_traffic_files_match_their_capture_only():
     import bench
 
-    assert bench.load_traffic(2**20, {"variant": 7, "jsplit": 2048}) > 1e10
+    # the fixed-point accumulators leave positions and sums in L2: tens of MB per evaluation
+    assert 1e7 < bench.load_traffic(2**20, {"variant": 7, "jsplit": 2048}) < 1e9
     assert bench.load_traffic(2**19, {"variant": 7, "jsplit": 2048}) is None
-    assert bench.load_traffic(2**19, {"variant": 3, "jsplit": 512}, cutoff=True) > 1e9
+    assert 1e7 < bench.load_traffic(2**19, {"variant": 3, "jsplit": 512}, cutoff=True) < 1e9
     assert bench.load_traffic(2**19, {"variant": 3, "jsplit": 1024}, cutoff=True) is None
