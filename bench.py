@@ -41,11 +41,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = 25
-KERNELS_PER_STEP = 4          # all pairs: kick/drift, pairs, kick/flag (takes the fixed-point
-                              # sums; its last block compacts and re-injects), correct/orbit
-                              # (its last block runs the FP64 tail)
-KERNELS_PER_STEP_CUTOFF = 10  # + cell clear, count, scan, scatter, sort, chunk scan
-KERNELS_PER_STEP_CUTOFF_TILES = 14  # + clear, count, scan, scatter, sort, boxes, pairs,
+KERNELS_PER_STEP = 5          # all pairs: kick/drift, pairs, kick/flag (takes the fixed-point
+                              # sums), collect/inject, correct/orbit (its last block runs the
+                              # FP64 tail)
+KERNELS_PER_STEP_CUTOFF = 11  # + cell clear, count, scan, scatter, sort, chunk scan
+KERNELS_PER_STEP_CUTOFF_TILES = 15  # + clear, count, scan, scatter, sort, boxes, pairs,
                                     # scan, list, tile-pair kernel, slot take (cutoff variant 3)
 
 

@@ -86,7 +86,6 @@ struct od_dstate {
   int64_t n_avg;
   int64_t n_inj_total;
   uint32_t ticket;                    // orbit blocks of K5 done this step (0 between steps)
-  uint32_t ticket3;                   // blocks of the fused K3 + K4 done (0 between steps)
 };
 
 // ------------------------------------------------------------------ Philox4x32-10

@@ -756,33 +756,6 @@ __global__ void __launch_bounds__(kCT) k_collect_inject(
   collect_inject_body(*dp, ds, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
 }
 
-// K3 + K4 in one launch of kCT-thread blocks: every block kicks and flags its ions; the last
-// block to finish (a ticket taken after its flags and velocities are fenced) compacts the whole
-// list and re-injects, as k_collect_inject does, so the compaction needs no launch of its own.
-__global__ void __launch_bounds__(kCT) k_kick_flag_collect(
-    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ pos,
-    float4* __restrict__ vel, const float4* __restrict__ ph, const float4* __restrict__ pl,
-    int jsplit, float4* __restrict__ fhi, float4* __restrict__ flo, uint32_t* __restrict__ flags,
-    const float* __restrict__ cq, unsigned long long* __restrict__ acc,
-    int32_t* __restrict__ list, int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
-    float4* __restrict__ list_new, float4* __restrict__ list_v) {
-  // whole warps beyond Npad (a multiple of 512) have no ions and no flag word
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i - (int)(threadIdx.x & 31) < dp->Npad)
-    kick_flag_body(*dp, ds, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq, i, acc);
-  __shared__ bool s_last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(&ds->ticket3, 1u) == gridDim.x - 1u;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  collect_inject_body(*dp, ds, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
-  if (threadIdx.x == 0) ds->ticket3 = 0u;
-}
-
 // list + per-grain counts of a snapshot (no state change)
 __global__ void __launch_bounds__(kCT) k_list_only(const od_dparams* __restrict__ dp, int nwords,
                                                    const float4* __restrict__ pos,
@@ -1295,9 +1268,10 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
     return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz, b.n3}, N, Npad, b.part_hi, b.part_lo,
                            &ds->err, s, fc.acc == nullptr);
   const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
-  k_kick_flag_collect<<<(Npad + kCT - 1) / kCT, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit,
-                                                b.fhi, b.flo, b.flags, b.cq, fc.acc, b.list,
-                                                b.list_bits, b.list_old, b.list_new, b.list_v);
+  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
+                                  b.flags, b.cq, fc.acc);
+  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
+                                     b.list_old, b.list_new, b.list_v);
   k_correct_orbit_tail<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
                                                  b.list_old, b.list_new, b.orbit_part, nb, b.s_q,
                                                  b.s_orbit, b.s_collect, b.s_dust, b.s_field,
