@@ -229,9 +229,15 @@ struct cut_traits {
   static constexpr bool HS = MT > 2;                  // target sums kept in the segment slot
   static constexpr size_t RFL = (size_t)NI * 3 * GS;  // reaction slots (floats)
   static constexpr size_t TFL = (size_t)NSEG * 6 * GT;  // two-float target segment slots
-  static constexpr size_t SMEM = sizeof(float) * (RFL + TFL) + 384;  // + list metadata
+  static constexpr size_t SMEM = sizeof(float) * (RFL + TFL) + 256;  // + list metadata
 };
 
+// warp that owns list entry i of n
+__device__ __forceinline__ int cut_owner(int i, int n) {
+  int w = 0;
+  while (w < kWarps - 1 && (((w + 1) * n) >> 3) <= i) w++;
+  return w;
+}
 
 // group pair (ga, gb) of a diagonal tile: 2 each pair once, 1 directed (the sources lie in the
 // target group), 0 skipped (counted from the other side)
@@ -265,9 +271,6 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
   signed char* const gs0 = item_of + 64;  // first and last segment of each target group
   signed char* const gs1 = gs0 + 8;
   int* const s_n = reinterpret_cast<int*>(items + 208);
-  unsigned char* const wt = items + 212;                      // estimated cost of each entry
-  unsigned char* const own = items + 276;                     // warp that owns each entry
-  int* const bnd = reinterpret_cast<int*>(items + 340);       // slice starts [9]
   const bool diag = a == b;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
 
@@ -279,7 +282,6 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
       const int c = r * 32 + lane, ga = c / NBS, gb = c % NBS;
       const int mode = diag ? cut_diag_mode<GT, GS>(ga, gb) : 2;
       bool keep = mode == 1, inner = false;
-      int cost = 5;  // directed group pair of a diagonal tile (no reactions)
       if (mode != 0) {
         float ta[6], tb[6];
         group_box(gbox, (a * NBT + ga) * (GT / 64), GT / 64, ta);
@@ -296,49 +298,12 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
         // every pair of the two groups closer than the switching radius (hard cutoff: the
         // cutoff): the switching factor is exactly 1 there, so the plain term applies
         inner = f2 < k_in2;
-        // estimated cost of the group pair, for the warps' slices: the plain term 8; with the
-        // switching polynomial ~1.6x per evaluated pack, and the packs beyond the cutoff (about
-        // the share of the box-distance range past r_c) skipped at ~0.2x
-        if (mode == 2) {
-          const float dn = sqrtf(d2), df = sqrtf(f2), rc = sqrtf(cull2);
-          const float in = fminf(fmaxf((rc - dn) / fmaxf(df - dn, 1e-6f), 0.f), 1.f);
-          cost = inner ? 8 : (int)(8.f * (0.2f + 1.4f * in) + 0.5f);
-        }
       }
       const unsigned int bal = __ballot_sync(0xffffffffu, keep);
       const int pos = n + __popc(bal & ((1u << lane) - 1u));
-      if (keep) {
-        items[pos] = (unsigned char)(c | (inner ? kInner : 0));
-        wt[pos] = (unsigned char)(cost < 1 ? 1 : cost);
-      }
+      if (keep) items[pos] = (unsigned char)(c | (inner ? kInner : 0));
       item_of[c] = keep ? (signed char)pos : (signed char)-1;
       n += __popc(bal);
-    }
-    __syncwarp();
-    // slices of equal estimated cost: entry i goes to the warp whose share of the total holds
-    // the middle of the entry's cost (nondecreasing in i, so the slices stay contiguous)
-    {
-      int w0 = 0, w1 = 0, tot = 0;
-      if (lane < n) w0 = wt[lane];
-      if (32 + lane < n) w1 = wt[32 + lane];
-      int s0 = w0, s1 = w1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y0 = __shfl_up_sync(0xffffffffu, s0, o), y1 = __shfl_up_sync(0xffffffffu, s1, o);
-        if (lane >= o) { s0 += y0; s1 += y1; }
-      }
-      const int t0 = __shfl_sync(0xffffffffu, s0, 31);
-      tot = t0 + __shfl_sync(0xffffffffu, s1, 31);
-      s1 += t0;
-      // owner = floor(8 (exclusive prefix + cost/2) / total)
-      if (lane < n) own[lane] = (unsigned char)min(kWarps - 1, (2 * (s0 - w0) + w0) * kWarps / (2 * max(tot, 1)));
-      if (32 + lane < n) own[32 + lane] = (unsigned char)min(kWarps - 1, (2 * (s1 - w1) + w1) * kWarps / (2 * max(tot, 1)));
-      __syncwarp();
-      if (lane <= kWarps) {
-        int b = 0;  // entries owned by warps below `lane`
-        for (int i = 0; i < n; i++) b += own[i] < lane;
-        bnd[lane] = lane == kWarps ? n : b;
-      }
     }
     __syncwarp();
     // a segment starts at every change of target group and at the start of every slice
@@ -348,7 +313,7 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
       bool f = false;
       if (i < n)
         f = i == 0 || (items[i - 1] & kItem) / NBS != (items[i] & kItem) / NBS ||
-            own[i - 1] != own[i];
+            cut_owner(i - 1, n) != cut_owner(i, n);
       const unsigned int bal = __ballot_sync(0xffffffffu, f);
       if (i < n) segid[i] = (unsigned char)(nseg + __popc(bal & ((2u << lane) - 1u)) - 1);
       nseg += __popc(bal);
@@ -368,7 +333,7 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
   __syncthreads();
 
   // 2. this warp's slice of the list
-  const int i0 = bnd[w], i1 = bnd[w + 1];
+  const int n = *s_n, i0 = (w * n) >> 3, i1 = ((w + 1) * n) >> 3;
   unsigned int cnt = 0;
   od_u64 X[MT], Y[MT], Z[MT];
   float hreg[HS ? 1 : 6 * MT];
