@@ -183,25 +183,43 @@ __device__ __forceinline__ void od_acc2(float& hi, float& lo, float x) {
 // two-float partial's own rounding of ~1e-7 of its size.
 #define OD_FIX_SCALE 4294967296.0f          // 2^32
 #define OD_FIX_INV 2.3283064365386963e-10   // 2^-32
+#define OD_FIX_INV_F 2.3283064365386963e-10f
+// v 2^32 truncated toward zero, from the float's bits (integer operations only): v = ±M 2^(E-150)
+// with the 24-bit significand M, so v 2^32 = ±M 2^(E-118). |v| < 2^31 here (shift <= 39).
+__device__ __forceinline__ long long od_f2fix(float v) {
+  const int b = __float_as_int(v);
+  const int ex = (b >> 23) & 0xFF;
+  const int sh = ex - 118;
+  const long long m = (long long)((b & 0x7FFFFF) | 0x800000);
+  long long mag = sh >= 0 ? (m << min(sh, 39)) : (sh > -24 ? (m >> -sh) : 0ll);
+  if (ex == 0) mag = 0;  // zero (and subnormals, far below the 2^-32 resolution)
+  return b < 0 ? -mag : mag;
+}
 __device__ __forceinline__ unsigned long long od_fix(float hi, float lo) {
-  return (unsigned long long)(__float2ll_rn(hi * OD_FIX_SCALE) + __float2ll_rn(lo * OD_FIX_SCALE));
+  return (unsigned long long)(od_f2fix(hi) + od_f2fix(lo));
 }
 __device__ __forceinline__ void od_fix_add(unsigned long long* a, float hi, float lo) {
   atomicAdd(a, od_fix(hi, lo));
 }
 // accumulator (3 words, component stride `stride`) -> two-float sums, and the words cleared for
 // the next evaluation
+// (FP32 only: FP64 is slow on GB300.) A word x is H + M 2^-16 + L 2^-32 with H = x >> 32
+// (signed, exact in FP32 for |H| < 2^24) and M, L its two low 16-bit halves, each exact in FP32;
+// the two-float sum is TwoSum(H, M 2^-16) with L 2^-32 added to the low part.
+__device__ __forceinline__ void od_fix_split(unsigned long long x, float& hi, float& lo) {
+  const float h = (float)(int)((long long)x >> 32);  // arithmetic shift: floor(x / 2^32)
+  const float m = (float)(unsigned)((x >> 16) & 0xFFFFull) * 1.52587890625e-05f;  // 2^-16
+  const float l = (float)(unsigned)(x & 0xFFFFull) * OD_FIX_INV_F;
+  od_two_sum(h, m, hi, lo);
+  lo += l;
+}
 __device__ __forceinline__ void od_fix_take(unsigned long long* a, size_t stride, float3& hi,
                                            float3& lo) {
-  double v[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    v[c] = (double)(long long)a[c * stride] * OD_FIX_INV;
-    a[c * stride] = 0ull;
-  }
-  hi = make_float3((float)v[0], (float)v[1], (float)v[2]);
-  lo = make_float3((float)(v[0] - (double)hi.x), (float)(v[1] - (double)hi.y),
-                   (float)(v[2] - (double)hi.z));
+  const unsigned long long x = a[0], y = a[stride], z = a[2 * stride];
+  a[0] = 0ull; a[stride] = 0ull; a[2 * stride] = 0ull;
+  od_fix_split(x, hi.x, lo.x);
+  od_fix_split(y, hi.y, lo.y);
+  od_fix_split(z, hi.z, lo.z);
 }
 
 // ------------------------------------------------------------------ pair kernel
