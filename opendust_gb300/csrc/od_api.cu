@@ -332,12 +332,17 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   p->Rh2f = (float)(Rh * Rh);
   p->Hz_f = float_ceil(Hh / 2.0);
   p->p_coll = dt * c->w_c;
+  // u <= p_coll with u = k 2^-24: k <= floor(p_coll 2^24) (exact in FP64); -1 below zero
+  p->pcoll_int = p->p_coll < 0 ? -1
+                 : (int32_t)std::min(floor(p->p_coll * 16777216.0), 16777216.0);
   if (c->collision_model == OD_COLL_MFP) {
     double mfp_h = c->mfp / lam;
     double vmax = 3.0 * fabs(c->v_fl / vunit) + 10.0 * (c->v_T / vunit);
     p->mfp_inv = (float)(1.0 / mfp_h);
     p->vmax_mfp = (float)vmax;
     p->Pmax_mfp = 1.0 - exp(-vmax / mfp_h);
+    // u < Pmax with u = k 2^-24: k < ceil(Pmax 2^24)
+    p->pmax_int = (uint32_t)std::min(ceil(p->Pmax_mfp * 16777216.0), 16777216.0);
     p->mfp_inv_d = 1.0 / mfp_h;
   }
   p->p_t = c->p_top; p->p_s = c->p_side; p->p_b = c->p_bottom;

@@ -25,6 +25,10 @@ struct od_dparams {
   uint32_t seed_lo, seed_hi;
   int32_t force_every;               // ion–ion force interval k (1: every step)
   int32_t ion0;                      // global index of local ion 0 (a shard of a larger run; 0)
+  // integer forms of u < Pmax (u < pmax_int 2^-24) and u <= p_coll (u <= pcoll_int 2^-24;
+  // -1: never) for u = (w >> 8) 2^-24
+  uint32_t pmax_int;
+  int32_t pcoll_int;
   // FP32 hot-loop constants (lambda / d_t units)
   float A_ii, rho0, Rh, Hh, Hh_half, a_field, vT, vfl;
   float rc2, rc, rs, inv_w;          // cutoff^2, cutoff, switch start, 1/(rc-rs)

@@ -412,10 +412,11 @@ __global__ void k_reduce(int Npad, int jsplit, const float4* __restrict__ ph,
 __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint32_t step,
                                         float4& v) {
   if (p.coll == OD_COLL_PER_DOF) {
-    // opendust.py:869-873: collision = step(p_collision - uniform) per velocity component
+    // opendust.py:869-873: collision = step(p_collision - uniform) per velocity component;
+    // u01 is a multiple of 2^-24, so u <= p_coll is an integer comparison (exact)
     od_u4 w = od_draw(p, ion, step, OD_RNG_COLL_TEST);
-    bool c0 = (double)od_u01(w.x) <= p.p_coll, c1 = (double)od_u01(w.y) <= p.p_coll,
-         c2 = (double)od_u01(w.z) <= p.p_coll;
+    const bool c0 = (int)(w.x >> 8) <= p.pcoll_int, c1 = (int)(w.y >> 8) <= p.pcoll_int,
+               c2 = (int)(w.z >> 8) <= p.pcoll_int;
     if (c0 | c1 | c2) {
       od_u4 g = od_draw(p, ion, step, OD_RNG_COLL_GAUSS);
       float gx, gy, gz, dummy;
@@ -428,17 +429,32 @@ __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint3
   } else if (p.coll == OD_COLL_MFP) {
     // null collision: candidate with probability Pmax = 1 - exp(-vmax/mfp), real with
     // probability |v|/vmax; an ion faster than the majorant vmax (accelerated by a grain or the
-    // field) collides with its own probability 1 - exp(-|v| d_t/mfp) instead of being capped
-    // The branch and the acceptance test are decided in FP64 against the FP32 majorant, the
-    // same way the oracle decides them: the squares of FP32 components are exact in FP64, so
-    // the sum (x^2 + y^2) + z^2 rounds identically with or without FMA contraction.
+    // field) collides with its own probability 1 - exp(-|v| d_t/mfp) instead of being capped.
+    // The decisions are the oracle's FP64 ones against the FP32 majorant: FP32 decides when it
+    // is 1e-5 away from the boundary (its error is ~2e-7), FP64 inside that band (the squares of
+    // FP32 components are exact in FP64, so (x^2 + y^2) + z^2 rounds the same with or without
+    // FMA contraction); u < Pmax is an integer comparison (u is a multiple of 2^-24).
     od_u4 w = od_draw(p, ion, step, OD_RNG_MFP_TEST);
-    const double sp2 = (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z;
-    const double vm = (double)p.vmax_mfp;
-    const double sp = sqrt(sp2);
-    const bool hit = sp2 <= vm * vm
-                         ? (double)od_u01(w.x) < p.Pmax_mfp && (double)od_u01(w.y) * vm < sp
-                         : (double)od_u01(w.z) < 1.0 - exp(-sp * p.mfp_inv_d);
+    const float vm = p.vmax_mfp, vm2 = vm * vm;
+    const float sp2f = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
+    bool slow;
+    if (sp2f < vm2 * (1.f - 1e-5f)) slow = true;
+    else if (sp2f > vm2 * (1.f + 1e-5f)) slow = false;
+    else slow = (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z <= (double)vm * vm;
+    bool hit;
+    if (slow) {
+      hit = false;
+      if ((w.x >> 8) < p.pmax_int) {
+        const float t = od_u01(w.y) * vm, spf = sqrtf(sp2f);
+        if (t < spf * (1.f - 1e-5f)) hit = true;
+        else if (t > spf * (1.f + 1e-5f)) hit = false;
+        else hit = (double)od_u01(w.y) * (double)vm <
+                   sqrt((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+      }
+    } else {  // faster than the majorant (rare)
+      const double sp = sqrt((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+      hit = (double)od_u01(w.z) < 1.0 - exp(-sp * p.mfp_inv_d);
+    }
     if (hit) {
       od_u4 g = od_draw(p, ion, step, OD_RNG_MFP_GAUSS);
       float gx, gy, gz, dummy;
