@@ -188,19 +188,8 @@ __device__ __forceinline__ void od_acc2(float& hi, float& lo, float x) {
 #define OD_FIX_SCALE 4294967296.0f          // 2^32
 #define OD_FIX_INV 2.3283064365386963e-10   // 2^-32
 #define OD_FIX_INV_F 2.3283064365386963e-10f
-// v 2^32 truncated toward zero, from the float's bits (integer operations only): v = ±M 2^(E-150)
-// with the 24-bit significand M, so v 2^32 = ±M 2^(E-118). |v| < 2^31 here (shift <= 39).
-__device__ __forceinline__ long long od_f2fix(float v) {
-  const int b = __float_as_int(v);
-  const int ex = (b >> 23) & 0xFF;
-  const int sh = ex - 118;
-  const long long m = (long long)((b & 0x7FFFFF) | 0x800000);
-  long long mag = sh >= 0 ? (m << min(sh, 39)) : (sh > -24 ? (m >> -sh) : 0ll);
-  if (ex == 0) mag = 0;  // zero (and subnormals, far below the 2^-32 resolution)
-  return b < 0 ? -mag : mag;
-}
 __device__ __forceinline__ unsigned long long od_fix(float hi, float lo) {
-  return (unsigned long long)(od_f2fix(hi) + od_f2fix(lo));
+  return (unsigned long long)(__float2ll_rn(hi * OD_FIX_SCALE) + __float2ll_rn(lo * OD_FIX_SCALE));
 }
 __device__ __forceinline__ void od_fix_add(unsigned long long* a, float hi, float lo) {
   atomicAdd(a, od_fix(hi, lo));
