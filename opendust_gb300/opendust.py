@@ -303,7 +303,9 @@ class OpenDust:
         init: "device" samples the initial ions on the GPU (od_init_state), "host" with numpy
         (setup_host.initial_state); a restart file overrides both. pair_plan: all-pairs work
         decomposition (threads, ions per thread, variant[, jsplit or tile]) passed to
-        od_set_pair_plan; None keeps the library's default for this ion count."""
+        od_set_pair_plan; None keeps the library's default for this ion count; "tuned" takes
+        the autotuner's plan for this GPU model and size bucket from the persisted plan cache
+        (tuning.tuned_plan: measured once on the initial state, then reused)."""
         plasma = self.plasmaParametersInSIUnits
         sim = self.simulationParametersInSIUnits
         out = self.outputParameters
@@ -323,7 +325,7 @@ class OpenDust:
                                         self.distributionType, seed)
         eng = _lib.Engine(holder, device)
         try:
-            if pair_plan is not None:
+            if pair_plan is not None and pair_plan != "tuned":
                 eng.set_pair_plan(*pair_plan)
             if pos is not None:
                 eng.set_state(pos, vel)
@@ -331,6 +333,9 @@ class OpenDust:
                 eng.init_state(sh.field_driven_vz_table(plasma.v_fl, plasma.v_T))
             else:
                 eng.init_state()
+            if pair_plan == "tuned" and not cutOff and cutoff_distance is None:
+                from . import tuning
+                tuning.tuned_plan(eng, device)
             self._run_loop(eng, out, plasma, quiet)
             ser = eng.series(0, self.n)
             self.averages, _ = eng.averages()
