@@ -100,7 +100,10 @@ __device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[M
                                          od_u64 (&AZ)[MT], od_u64 (&RX)[MS / 2],
                                          od_u64 (&RY)[MS / 2], od_u64 (&RZ)[MS / 2], int src,
                                          unsigned int& cnt) {
-#pragma unroll 1
+  // cutoff forms: two lane steps interleaved (more independent work per warp; the 2 x 2 shape
+  // has only two packs per step)
+  constexpr int kUnroll = CUT != 0 ? 2 : 1;
+#pragma unroll kUnroll
   for (int st = 0; st < 32; st++) {
 #pragma unroll
     for (int q = 0; q < MS / 2; q++) {
