@@ -273,15 +273,16 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * pair on the Newton path of variant 4, 7: each unordered pair evaluated once and applied to
  * both ions (threads 256; targets_per_thread = target ions per lane: 2 or 4 with as many source
  * ions, 8 with two; jsplit = ions per tile, 1024, 2048 or 4096 (not 1024 with 8), <= 0 for the
- * default; needs 24 bytes of device memory per ion and tile, OD_ERR_OOM when that does not
- * fit). From 2^15 ions od_create selects variant 7 when its memory fits 32 GiB.
+ * default). Variants 2-7 add their sums into 64-bit fixed-point accumulators (24 bytes per ion)
+ * with integer atomics, so results do not depend on the order of the GPU's blocks. From 2^15
+ * ions od_create selects variant 7.
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step.
  * Cutoff method (force_method OD_FORCE_CUTOFF): variant 0 or 2 walks a stencil of cells per
- * target cell (scalar or packed); variant 3 (the default when its memory fits 64 GiB) sorts
+ * target cell (scalar or packed); variant 3 (the default) sorts
  * the ions along a Hilbert curve and evaluates each pair inside the cutoff once over tile
  * pairs whose bounding boxes come within it — targets_per_thread 2 with 512-ion tiles
  * (balanced group-pair lists) or 4 with 1024-ion tiles; a positive jsplit must name that tile
- * size; 24 bytes of device memory per ion and tile. */
+ * size; 24 bytes of accumulators per ion slot. */
 od_status od_set_pair_plan(od_handle* h, int32_t threads, int32_t targets_per_thread,
                            int32_t variant, int32_t jsplit);
 /* Autotuner: times every supported (threads, targets_per_thread, variant) and three source
@@ -410,8 +411,8 @@ od_status od_batch_step(od_batch* b, int64_t nsteps);
 od_status od_batch_last_step_ms(const od_batch* b, double* ms);
 /* The all-pairs plan a batch member with n_ions ions steps with (plan5 as od_get_pair_plan;
  * jsplit 0 = the member's default split): variant 7 with 4 x 4 ions per lane and 1024-ion
- * tiles up to 2^16 ions, 8 x 2 and 2048-ion tiles above, or variant 5 when the tile-pair matrix
- * does not fit. A single simulation given the same plan produces bitwise the same results. No
+ * tiles up to 2^16 ions, 8 x 2 and 2048-ion tiles above (od_batch_set_plan changes it). A single
+ * simulation given the same plan produces bitwise the same results. No
  * counterpart in the reference (it has no batching). */
 od_status od_batch_pair_plan(int64_t n_ions, int32_t* plan5);
 od_status od_batch_destroy(od_batch* b);
@@ -419,8 +420,7 @@ const char* od_batch_last_error(const od_batch* b);
 /* Free and total device memory (admission control of a request server). */
 od_status od_device_memory(int32_t device, int64_t* free_bytes, int64_t* total_bytes);
 /* Device bytes a simulation created by od_create with this configuration allocates, including
- * the tile-pair matrix of the default all-pairs plan (variant 7 from 2^15 ions; batch members
- * do not allocate it) (admission control). */
+ * the fixed-point accumulators and the cutoff's sort and tile-pair list (admission control). */
 od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes);
 
 /* Trajectory dumps of OpenDust.simulate() (opendust.py:1071-1098, which writes them with a Python

@@ -365,13 +365,12 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
 // (variant 5, the fastest measured on GB300 from 2^16 to 2^20 ions), with enough source chunks
 // for several waves on every SM.
 // From 2^15 padded ions the default is variant 7 (each unordered pair once: 4 x 4 ions per lane
-// with 1024-ion tiles up to 2^16 ions, then 8 x 2 with 2048-ion tiles) when its tile-pair matrix
-// fits OD_N3_BUDGET (about a ninth of a GB300's memory: 2048-ion tiles up to 2^20 ions, 4096-ion
-// tiles up to 2^21); od_create falls back to the plan below otherwise.
+// with 1024-ion tiles up to 2^16 ions, then 8 x 2 with 2048-ion tiles); its sums go to 24 bytes of
+// fixed-point accumulators per ion, so it always fits (the budget below only bounds the rule).
 static constexpr size_t OD_N3_BUDGET = (size_t)32 << 30;
-// The cutoff's tile-pair matrix (cutoff variant 3) may take up to a quarter of a GB300's memory:
-// 512-ion tiles, with the balanced group-pair lists (1.4x faster per step than the 1024-ion
-// fallback at 2^19 ions), up to about 2^20 ions.
+// The cutoff's tile-pair path (variant 3: 512-ion tiles with balanced group-pair lists) needs its
+// sort, boxes, tile-pair list and slot accumulators (0.3 GB at 2^20 ions); the budget bounds the
+// tile-pair list for very large N, beyond which 1024-ion tiles or the cell stencil take over.
 static constexpr size_t OD_CUTN3_BUDGET = (size_t)64 << 30;
 static bool uses_n3_default(int Npad) { return Npad >= 32768; }
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile);
@@ -442,7 +441,7 @@ extern "C" od_status od_create(const od_config* cfg, int32_t device, od_handle**
 }
 
 // n3_default = false: keep the directed-pair default plan (batch members, which the batched
-// all-pairs kernel steps with their own plan), so that no tile-pair matrix is allocated.
+// all-pairs kernel steps with their own plan).
 static od_status create_handle(const od_config* cfg, int32_t device, bool n3_default,
                                od_handle** out) {
   if (!out) return fail(nullptr, OD_ERR_INVALID, "out is NULL");
@@ -504,7 +503,7 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
   if (n3_default && cfg->force_method != OD_FORCE_CUTOFF && uses_n3_default(h->Npad))
     n3_tile = od_n3_default(h->Npad, OD_N3_BUDGET, &n3_ipt);
   if (n3_tile && set_plan_n3(h, n3_ipt, n3_tile) != OD_OK) {
-    // the tile-pair matrix did not fit: stay on the directed-pair default
+    // no each-pair-once shape for this size: stay on the directed-pair default
     cudaGetLastError();
     h->err.clear();
   }
@@ -553,8 +552,8 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
     OD_CKC(cudaMemcpy(h->cut.stencil, st.data(), sizeof(int4) * st.size(), cudaMemcpyHostToDevice));
     OD_CKC(cudaMemset(h->d_pairs, 0, sizeof(unsigned long long)));
     h->has_cut = true;
-    // default: tile pairs with each pair once (512-ion tiles, else 1024) when the tile-pair
-    // matrix fits the budget; the cell-stencil kernel otherwise
+    // default: tile pairs with each pair once (512-ion tiles, else 1024) when their memory
+    // fits the budget; the cell-stencil kernel otherwise
     const int G = od_cutn3_grid(h->N);
     const int cut_ipt = od_cutn3_bytes(h->N, 512, G) <= OD_CUTN3_BUDGET ? 2
                         : (od_cutn3_bytes(h->N, 1024, G) <= OD_CUTN3_BUDGET ? 4 : 0);
@@ -971,8 +970,8 @@ static void free_cutn3(od_handle* h) {
   h->cut.n3 = nullptr;
 }
 
-// Cutoff variant 3: Hilbert-sorted tiles of T ions (ipt 4: 1024, ipt 2: 512) and the dense
-// tile-pair matrix of partial sums (24 bytes per ion and tile).
+// Cutoff variant 3: Hilbert-sorted tiles of T ions (ipt 4: 1024, ipt 2: 512) and the per-slot
+// fixed-point accumulators (24 bytes per slot).
 static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   free_cutn3(h);
   OD_CK(h, cudaSetDevice(h->device));
@@ -1191,7 +1190,7 @@ extern "C" od_status od_autotune(od_handle* h, int32_t use_cache, double* best_p
   for (const auto& sh : shapes) {
     if (sh[2] == 7) {
       // each unordered pair once: timed over a full launch with the default tile, and only
-      // when its tile-pair matrix fits (the pair rate counts directed pairs, as for the others)
+      // (the pair rate counts directed pairs, as for the others)
       if (h->Npad < 8192 || od_set_pair_plan(h, sh[0], sh[1], 7, 0) != OD_OK) {
         cudaGetLastError();
         continue;
@@ -1597,7 +1596,7 @@ extern "C" od_status od_batch_add(od_batch* b, const od_config* cfg, const doubl
   od_handle* h = nullptr;
   od_status st = create_handle(cfg, b->device, false, &h);
   if (st != OD_OK) return bfail(b, st, g_err);
-  // each unordered pair once when the member's tile-pair matrix fits, else the directed kernel
+  // each unordered pair once (od_n3_batch_plan), else the directed kernel
   int ipt = 0;
   const int tile = od_n3_batch_plan(h->Npad, OD_N3_BUDGET, &ipt);
   st = tile ? set_plan_n3(h, ipt, tile) : OD_ERR_OOM;

@@ -45,9 +45,9 @@ struct od_dbufs {
 int od_num_sms(int device);
 
 // Variant 7 (od_n3.cu): whether (ions per lane, tile) has a kernel; the default (ions per lane,
-// tile) for a padded ion count whose tile-pair matrix fits the byte budget (returns the tile, 0
-// when none fits); floats of that matrix; and the launch (pair kernel + fixed-order row sums
-// into slab 0 of ph/pl).
+// tile) for a padded ion count (returns the tile, 0 when none fits the byte budget); the size of
+// the fixed-point accumulators in 4-byte units; and the launch (pair kernel, then with take the
+// accumulators into slab 0 of ph/pl).
 bool od_n3_supported(int ipt, int tile);
 int od_n3_default(int Npad, size_t budget_bytes, int* ipt);
 size_t od_n3_floats(int Npad, int tile);
@@ -62,7 +62,7 @@ struct od_simdesc {
   od_dbufs b;
   int N, Npad, nb, jsplit, chunk, nrec;
   float rho0, newton_r2;
-  int n3_tile;  // variant-7 tile of this member (its tile-pair matrix is b.n3), 0 otherwise
+  int n3_tile;  // variant-7 tile of this member (its accumulators are b.n3), 0 otherwise
 };
 // Device tables of one batch step.
 struct od_batchview {

@@ -151,7 +151,7 @@ int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
   // 4 x 4 with 1024-ion tiles up to 2^16 ions (2.79e12 pair terms/s at 2^16 against 2.51e12
   // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.91e12 at 2^17 against 2.87e12 for 4 x 4,
   // 2.99e12 at 2^18, 3.05e12 at 2^20), then 4 x 4 with 4096-ion tiles: the first whose
-  // tile-pair matrix fits the budget
+  // accumulators fit the budget (always: 24 bytes per ion)
   const int cand[3][2] = {{4, 1024}, {8, 2048}, {4, 4096}};
   for (int c = Npad <= (1 << 16) ? 0 : 1; c < 3; c++)
     if (sizeof(float) * od_n3_floats(Npad, cand[c][1]) <= budget_bytes) {
