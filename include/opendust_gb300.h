@@ -21,7 +21,9 @@
  *    od_last_error(NULL) for failures without a handle).
  *  - One host thread per handle. Each handle owns one CUDA stream.
  *  - All device-side waits inside the library are bounded; a wait that runs out
- *    sets a device error word that the next host call reports as OD_ERR_TIMEOUT.
+ *    sets a device error word that the next host call reports as OD_ERR_TIMEOUT. The step
+ *    that timed out is incomplete (its ion–ion accumulators may be partly filled): destroy the
+ *    handle and start again from the last good state.
  *  - Units at the boundary are SI (m, s, m/s, C, kg, N), as in the reference API.
  *
  * Random numbers (identical definition in the CUDA library and the CPU oracle)
