@@ -171,11 +171,12 @@ class Server:
 
 
 def run_plain(requests: list[Request], device: int = 0, batch_plan: bool = False,
-              pool=None) -> dict:
+              pool=None, interval=None) -> dict:
     """Baseline: the same requests, one at a time through the single-simulation path (its
     default all-pairs plan, or with batch_plan the plan the server's batch gives each request,
     so that results are bitwise comparable). pool: the server's process pool, so that the host
-    part of every request's setup overlaps the GPU work here as it does in the server."""
+    part of every request's setup overlaps the GPU work here as it does in the server.
+    interval: as Server's (None: every step)."""
     reqs = sorted(requests, key=lambda r: r.arrival)
     futures = {r.rid: pool.submit(host_prepare, r) for r in reqs} if pool is not None else None
     t0 = time.perf_counter()
@@ -188,6 +189,8 @@ def run_plain(requests: list[Request], device: int = 0, batch_plan: bool = False
             holder, pos, vel = finish_prepare(r, futures[r.rid].result(), device)
         else:
             holder, pos, vel = prepare(r, device)
+        if interval is not None:
+            holder.cfg.force_every = int(interval(int(r.sim.N)))
         with _lib.Engine(holder, device) as eng:
             if batch_plan:
                 eng.set_pair_plan(*_lib.batch_pair_plan(r.sim.N))

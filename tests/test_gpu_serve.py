@@ -28,3 +28,17 @@ def test_server_results_equal_alone(gpu_lib):
             assert np.array_equal(a.series[k], b.series[k]), (a.rid, k)
         assert np.array_equal(a.averages, b.averages)
     assert stats["latency_p99_s"] >= stats["latency_p50_s"] > 0
+
+
+def test_server_with_force_interval_equals_alone(gpu_lib):
+    # requests served with a force interval (members at different step phases in the mix) equal
+    # the same requests run alone with the same interval and plan, bitwise
+    rule = lambda n: 4 if n >= 4096 else 2
+    reqs = serve.poisson_requests(rate=40.0, duration=0.2, seed=5, log2n=(11, 13), window=21, max_grains=2)
+    mixed = copy.deepcopy(reqs)
+    serve.Server(chunk=5, interval=rule).run(mixed)
+    alone = copy.deepcopy(reqs)
+    serve.run_plain(alone, batch_plan=True, interval=rule)
+    for a, b in zip(sorted(mixed, key=lambda r: r.rid), sorted(alone, key=lambda r: r.rid)):
+        for k in a.series:
+            assert np.array_equal(a.series[k], b.series[k]), (a.rid, k)
