@@ -366,6 +366,15 @@ __device__ __forceinline__ void od_bulk_g2s(void* dst, const void* src, uint32_t
       "l"(src), "r"(bytes), "r"(od_smem_addr(bar))
       : "memory");
 }
+// Programmatic dependent launch (sm_90+): a kernel launched with programmatic stream
+// serialization may start while its predecessor runs; it waits here until the predecessor has
+// completed and its memory is visible (a no-op for an ordinary launch). A kernel lets its
+// successor launch early with od_pdl_trigger (its successors still wait for its completion).
+__device__ __forceinline__ void od_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void od_pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Impulse multiple time stepping (force interval k = p.force_every): the ion–ion force is
 // evaluated at the end of steps with step % k == k - 1 and enters the half kicks at the end of
 // that step and at the start of the next with weight k; weight 1 every step for k = 1.

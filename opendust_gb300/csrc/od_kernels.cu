@@ -551,6 +551,8 @@ __global__ void __launch_bounds__(kBlk) k_kick_flag(const od_dparams* __restrict
                                                     uint32_t* __restrict__ flags,
                                                     const float* __restrict__ cq,
                                                     unsigned long long* __restrict__ acc) {
+  od_pdl_wait();
+  od_pdl_trigger();
   kick_flag_body(*dp, ds, pos, vel, ph, pl, jsplit, fhi, flo, flags, cq,
                  blockIdx.x * blockDim.x + threadIdx.x, acc);  // grid covers Npad exactly
 }
@@ -769,6 +771,8 @@ __global__ void __launch_bounds__(kCT) k_collect_inject(
     float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
     int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
     float4* __restrict__ list_new, float4* __restrict__ list_v) {
+  od_pdl_wait();
+  od_pdl_trigger();
   collect_inject_body(*dp, ds, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
 }
 
@@ -1056,6 +1060,7 @@ __global__ void __launch_bounds__(kBlk) k_correct_orbit_tail(
     double* __restrict__ orbit_part, int nb, double* __restrict__ s_q,
     double* __restrict__ s_orbit, double* __restrict__ s_collect, double* __restrict__ s_dust,
     double* __restrict__ s_field, float* __restrict__ cq) {
+  od_pdl_wait();
   correct_orbit_body(*dp, ds, pos, fhi, flo, flags, list, list_old, list_new, orbit_part, nb,
                      blockIdx.x, gridDim.x - nb);
   if ((int)blockIdx.x >= nb) return;  // re-injected ions' sums: the tail does not read them
@@ -1179,6 +1184,23 @@ cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* pos, float
 }
 
 // ============================================================== launch wrappers
+// launch with programmatic stream serialization (the kernel calls od_pdl_wait first)
+template <typename... KArgs, typename... Args>
+static cudaError_t od_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                                 Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 int od_num_sms(int device) {
   int n = 0;
   cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
@@ -1284,14 +1306,22 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
     return od_launch_force(fc, od_pair_io{b.pos, b.sx, b.sy, b.sz, b.n3}, N, Npad, b.part_hi, b.part_lo,
                            &ds->err, s, fc.acc == nullptr);
   const int jsplit = fc.cut ? 1 : fc.plan.jsplit;
-  k_kick_flag<<<nb, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit, b.fhi, b.flo,
-                                  b.flags, b.cq, fc.acc);
-  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
-                                     b.list_old, b.list_new, b.list_v);
-  k_correct_orbit_tail<<<nb + nrec, kBlk, 0, s>>>(dp, ds, b.pos, b.fhi, b.flo, b.flags, b.list,
-                                                 b.list_old, b.list_new, b.orbit_part, nb, b.s_q,
-                                                 b.s_orbit, b.s_collect, b.s_dust, b.s_field,
-                                                 b.cq);
+  // K3, K4 and K5 with programmatic dependent launch: each starts launching while its
+  // predecessor runs and waits in od_pdl_wait for the predecessor's results
+  cudaError_t e = od_launch_pdl(k_kick_flag, dim3(nb), dim3(kBlk), s, dp, ds, b.pos, b.vel,
+                                (const float4*)b.part_hi, (const float4*)b.part_lo, jsplit, b.fhi,
+                                b.flo, b.flags, (const float*)b.cq, fc.acc);
+  if (e == cudaSuccess)
+    e = od_launch_pdl(k_collect_inject, dim3(1), dim3(kCT), s, dp, ds, b.pos, b.vel,
+                      (const uint32_t*)b.flags, b.list, b.list_bits, b.list_old, b.list_new,
+                      b.list_v);
+  if (e == cudaSuccess)
+    e = od_launch_pdl(k_correct_orbit_tail, dim3(nb + nrec), dim3(kBlk), s, dp, ds,
+                      (const float4*)b.pos, b.fhi, b.flo, (const uint32_t*)b.flags,
+                      (const int32_t*)b.list, (const float4*)b.list_old,
+                      (const float4*)b.list_new, b.orbit_part, nb, b.s_q, b.s_orbit,
+                      b.s_collect, b.s_dust, b.s_field, b.cq);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
