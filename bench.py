@@ -56,7 +56,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="full_plain",
-                    choices=["full_plain", "small_plain", "field_chain", "sweep", "serve"])
+                    choices=["full_plain", "small_plain", "field_chain", "cutoff_scaling", "sweep",
+                             "serve"])
+    ap.add_argument("--scale", type=int, default=8,
+                    help="cutoff_scaling: k in N = k*2^15 ions, H = k*6 lambda")
     ap.add_argument("--sweep-sims", type=int, default=64)
     ap.add_argument("--sweep-exact", action="store_true")
     ap.add_argument("--pilot-steps", type=int, default=100)
@@ -149,9 +152,11 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def workload(name: str, n_total: int):
+def workload(name: str, n_total: int, scale: int = 8):
     from opendust_gb300 import workloads
 
+    if name == "cutoff_scaling":
+        return workloads.cutoff_scaling(k=scale, n=n_total)
     if name == "full_plain":
         return workloads.full_plain(n=n_total)
     if name == "field_chain":
@@ -160,19 +165,26 @@ def workload(name: str, n_total: int):
 
 
 def describe(name, sim, ext):
-    w = {"full_plain": "Ar+ Mach 1 flow past one grain (r=10 um, consistent charging), "
+    w = {"cutoff_scaling": "",
+         "full_plain": "Ar+ Mach 1 flow past one grain (r=10 um, consistent charging), "
                        "N=2^20 superions, all-pairs Yukawa, charge-exchange mfp 2 lambda, d_t=1e-10 s",
          "small_plain": "Ar+ Mach 1 flow past one grain, N=16384, all-pairs Yukawa, no collisions, "
                         "d_t=1e-10 s",
          "field_chain": "field-driven Ar+ (Mach 0.5, charge-exchange mfp 1 lambda) past a chain of 5 "
                         "grains (r=5 um, 1 lambda apart), N=2^19, cutoff 2 lambda over a device cell "
                         "list, d_t=1e-10 s"}[name]
-    cut = "cutoff_distance" in ext
+    if name == "cutoff_scaling":
+        k = int(sim.N) // 2**15
+        w = (f"the reference's cutoff benchmark at k={k}: Ar+ Mach 1 (T_e=29011 K, T_i=290.11 K), "
+             f"R=3 lambda, H={6 * k} lambda, N={k}*2^15, cutoff 3.2 lambda with switching from "
+             "3.0 lambda, one grain of given charge, d_t=3.5148e-9 s")
+    cut = "cutoff_distance" in ext or ext.get("cutOff", False)
     return {"workload": f"{name}: {w}", "n_ions": int(sim.N), "grains": len(sim_grains(name)),
-            "force": "cutoff over cell list" if cut else "all-pairs",
+            "force": "cutoff (Hilbert-sorted tile pairs)" if cut else "all-pairs",
             "collisions": ext.get("collisions", "none"),
             "l2": "flushed (512 MB write) before every timed step",
-            "steps_in_workload": {"full_plain": 20000, "small_plain": 2000, "field_chain": 30000}[name]}
+            "steps_in_workload": {"full_plain": 20000, "small_plain": 2000, "field_chain": 30000,
+                                  "cutoff_scaling": 3}[name]}
 
 
 def sim_grains(name):
@@ -208,7 +220,7 @@ def run_reference(args, dist: Dist):
     from opendust_gb300 import build_simulation, setup_host
     from oracle import oracle
 
-    plasma, sim, grains, d, ext = workload(args.workload, 10)
+    plasma, sim, grains, d, ext = workload(args.workload, 10, args.scale)
     holder, _ = build_simulation(plasma, sim, grains, d, seed=1, trap=np.zeros(15), **ext)
     pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
                                         plasma.v_fl, plasma.v_T, d, 1)
@@ -222,7 +234,8 @@ def run_reference(args, dist: Dist):
         per_step.append(s)
     sec = sum(per_step) / len(per_step)
     value = sim.N / sec
-    sample = (f"{T} of {sim.N} target ions x 2 ion-ion evaluations against all sources + one "
+    srcs = "the sources within the cutoff (cell list)" if holder.cfg.cutoff > 0 else "all sources"
+    sample = (f"{T} of {sim.N} target ions x 2 ion-ion evaluations against {srcs} + one "
               f"linear pass over all ions per step; time per full step extrapolated by N/T")
     line = {
         "impl": "reference", "metric": "ion-steps/s", "value": value, "unit": "ion-steps/s",
@@ -265,7 +278,7 @@ def run_ours(args, dist: Dist):
     K, W = args.steps, args.warmup
     K_e2e = max(2, K)
     n_total = W + K + K_e2e + 5
-    plasma, sim, grains, d, ext = workload(args.workload, n_total)
+    plasma, sim, grains, d, ext = workload(args.workload, n_total, args.scale)
     seed = 1000 + dist.rank
     holder, _ = build_simulation(plasma, sim, grains, d, seed=seed, device=device, **ext)
     pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
@@ -347,6 +360,9 @@ def run_ours(args, dist: Dist):
     eng.close()
     assert np.isfinite(ser["q"]).all() and np.isfinite(p_out).all()
 
+    script = None
+    if args.workload == "cutoff_scaling" and dist.rank == 0:
+        script = time_reference_script(args.scale, device)
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         from oracle import oracle
@@ -384,8 +400,32 @@ def run_ours(args, dist: Dist):
             "clocks": clk,
             "cpu_baseline": cpu,
         }
+        if script is not None:
+            line["reference_script"] = script
         print(json.dumps(line), flush=True)
     return 0
+
+
+# wall seconds of one run of performance/CutOff-Performance/benchmark.py per scale k, as logged
+# in performance/CutOff-Performance/time.txt (V100-class GPU; setup + 3 steps)
+CUTOFF_SCRIPT_PUBLISHED_S = {1: 80.17, 2: 174.09, 4: 388.38, 8: 886.01, 32: 1316.75}
+
+
+def time_reference_script(k: int, device: int):
+    """The reference's cutoff benchmark script through the drop-in API: OpenDust(...) with its
+    parameters and simulate(deviceIndex, cutOff=True), 3 steps; wall clock around simulate() as
+    the script times it (setup of tables, trap fit and initial state included)."""
+    from opendust_gb300 import OpenDust, OutputParameters, workloads
+
+    plasma, sim, grains, d, _ = workloads.cutoff_scaling(k=k, n=3)
+    od = OpenDust(plasma, sim, OutputParameters(2999, 2999), grains, d)
+    t0 = time.perf_counter()
+    od.simulate(deviceIndex=str(device), cutOff=True, quiet=True)
+    t1 = time.perf_counter()
+    pub = CUTOFF_SCRIPT_PUBLISHED_S.get(k)
+    return {"k": k, "n_ions": int(sim.N), "steps": 3, "simulate_s": t1 - t0, "published_s": pub,
+            "published_hw": "V100-class (reference log)",
+            "source": "performance/CutOff-Performance/benchmark.py, time.txt"}
 
 
 def run_sweep(args, dist: Dist):

@@ -13,6 +13,8 @@ objects for the five workloads this engine is measured on:
   field_chain   field-driven ions, E set for Mach 0.5 with mean free path 1 lambda, five
                 grains r=5e-6 m at z = -2..2 lambda on the axis, N=2^19, cutoff 2 lambda,
                 30000 steps.
+  cutoff_scaling  the reference's cutoff benchmark at scale k (N = k*2^15, H = k*6 lambda,
+                cutoff 3.2 lambda with switching from 3.0 lambda, 3 steps).
   (the batched-sweep and serving-stream workloads draw their members from a seed; see
    sweep_member()).
 """
@@ -63,6 +65,20 @@ def field_chain(N: int = 2**19, n: int = 30000, d_t: float = 1e-10):
     grains = [DustParticle(0.0, 0.0, z * lam, 5e-6, "consistent", 0.0) for z in (-2, -1, 0, 1, 2)]
     return plasma, sim, grains, "fieldDriven", {
         "collisions": "mfp", "mean_free_path": mfp, "cutoff_distance": 2 * lam}
+
+
+def cutoff_scaling(k: int = 8, n: int = 3):
+    """The reference's own cutoff benchmark (performance/CutOff-Performance/benchmark.py:14-75)
+    at scale k: Ar+ (m=6.6335209e-26 kg, T_i=290.11 K, T_e=29011 K, n_inf=1e14 m^-3), Mach 1
+    Maxwellian inflow, R=3 lambda, H=k*6 lambda, N=k*2^15 (constant density), d_t=3.5148e-9 s,
+    n=3 steps, one grain r=5.88e-6 m at z=-1 lambda with the given charge 392500 e, and
+    simulate(cutOff=True): cutoff 3.2 lambda with OpenMM's switching from 3.0 lambda
+    (performance/CutOff-Performance/opendust.py:480-484)."""
+    plasma = PlasmaParametersInSIUnitsMaxwell(290.11, 29011.0, 1e14, 1.0, 6.6335209e-26)
+    lam = plasma.r_D_e
+    sim = SimulationParametersInSIUnits(3 * lam, k * 6 * lam, k * 2**15, n, 3.5148240854e-09, plasma)
+    grains = [DustParticle(0.0, 0.0, -1 * lam, 58.8e-7, "given", 392500.0 * plasma.e)]
+    return plasma, sim, grains, "Maxwellian", {"cutOff": True}
 
 
 def sweep_member(seed: int, n_steps: int = 5000, max_log2n: int = 18):

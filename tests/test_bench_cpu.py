@@ -37,3 +37,24 @@ def test_traffic_files_match_their_capture_only():
     assert bench.load_traffic(2**19, {"variant": 7, "jsplit": 2048}) is None
     assert 1e7 < bench.load_traffic(2**19, {"variant": 3, "jsplit": 512}, cutoff=True) < 1e9
     assert bench.load_traffic(2**19, {"variant": 3, "jsplit": 1024}, cutoff=True) is None
+
+
+def test_cutoff_scaling_workload_matches_reference_benchmark():
+    # performance/CutOff-Performance/benchmark.py:14-75 at scale k, with simulate(cutOff=True)
+    import bench
+    from opendust_gb300 import build_simulation, workloads
+
+    for k in (1, 8, 32):
+        plasma, sim, grains, d, ext = workloads.cutoff_scaling(k=k)
+        lam = plasma.r_D_e
+        assert sim.N == k * 2**15 and sim.n == 3
+        assert abs(sim.R / lam - 3) < 1e-12 and abs(sim.H / lam - 6 * k) < 1e-9
+        assert abs(sim.d_t - 3.5148240854e-09) < 1e-20 and d == "Maxwellian"
+        assert len(grains) == 1 and grains[0].chargeCalculationMethod == "given"
+        assert abs(grains[0].q / (392500.0 * plasma.e) - 1) < 1e-15
+        assert abs(grains[0].z / lam + 1) < 1e-12 and ext == {"cutOff": True}
+        desc = bench.describe("cutoff_scaling", sim, ext)
+        assert desc["n_ions"] == k * 2**15 and desc["steps_in_workload"] == 3
+    holder, _ = build_simulation(plasma, sim, grains, d, trap=[0.0] * 15, **ext)
+    assert abs(holder.cfg.cutoff / lam - 3.2) < 1e-12 and abs(holder.cfg.switch_dist / lam - 3.0) < 1e-12
+    assert set(bench.CUTOFF_SCRIPT_PUBLISHED_S) == {1, 2, 4, 8, 32}
