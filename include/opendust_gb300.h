@@ -202,7 +202,11 @@ od_status od_destroy(od_handle* h);
 const char* od_last_error(const od_handle* h);
 
 /* Replaces context.setPositions / setVelocities (opendust.py:1043-1044) and the
- * restart-file read (opendust.py:452-466). pos [m], vel [m/s], both n x 3 row-major. */
+ * restart-file read (opendust.py:452-466). pos [m], vel [m/s], both n x 3 row-major.
+ * Positions are held cell-relative: per axis a cell index c on a grid of side s (in Debye
+ * lengths, the smallest power of two not below 1/256 of the domain's half extent) and the FP32 offset
+ * x - c s, rounded once from the FP64 input; the force, flag and injection kernels read the
+ * absolute FP32 position fmaf(c, s, offset) derived from it each step. */
 od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n);
 
 /* Samples the initial ion state on the device (replaces the host loops of opendust.py:373-451):
@@ -243,7 +247,8 @@ od_status od_set_grains(od_handle* h, const double* x, const double* y, const do
  * a new simulation per window (launch.py:120-145). */
 od_status od_begin_window(od_handle* h);
 
-/* Replaces context.getState(...).getPositions/getVelocities (opendust.py:1074-1078, :1102-1105). */
+/* Replaces context.getState(...).getPositions/getVelocities (opendust.py:1074-1078, :1102-1105).
+ * Positions are the cell-relative state, exactly (c s + offset in FP64). */
 od_status od_get_state(od_handle* h, double* pos, double* vel, int64_t n);
 
 /* Replaces `integrator.step(1)` plus the host tail, nsteps times (opendust.py:1059-1383).

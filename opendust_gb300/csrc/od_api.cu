@@ -329,6 +329,10 @@ static void fill_params(const od_config* c, int N, int Npad, od_dparams* p) {
   }
   p->Rh2 = Rh * Rh;
   p->Hh_half_d = Hh / 2.0;
+  // cell side of the cell-relative positions: the power of two with the domain's half extent
+  // at most 256 cells (of the 512 each way the 10-bit indices give)
+  p->rel_s = (float)std::ldexp(1.0, (int)std::ceil(std::log2(std::max(Rh, Hh / 2.0) / 256.0)));
+  p->rel_inv = 1.0f / p->rel_s;
   p->Rh2f = (float)(Rh * Rh);
   p->Hz_f = float_ceil(Hh / 2.0);
   p->p_coll = dt * c->w_c;
@@ -410,7 +414,7 @@ static void free_all(od_handle* h) {
   if (h->graph_exec_nf) { cudaGraphExecDestroy(h->graph_exec_nf); h->graph_exec_nf = nullptr; }
   if (h->graph_nf) { cudaGraphDestroy(h->graph_nf); h->graph_nf = nullptr; }
   free_timing(h);
-  void* ptrs[] = {h->dp, h->ds, h->b.pos, h->b.vel, h->b.fhi, h->b.flo, h->b.part_hi, h->b.part_lo,
+  void* ptrs[] = {h->dp, h->ds, h->b.pos, h->b.rel, h->b.vel, h->b.fhi, h->b.flo, h->b.part_hi, h->b.part_lo,
                   h->b.flags, h->b.list, h->b.list_bits, h->b.list_old, h->b.list_new, h->b.list_v,
                   h->b.orbit_part, h->b.s_q, h->b.s_orbit, h->b.s_collect, h->b.s_dust,
                   h->b.s_field, h->b.cq, h->snap_pos, h->snap_hi, h->snap_lo, h->snap_counts,
@@ -478,6 +482,7 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
   OD_CKC(dalloc(&h->dp, 1));
   OD_CKC(dalloc(&h->ds, 1));
   OD_CKC(dalloc(&h->b.pos, Np));
+  OD_CKC(dalloc(&h->b.rel, Np));
   OD_CKC(dalloc(&h->b.vel, Np));
   OD_CKC(dalloc(&h->b.fhi, Np));
   OD_CKC(dalloc(&h->b.flo, Np));
@@ -554,9 +559,9 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
     h->has_cut = true;
     // default: tile pairs with each pair once (512-ion tiles, else 1024) when their memory
     // fits the budget; the cell-stencil kernel otherwise
-    const int G = od_cutn3_grid(h->N);
-    const int cut_ipt = od_cutn3_bytes(h->N, 512, G) <= OD_CUTN3_BUDGET ? 2
-                        : (od_cutn3_bytes(h->N, 1024, G) <= OD_CUTN3_BUDGET ? 4 : 0);
+    const int nc3 = od_cutn3_grid(h->N, h->hp.Rh, h->hp.Hh).ncells;
+    const int cut_ipt = od_cutn3_bytes(h->N, 512, nc3) <= OD_CUTN3_BUDGET ? 2
+                        : (od_cutn3_bytes(h->N, 1024, nc3) <= OD_CUTN3_BUDGET ? 4 : 0);
     if (cut_ipt && alloc_cutn3(h, cut_ipt, cut_ipt == 2 ? 512 : 1024) != OD_OK) {
       cudaGetLastError();
       h->err.clear();
@@ -569,6 +574,7 @@ static od_status create_handle(const od_config* cfg, int32_t device, bool n3_def
   // padded slots: far-away sources, zero velocity
   std::vector<float4> pad(Np, make_float4(OD_SENTINEL, OD_SENTINEL, OD_SENTINEL, 0.f));
   OD_CKC(cudaMemcpy(h->b.pos, pad.data(), sizeof(float4) * Np, cudaMemcpyHostToDevice));
+  OD_CKC(cudaMemset(h->b.rel, 0, sizeof(float4) * Np));
   OD_CKC(od_launch_aos_to_soa(h->b.pos, h->Npad, h->b.sx, h->b.sy, h->b.sz, h->stream));
   OD_CKC(cudaMemset(h->b.vel, 0, sizeof(float4) * Np));
   OD_CKC(cudaMemset(h->b.fhi, 0, sizeof(float4) * Np));
@@ -630,13 +636,41 @@ static od_status refresh_forces(od_handle* h) {
   return OD_OK;
 }
 
+// Cell-relative state (od_common.cuh) of positions in metres, and the absolute FP32 positions
+// that the device derives from it: per axis, c = floor(x / s) and the offset x - c s rounded
+// once to FP32 (from the FP64 position, so nothing is lost to an FP32 absolute first).
+static void to_rel_state(const od_handle* h, const double* pos, int64_t n,
+                         std::vector<float4>& rel, std::vector<float4>& xp) {
+  const double lam = h->hp.lam, s = h->hp.rel_s, inv = h->hp.rel_inv;
+  rel.resize(n);
+  xp.resize(n);
+  for (int64_t i = 0; i < n; i++) {
+    int c[3];
+    float o[3], a[3];
+    for (int d = 0; d < 3; d++) {
+      const double v = pos[3 * i + d] / lam;
+      c[d] = od_rel_clamp((int)std::max(std::min(std::floor(v * inv), 1e9), -1e9));
+      o[d] = (float)(v - c[d] * s);
+      if (o[d] == (float)s && c[d] < OD_REL_BIAS - 1) { c[d] += 1; o[d] = 0.f; }
+      a[d] = (float)std::fma((double)c[d], s, (double)o[d]);  // exact, then rounded once
+    }
+    int key = od_rel_pack(c[0], c[1], c[2]);
+    float w;
+    memcpy(&w, &key, sizeof(w));
+    rel[i] = make_float4(o[0], o[1], o[2], w);
+    xp[i] = make_float4(a[0], a[1], a[2], 0.f);
+  }
+}
+
 extern "C" od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!pos || !vel) return fail(h, OD_ERR_INVALID, "pos/vel is NULL");
   if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
   OD_CK(h, cudaSetDevice(h->device));
-  std::vector<float4> xp, vp;
+  std::vector<float4> xp, vp, rel;
   to_device_units(h, pos, vel, n, xp, &vp);
+  to_rel_state(h, pos, n, rel, xp);
+  OD_CK(h, cudaMemcpyAsync(h->b.rel, rel.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
   OD_CK(h, cudaMemcpyAsync(h->b.pos, xp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
   OD_CK(h, cudaMemcpyAsync(h->b.vel, vp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
   od_status st = refresh_forces(h);
@@ -664,7 +698,7 @@ extern "C" od_status od_init_state(od_handle* h, const double* vz_v, const doubl
     OD_CK(h, cudaMemcpy(d_v, v.data(), sizeof(float) * vz_n, cudaMemcpyHostToDevice));
     OD_CK(h, cudaMemcpy(d_x, vz_cdf, sizeof(double) * vz_n, cudaMemcpyHostToDevice));
   }
-  cudaError_t e = od_launch_init_state(h->dp, h->N, h->b.pos, h->b.vel, d_v, d_x, vz_n,
+  cudaError_t e = od_launch_init_state(h->dp, h->N, h->b.rel, h->b.pos, h->b.vel, d_v, d_x, vz_n,
                                        &h->ds->err, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (d_v) cudaFree(d_v);
@@ -780,13 +814,21 @@ extern "C" od_status od_get_state(od_handle* h, double* pos, double* vel, int64_
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
   OD_CK(h, cudaSetDevice(h->device));
-  std::vector<float4> xp(n), vp(n);
-  OD_CK(h, cudaMemcpyAsync(xp.data(), h->b.pos, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<float4> rp(n), vp(n);
+  OD_CK(h, cudaMemcpyAsync(rp.data(), h->b.rel, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
   OD_CK(h, cudaMemcpyAsync(vp.data(), h->b.vel, sizeof(float4) * n, cudaMemcpyDeviceToHost, h->stream));
   OD_CK(h, cudaStreamSynchronize(h->stream));
-  const double lam = h->hp.lam, vunit = h->hp.vunit;
+  const double lam = h->hp.lam, vunit = h->hp.vunit, s = h->hp.rel_s;
   for (int64_t i = 0; i < n; i++) {
-    if (pos) { pos[3 * i] = xp[i].x * lam; pos[3 * i + 1] = xp[i].y * lam; pos[3 * i + 2] = xp[i].z * lam; }
+    if (pos) {  // the cell-relative state, exactly (c s + offset is exact in FP64)
+      int key;
+      memcpy(&key, &rp[i].w, sizeof(key));
+      const double c[3] = {(double)((key & 1023) - OD_REL_BIAS), (double)(((key >> 10) & 1023) - OD_REL_BIAS),
+                           (double)(((key >> 20) & 1023) - OD_REL_BIAS)};
+      pos[3 * i] = (c[0] * s + rp[i].x) * lam;
+      pos[3 * i + 1] = (c[1] * s + rp[i].y) * lam;
+      pos[3 * i + 2] = (c[2] * s + rp[i].z) * lam;
+    }
     if (vel) { vel[3 * i] = vp[i].x * vunit; vel[3 * i + 1] = vp[i].y * vunit; vel[3 * i + 2] = vp[i].z * vunit; }
   }
   return OD_OK;
@@ -979,14 +1021,17 @@ static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   od_cutn3* L = new (std::nothrow) od_cutn3();
   if (!L) return fail(h, OD_ERR_OOM, "host allocation");
   h->cut.n3 = L;
-  const int N = h->N, G = od_cutn3_grid(N);
+  const int N = h->N;
+  const od_cgrid g = od_cutn3_grid(N, h->hp.Rh, h->hp.Hh);
+  const int G = g.G;
   L->G = G;
   L->bits = 0;
   while ((1 << L->bits) < G) L->bits++;
-  L->ncells = G * G * G;
-  const double side = std::max(2.0 * h->hp.Rh, (double)h->hp.Hh) * 1.02;
-  L->lo = (float)(-side / 2.0);
-  L->inv_s = (float)(G / side);
+  L->nb = g.nb;
+  L->ncells = g.ncells;
+  L->lo = (float)(-g.side / 2.0);
+  L->lo_z = (float)(-g.side * g.nb / 2.0);
+  L->inv_s = (float)(G / g.side);
   L->T = T; L->ipt = ipt;
   L->nT = (N + T - 1) / T;
   L->nslots = L->nT * T;
@@ -1824,9 +1869,9 @@ extern "C" od_status od_config_device_bytes(const od_config* cfg, int64_t* bytes
   const int64_t P = std::max(cfg->n_grains, 1);
   int64_t b = 0;
   if (cfg->force_method == OD_FORCE_CUTOFF) {  // tile-pair cutoff, as od_create chooses it
-    const int G = od_cutn3_grid((int)cfg->n_ions);
-    const size_t c512 = od_cutn3_bytes((int)cfg->n_ions, 512, G);
-    const size_t c1024 = od_cutn3_bytes((int)cfg->n_ions, 1024, G);
+    const int nc = od_cutn3_grid((int)cfg->n_ions, cfg->R, cfg->H).ncells;
+    const size_t c512 = od_cutn3_bytes((int)cfg->n_ions, 512, nc);
+    const size_t c1024 = od_cutn3_bytes((int)cfg->n_ions, 1024, nc);
     if (c512 <= OD_CUTN3_BUDGET) b += (int64_t)c512;
     else if (c1024 <= OD_CUTN3_BUDGET) b += (int64_t)c1024;
   }
@@ -1957,9 +2002,10 @@ extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
   if (!h->shard) return fail(h, OD_ERR_STATE, "not a shard handle (od_shard_create)");
   if (!pos_all || !vel_own) return fail(h, OD_ERR_INVALID, "pos_all/vel_own is NULL");
   OD_CK(h, cudaSetDevice(h->device));
-  std::vector<float4> xa, vp, xo;
-  to_device_units(h, pos_all, nullptr, h->n_total, xa, nullptr);
+  std::vector<float4> xa, vp, xo, ra, ro;
+  to_rel_state(h, pos_all, h->n_total, ra, xa);  // every shard's sources, as their owners hold them
   to_device_units(h, pos_all + 3 * h->ion0, vel_own, h->N, xo, &vp);
+  to_rel_state(h, pos_all + 3 * h->ion0, h->N, ro, xo);
   std::vector<float> c(h->n_total);
   float* dst[3] = {h->ssx, h->ssy, h->ssz};
   for (int d = 0; d < 3; d++) {
@@ -1967,6 +2013,7 @@ extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
     OD_CK(h, cudaMemcpy(dst[d], c.data(), sizeof(float) * h->n_total, cudaMemcpyHostToDevice));
   }
   OD_CK(h, cudaMemcpy(h->b.pos, xo.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
+  OD_CK(h, cudaMemcpy(h->b.rel, ro.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
   OD_CK(h, cudaMemcpy(h->b.vel, vp.data(), sizeof(float4) * h->N, cudaMemcpyHostToDevice));
   od_status st = shard_forces_now(h, true);
   if (st != OD_OK) return st;

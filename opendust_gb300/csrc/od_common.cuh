@@ -41,6 +41,7 @@ struct od_dparams {
   float gr2f[OD_MAX_GRAINS];
   float Rh2f, Hz_f;
   float mfp_inv, vmax_mfp;
+  float rel_s, rel_inv;              // cell side of the cell-relative positions (a power of two)
   // FP64 exact-flag constants (identical doubles in the CPU oracle)
   double gx[OD_MAX_GRAINS], gy[OD_MAX_GRAINS], gz[OD_MAX_GRAINS], gr2[OD_MAX_GRAINS];
   double Rh2, Hh_half_d;
@@ -405,4 +406,60 @@ __device__ __forceinline__ bool od_mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 __device__ __forceinline__ void od_mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(od_smem_addr(bar)) : "memory");
+}
+
+// Cell-relative positions. The integration state of an ion is its cell (cx, cy, cz) on a grid
+// of side s = rel_s (a power of two in lambda units, chosen per simulation so that the domain
+// spans at most half of the index range) and its FP32 offset from that cell's corner; w holds
+// the three cell indices, biased by 512 and packed 10 bits each (bits 30-31 stay clear, so the
+// word is never a NaN pattern). The absolute FP32 position that the force, flag and injection
+// kernels read is fmaf(c, s, offset): the exact sum, rounded once. An offset stays below s, so
+// the drift keeps 24 bits below the cell size whatever the distance from the origin.
+constexpr int OD_REL_BIAS = 512;   // cell indices in [-512, 511]
+__host__ __device__ __forceinline__ int od_rel_pack(int cx, int cy, int cz) {
+  return (cx + OD_REL_BIAS) | ((cy + OD_REL_BIAS) << 10) | ((cz + OD_REL_BIAS) << 20);
+}
+__host__ __device__ __forceinline__ int od_rel_clamp(int c) {
+  return c < -OD_REL_BIAS ? -OD_REL_BIAS : (c > OD_REL_BIAS - 1 ? OD_REL_BIAS - 1 : c);
+}
+__device__ __forceinline__ int3 od_rel_cells(float w) {
+  const int k = __float_as_int(w);
+  return make_int3((k & 1023) - OD_REL_BIAS, ((k >> 10) & 1023) - OD_REL_BIAS,
+                   ((k >> 20) & 1023) - OD_REL_BIAS);
+}
+// absolute FP32 position of a cell-relative state
+__device__ __forceinline__ float4 od_rel_abs(const od_dparams& p, float4 r) {
+  const int3 c = od_rel_cells(r.w);
+  return make_float4(__fmaf_rn((float)c.x, p.rel_s, r.x), __fmaf_rn((float)c.y, p.rel_s, r.y),
+                     __fmaf_rn((float)c.z, p.rel_s, r.z), 0.f);
+}
+// cell-relative state of an absolute FP32 position (offset x - c s rounded once)
+__device__ __forceinline__ float od_rel_axis(float x, float s, float inv, int& c) {
+  c = od_rel_clamp((int)floorf(x * inv));
+  return __fmaf_rn(-(float)c, s, x);
+}
+__device__ __forceinline__ float4 od_rel_encode(const od_dparams& p, float x, float y, float z) {
+  int cx, cy, cz;
+  const float ox = od_rel_axis(x, p.rel_s, p.rel_inv, cx);
+  const float oy = od_rel_axis(y, p.rel_s, p.rel_inv, cy);
+  const float oz = od_rel_axis(z, p.rel_s, p.rel_inv, cz);
+  return make_float4(ox, oy, oz, __int_as_float(od_rel_pack(cx, cy, cz)));
+}
+// offset o += d on one axis, moved to the cell it has entered
+__device__ __forceinline__ float od_rel_move(float o, float d, float s, float inv, int& c) {
+  o += d;
+  if (!(o >= 0.f && o < s)) {
+    const int cn = od_rel_clamp(c + (int)floorf(o * inv));
+    o = __fmaf_rn(-(float)(cn - c), s, o);
+    c = cn;
+  }
+  return o;
+}
+__device__ __forceinline__ void od_rel_drift(const od_dparams& p, float4& r, float dx, float dy,
+                                             float dz) {
+  int3 c = od_rel_cells(r.w);
+  r.x = od_rel_move(r.x, dx, p.rel_s, p.rel_inv, c.x);
+  r.y = od_rel_move(r.y, dy, p.rel_s, p.rel_inv, c.y);
+  r.z = od_rel_move(r.z, dz, p.rel_s, p.rel_inv, c.z);
+  r.w = __int_as_float(od_rel_pack(c.x, c.y, c.z));
 }

@@ -18,15 +18,20 @@ __global__ void k_mc_clear(int ncells, int32_t* __restrict__ count, int32_t* __r
   if (c < ncells) { count[c] = 0; fill[c] = 0; }
 }
 
-__global__ void k_mc_count(int n, const float4* __restrict__ pos, float lo, float inv_s, int G,
-                           int32_t* __restrict__ cell_of, int32_t* __restrict__ count) {
+// Cubes of G^3 cells stacked nb deep along z (nb = 1 for a compact domain); a cell's key is its
+// cube's index times G^3 plus its index along the cube's Hilbert curve.
+__global__ void k_mc_count(int n, const float4* __restrict__ pos, float lo, float lo_z,
+                           float inv_s, int G, int nb, int32_t* __restrict__ cell_of,
+                           int32_t* __restrict__ count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 p = pos[i];
+  const int bits = 31 - __clz(G);
   const int cx = min(max((int)floorf((p.x - lo) * inv_s), 0), G - 1);
   const int cy = min(max((int)floorf((p.y - lo) * inv_s), 0), G - 1);
-  const int cz = min(max((int)floorf((p.z - lo) * inv_s), 0), G - 1);
-  const int c = (int)od_hilbert3((uint32_t)cx, (uint32_t)cy, (uint32_t)cz, 31 - __clz(G));
+  const int cz = min(max((int)floorf((p.z - lo_z) * inv_s), 0), nb * G - 1);
+  const int c = ((cz >> bits) << (3 * bits)) +
+                (int)od_hilbert3((uint32_t)cx, (uint32_t)cy, (uint32_t)(cz & (G - 1)), bits);
   cell_of[i] = c;
   atomicAdd(&count[c], 1);
 }
@@ -509,15 +514,22 @@ __global__ void __launch_bounds__(256) k_slot_take(int nslots, unsigned long lon
 
 }  // namespace
 
-int od_cutn3_grid(int N) {
-  // about 16 ions per cell: G the smallest power of two with G^3 >= N / 22, 8 <= G <= 128
-  int G = 8;
-  while (G < 128 && (double)G * G * G * 8.0 * 16.0 < (double)N * 1.4142) G <<= 1;
-  return G;
+od_cgrid od_cutn3_grid(int N, double R, double H) {
+  od_cgrid g;
+  // a domain at most 1.5 times as high as wide is one cube; a taller one a column of cubes as
+  // wide as the domain, so that the cells keep their size whatever the aspect ratio
+  g.nb = H <= 3.0 * R ? 1 : (int)std::ceil(H / (2.0 * R));
+  g.side = (g.nb == 1 ? std::max(2.0 * R, H) : 2.0 * R) * 1.02;
+  // about 16 ions per cell: G the smallest power of two with G^3 >= (N / nb) / 22, 8 <= G <= 128
+  const double per = (double)N / g.nb;
+  g.G = 8;
+  while (g.G < 128 && (double)g.G * g.G * g.G * 8.0 * 16.0 < per * 1.4142) g.G <<= 1;
+  g.ncells = g.nb * g.G * g.G * g.G;
+  return g;
 }
 
-size_t od_cutn3_bytes(int N, int T, int G) {
-  const size_t nT = (size_t)((N + T - 1) / T), ns = nT * T, nc = (size_t)G * G * G;
+size_t od_cutn3_bytes(int N, int T, int ncells) {
+  const size_t nT = (size_t)((N + T - 1) / T), ns = nT * T, nc = (size_t)ncells;
   const size_t nw = (nT + 31) / 32;
   return sizeof(unsigned long long) * 3 * ns                 // accumulators
          + sizeof(int2) * nT * (nT + 1) / 2                   // pairs
@@ -559,7 +571,8 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
                                 float4* part_lo, float rho0, float rc, float rs, uint32_t* err,
                                 unsigned long long* pair_count, cudaStream_t s) {
   k_mc_clear<<<(L.ncells + 255) / 256, 256, 0, s>>>(L.ncells, L.count, L.fill);
-  k_mc_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, L.lo, L.inv_s, L.G, L.cell_of, L.count);
+  k_mc_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, L.lo, L.lo_z, L.inv_s, L.G, L.nb,
+                                              L.cell_of, L.count);
   k_scan_excl<<<1, 1024, 0, s>>>(L.ncells, L.count, L.start);
   k_mc_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, L.cell_of, L.start, L.fill, L.perm);
   k_mc_sort<<<L.ncells, 128, 0, s>>>(L.count, L.start, pos, L.perm, L.xs, L.ys, L.zs, err);

@@ -28,7 +28,10 @@ struct od_pair_io {
 
 // Device buffers of one simulation.
 struct od_dbufs {
-  float4 *pos, *vel, *fhi, *flo;        // ion state and ion–ion sums (two-float)
+  float4 *pos, *vel, *fhi, *flo;        // absolute FP32 positions (derived from rel each
+                                        // step), velocities, ion–ion sums (two-float)
+  float4* rel;                          // [Npad] position state: cell-relative FP32 offsets
+                                        // and packed cell indices (od_rel_* in od_common.cuh)
   float4 *part_hi, *part_lo;            // [jsplit][Npad] partial sums
   uint32_t* flags;                      // [nwords] ballot words
   int32_t* list;                        // [Npad] flagged ion indices, increasing
@@ -104,8 +107,9 @@ struct od_cellgeom {
 // come within the cutoff evaluated with each unordered pair once (64-ion group pairs farther
 // apart than the cutoff skipped).
 struct od_cutn3 {
-  int G, bits, ncells;              // cells per axis (power of two), key bits per axis
-  float lo, inv_s;                  // grid origin (every axis) and 1 / cell side (lambda)
+  int G, bits, nb, ncells;          // cells per cube axis (power of two), key bits per axis,
+                                    // cubes along z, nb * G^3
+  float lo, lo_z, inv_s;            // grid origin (x and y, z) and 1 / cell side (lambda)
   int T, ipt, nT, nslots, nwords;   // tile, targets per lane, tiles, nT*T slots, bitmap words
   int32_t *cell_of, *count, *fill, *start;  // [N], [ncells], [ncells], [ncells + 1]
   int32_t* perm;                    // [nslots] ion of each sorted slot, -1 for sentinels
@@ -118,8 +122,11 @@ struct od_cutn3 {
   unsigned long long* acc;          // [3][nslots] fixed-point ion–ion sums per sorted slot
   int grid;                         // persistent blocks of the pair kernel
 };
-size_t od_cutn3_bytes(int N, int T, int G);
-int od_cutn3_grid(int N);           // cells per axis for N ions
+// cell grid of the tile-pair cutoff for N ions in a cylinder of radius R and height H (any
+// unit): nb cubes of side `side` (that unit) along z, G^3 cells each
+struct od_cgrid { int G, nb, ncells; double side; };
+od_cgrid od_cutn3_grid(int N, double R, double H);
+size_t od_cutn3_bytes(int N, int T, int ncells);
 bool od_cutn3_supported(int ipt, int T);
 cudaError_t od_cutn3_prepare(int ipt, int T);
 cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
@@ -157,7 +164,7 @@ cudaError_t od_launch_pairs(const od_pair_plan& pl, const od_pair_io& io, int Np
 cudaError_t od_launch_pairs_probe(const od_pair_plan& pl, const od_pair_io& io, int Npad,
                                   int gridx_limit, float4* part_hi, float4* part_lo, float rho0,
                                   uint32_t* err, cudaStream_t s);
-cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* pos, float4* vel,
+cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* rel, float4* pos, float4* vel,
                                  const float* vz_v, const double* vz_cdf, int vz_n, uint32_t* err,
                                  cudaStream_t s);
 cudaError_t od_launch_aos_to_soa(const float4* pos, int Npad, float* sx, float* sy, float* sz,

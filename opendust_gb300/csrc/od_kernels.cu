@@ -465,25 +465,31 @@ __device__ __forceinline__ void collide(const od_dparams& p, uint32_t ion, uint3
   }
 }
 
+// The drift moves the cell-relative state (rel) and writes the absolute FP32 position derived
+// from it to pos and to the SoA copy.
 __device__ __forceinline__ void kick_drift_body(const od_dparams& p, const od_dstate* __restrict__ ds,
-                                                float4* __restrict__ pos, float4* __restrict__ vel,
+                                                float4* __restrict__ rel, float4* __restrict__ pos,
+                                                float4* __restrict__ vel,
                                                 const float4* __restrict__ fhi,
                                                 const float4* __restrict__ flo,
                                                 const float* __restrict__ cq,
                                                 float* __restrict__ sx, float* __restrict__ sy,
                                                 float* __restrict__ sz, int i) {
   if (i >= p.N) return;
-  float4 x = pos[i], v = vel[i];
+  float4 r = rel[i], v = vel[i];
   if (p.coll != OD_COLL_NONE)
     collide(p, (uint32_t)(p.ion0 + i), (uint32_t)(ds->step + ds->rng_base), v);
   const float4 gh = fhi[i], gl = flo[i];
-  float3 a = od_ext_accel(p, cq, x.x, x.y, x.z);
+  const float4 x0 = od_rel_abs(p, r);
+  float3 a = od_ext_accel(p, cq, x0.x, x0.y, x0.z);
   const float aii = p.A_ii * od_first_kick_weight(p.force_every, ds->step);
   a.x = fmaf(aii, gh.x + gl.x, a.x);
   a.y = fmaf(aii, gh.y + gl.y, a.y);
   a.z = fmaf(aii, gh.z + gl.z, a.z);
   v.x = fmaf(0.5f, a.x, v.x); v.y = fmaf(0.5f, a.y, v.y); v.z = fmaf(0.5f, a.z, v.z);
-  x.x += v.x; x.y += v.y; x.z += v.z;
+  od_rel_drift(p, r, v.x, v.y, v.z);
+  const float4 x = od_rel_abs(p, r);
+  rel[i] = r;
   pos[i] = x;
   vel[i] = v;
   sx[i] = x.x; sy[i] = x.y; sz[i] = x.z;
@@ -491,6 +497,7 @@ __device__ __forceinline__ void kick_drift_body(const od_dparams& p, const od_ds
 
 __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restrict__ dp,
                                                      const od_dstate* __restrict__ ds,
+                                                     float4* __restrict__ rel,
                                                      float4* __restrict__ pos,
                                                      float4* __restrict__ vel,
                                                      const float4* __restrict__ fhi,
@@ -498,7 +505,8 @@ __global__ void __launch_bounds__(kBlk) k_kick_drift(const od_dparams* __restric
                                                      const float* __restrict__ cq,
                                                      float* __restrict__ sx, float* __restrict__ sy,
                                                      float* __restrict__ sz) {
-  kick_drift_body(*dp, ds, pos, vel, fhi, flo, cq, sx, sy, sz, blockIdx.x * blockDim.x + threadIdx.x);
+  kick_drift_body(*dp, ds, rel, pos, vel, fhi, flo, cq, sx, sy, sz,
+                  blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ============================================================== K3: kick + flags
@@ -714,8 +722,9 @@ __device__ __forceinline__ void list_sums(const od_dparams& p, od_dstate* __rest
 }
 
 __device__ __forceinline__ void collect_inject_body(
-    const od_dparams& p, od_dstate* __restrict__ ds, float4* __restrict__ pos,
-    float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
+    const od_dparams& p, od_dstate* __restrict__ ds, float4* __restrict__ rel,
+    float4* __restrict__ pos, float4* __restrict__ vel, const uint32_t* __restrict__ flags,
+    int32_t* __restrict__ list,
     int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
     float4* __restrict__ list_new, float4* __restrict__ list_v) {
   const int tid = threadIdx.x;
@@ -741,7 +750,12 @@ __device__ __forceinline__ void collect_inject_body(
       const int bits = list_bits[k];
       const float4 xo = list_old[k];
       float4 x = xo, v = list_v[k];
-      if (bits & (grains | (1 << 29))) inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
+      if (bits & (grains | (1 << 29))) {
+        inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
+        const float4 r = od_rel_encode(p, x.x, x.y, x.z);
+        x = od_rel_abs(p, r);
+        rel[i] = r;
+      }
       if (bits & (1 << 30)) {
         const float rr = sqrtf(fmaf(xo.x, xo.x, xo.y * xo.y));
         const float nx = xo.x / rr, ny = xo.y / rr;
@@ -760,6 +774,9 @@ __device__ __forceinline__ void collect_inject_body(
     const int i = list[k];
     float4 x, v;
     inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
+    const float4 r = od_rel_encode(p, x.x, x.y, x.z);
+    x = od_rel_abs(p, r);
+    rel[i] = r;
     pos[i] = x;
     vel[i] = v;
     list_new[k] = x;
@@ -767,13 +784,13 @@ __device__ __forceinline__ void collect_inject_body(
 }
 
 __global__ void __launch_bounds__(kCT) k_collect_inject(
-    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ pos,
-    float4* __restrict__ vel, const uint32_t* __restrict__ flags, int32_t* __restrict__ list,
-    int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
+    const od_dparams* __restrict__ dp, od_dstate* __restrict__ ds, float4* __restrict__ rel,
+    float4* __restrict__ pos, float4* __restrict__ vel, const uint32_t* __restrict__ flags,
+    int32_t* __restrict__ list, int32_t* __restrict__ list_bits, float4* __restrict__ list_old,
     float4* __restrict__ list_new, float4* __restrict__ list_v) {
   od_pdl_wait();
   od_pdl_trigger();
-  collect_inject_body(*dp, ds, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
+  collect_inject_body(*dp, ds, rel, pos, vel, flags, list, list_bits, list_old, list_new, list_v);
 }
 
 // list + per-grain counts of a snapshot (no state change)
@@ -1132,6 +1149,7 @@ __global__ void __launch_bounds__(kBlk) k_trap(double Rh, double Hh, int n_r, in
 // opendust.py:373-451: rejection sampling of uniform positions in the cylinder outside every
 // grain, Maxwellian (or tabulated field-driven v_z) velocities; Philox streams INIT_X / INIT_V.
 __global__ void __launch_bounds__(kBlk) k_init_state(const od_dparams* __restrict__ dp,
+                                                     float4* __restrict__ rel,
                                                      float4* __restrict__ pos,
                                                      float4* __restrict__ vel,
                                                      const float* __restrict__ vz_v,
@@ -1170,16 +1188,18 @@ __global__ void __launch_bounds__(kBlk) k_init_state(const od_dparams* __restric
   } else {
     vz = fmaf(p.vT, gz, p.vfl);
   }
-  pos[i] = x;
+  const float4 r = od_rel_encode(p, x.x, x.y, x.z);
+  rel[i] = r;
+  pos[i] = od_rel_abs(p, r);
   vel[i] = make_float4(p.vT * gx, p.vT * gy, vz, 0.f);
 }
 
 }  // namespace
 
-cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* pos, float4* vel,
-                                 const float* vz_v, const double* vz_cdf, int vz_n, uint32_t* err,
-                                 cudaStream_t s) {
-  k_init_state<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, pos, vel, vz_v, vz_cdf, vz_n, err);
+cudaError_t od_launch_init_state(const od_dparams* dp, int N, float4* rel, float4* pos,
+                                 float4* vel, const float* vz_v, const double* vz_cdf, int vz_n,
+                                 uint32_t* err, cudaStream_t s) {
+  k_init_state<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, rel, pos, vel, vz_v, vz_cdf, vz_n, err);
   return cudaGetLastError();
 }
 
@@ -1297,7 +1317,7 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
   (void)P;
   const int nb = Npad / kBlk;
   if (part == 0) {
-    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq,
+    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.rel, b.pos, b.vel, b.fhi, b.flo, b.cq,
                                                         b.sx, b.sy, b.sz);
     return cudaGetLastError();
   }
@@ -1312,7 +1332,7 @@ cudaError_t od_launch_step_part(int part, const od_dparams* dp, od_dstate* ds, c
                                 (const float4*)b.part_hi, (const float4*)b.part_lo, jsplit, b.fhi,
                                 b.flo, b.flags, (const float*)b.cq, fc.acc);
   if (e == cudaSuccess)
-    e = od_launch_pdl(k_collect_inject, dim3(1), dim3(kCT), s, dp, ds, b.pos, b.vel,
+    e = od_launch_pdl(k_collect_inject, dim3(1), dim3(kCT), s, dp, ds, b.rel, b.pos, b.vel,
                       (const uint32_t*)b.flags, b.list, b.list_bits, b.list_old, b.list_new,
                       b.list_v);
   if (e == cudaSuccess)
@@ -1463,7 +1483,7 @@ __global__ void __launch_bounds__(kBlk) k_b_kick_drift(const od_simdesc* __restr
                                                        const int2* __restrict__ blk) {
   const int2 e = blk[blockIdx.x];
   const od_simdesc& d = sims[e.x];
-  kick_drift_body(*d.dp, d.ds, d.b.pos, d.b.vel, d.b.fhi, d.b.flo, d.b.cq, d.b.sx, d.b.sy, d.b.sz,
+  kick_drift_body(*d.dp, d.ds, d.b.rel, d.b.pos, d.b.vel, d.b.fhi, d.b.flo, d.b.cq, d.b.sx, d.b.sy, d.b.sz,
                   e.y * kBlk + threadIdx.x);
 }
 
@@ -1498,7 +1518,7 @@ __global__ void __launch_bounds__(kBlk) k_b_kick_flag(const od_simdesc* __restri
 
 __global__ void __launch_bounds__(kCT) k_b_collect_inject(const od_simdesc* __restrict__ sims) {
   const od_simdesc& d = sims[blockIdx.x];
-  collect_inject_body(*d.dp, d.ds, d.b.pos, d.b.vel, d.b.flags, d.b.list, d.b.list_bits,
+  collect_inject_body(*d.dp, d.ds, d.b.rel, d.b.pos, d.b.vel, d.b.flags, d.b.list, d.b.list_bits,
                       d.b.list_old, d.b.list_new, d.b.list_v);
 }
 
@@ -1681,13 +1701,13 @@ cudaError_t od_launch_shard_part(int part, const od_dparams* dp, od_dstate* ds, 
                                  int N, int Npad, int jsplit, float* sx, float* sy, float* sz,
                                  cudaStream_t s) {
   if (part == 0) {
-    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.fhi, b.flo, b.cq,
+    k_kick_drift<<<(N + kBlk - 1) / kBlk, kBlk, 0, s>>>(dp, ds, b.rel, b.pos, b.vel, b.fhi, b.flo, b.cq,
                                                         sx, sy, sz);
     return cudaGetLastError();
   }
   k_kick_flag<<<Npad / kBlk, kBlk, 0, s>>>(dp, ds, b.pos, b.vel, b.part_hi, b.part_lo, jsplit,
                                           b.fhi, b.flo, b.flags, b.cq, b.n3);
-  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.pos, b.vel, b.flags, b.list, b.list_bits,
+  k_collect_inject<<<1, kCT, 0, s>>>(dp, ds, b.rel, b.pos, b.vel, b.flags, b.list, b.list_bits,
                                      b.list_old, b.list_new, b.list_v);
   return cudaGetLastError();
 }

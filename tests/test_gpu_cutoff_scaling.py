@@ -49,7 +49,7 @@ def test_reference_cutoff_config_snapshot(gpu_lib, k):
 
 def test_reference_cutoff_script_three_steps(gpu_lib):
     spatial = pytest.importorskip("scipy.spatial")
-    holder, pos, vel, plasma, sim = _scaling_case(1, 41)
+    holder, pos, vel, plasma, sim = _scaling_case(1, 41, n=4)  # 3 steps + 1 counted step
     lam = plasma.r_D_e
     with _lib.Engine(holder) as eng:
         eng.set_state(pos, vel)
