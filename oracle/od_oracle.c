@@ -607,12 +607,32 @@ int odo_max_threads(void) {
 #endif
 }
 
-/* positions [m] -> lambda units; round32 != 0 rounds each to float as the device does */
+/* The device's cell-relative position state (od_set_state): per axis a cell index c on a grid
+ * of side s (the smallest power of two not below 1/256 of max(R, H/2) in lambda) and the
+ * offset v - c s rounded once to float; the state is c s + offset exactly. */
+static double rel_side(const odo_par* p) {
+  return ldexp(1.0, (int)ceil(log2(fmax(p->Rh, p->Hh / 2.0) / 256.0)));
+}
+static double rel_state(double v, double s) {
+  double c = floor(v / s);
+  c = c < -512.0 ? -512.0 : (c > 511.0 ? 511.0 : c);
+  float o = (float)(v - c * s);
+  if (o == (float)s && c < 511.0) { c += 1.0; o = 0.f; }
+  return c * s + (double)o;
+}
+
+/* positions [m] -> lambda units. round32: 0 as given; 1 rounded to float (the snapshot calls'
+ * representation); 2 the absolute float positions the device derives from its cell-relative
+ * state (what its kernels read after od_set_state); 3 that state itself, exactly. */
+static double hat(double v, int round32, double s) {
+  if (round32 == 1) return (double)(float)v;
+  if (round32 == 2) return (double)(float)rel_state(v, s);
+  if (round32 == 3) return rel_state(v, s);
+  return v;
+}
 static void to_hat(const odo_par* p, const double* pos, int64_t n, int round32, double* xh) {
-  for (int64_t i = 0; i < 3 * n; i++) {
-    double v = pos[i] / p->lam;
-    xh[i] = round32 ? (double)(float)v : v;
-  }
+  const double s = rel_side(p);
+  for (int64_t i = 0; i < 3 * n; i++) xh[i] = hat(pos[i] / p->lam, round32, s);
 }
 
 /* ion–ion force [N] on each ion (the CustomNonbondedForce of opendust.py:471-485 alone) */
@@ -635,8 +655,9 @@ int odo_collect_flags(const od_config* c, const double* pos, int64_t n, int roun
   int64_t cnt = 0;
   for (int g = 0; g < p->P; g++) grain_counts[g] = 0;
   for (int64_t i = 0; i < n; i++) {
-    double x = pos[3 * i] / p->lam, y = pos[3 * i + 1] / p->lam, z = pos[3 * i + 2] / p->lam;
-    if (round32) { x = (float)x; y = (float)y; z = (float)z; }
+    const double s = rel_side(p);
+    double x = hat(pos[3 * i] / p->lam, round32, s), y = hat(pos[3 * i + 1] / p->lam, round32, s),
+           z = hat(pos[3 * i + 2] / p->lam, round32, s);
     int b = flag_bits(p, x, y, z);
     if (b) {
       if (cnt < cap) idx[cnt] = i;
@@ -696,7 +717,8 @@ int odo_inject(const od_config* c, int64_t ion, int64_t step, double* x, double*
  * pos [m] / vel [m/s] (n x 3) are updated in place; q_param[P] holds the charges the forces
  * use (q at the previous step) and is updated; per-step outputs (row i = step first_step+i):
  * q_out[P], f_orbit/f_collect/f_dust/f_field[P*3], n_inj (ions re-injected), dN[P].
- * round32 != 0 rounds the initial state to float first (the device representation).
+ * round32: 1 rounds the initial positions and velocities to float; 2 takes the device's
+ * cell-relative position state (to_hat mode 3) and float velocities.
  * rng_base: Philox step counter of step 0, for later windows whose random streams continue. */
 int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32,
             int64_t first_step, int64_t nsteps, int64_t rng_base, double* q_param, double* q_out,
@@ -709,7 +731,7 @@ int odo_run(const od_config* c, double* pos, double* vel, int64_t n, int round32
   double* v = (double*)malloc(sizeof(double) * 3 * n);
   double* a = (double*)malloc(sizeof(double) * 3 * n);
   int* fl = (int*)malloc(sizeof(int) * n);
-  to_hat(p, pos, n, round32, x);
+  to_hat(p, pos, n, round32 == 2 ? 3 : round32, x);
   for (int64_t i = 0; i < 3 * n; i++) {
     double vv = vel[i] / p->vunit;
     v[i] = round32 ? (double)(float)vv : vv;

@@ -85,6 +85,12 @@ def philox(ctr, key):
     return [int(x) for x in o]
 
 
+# round32 values: True rounds positions to float (what the snapshot calls consume);
+# DEVICE_STATE takes the device's cell-relative position state of od_set_state (od_run: the state
+# exactly; the snapshot functions: the absolute float positions the device derives from it)
+DEVICE_STATE = 2
+
+
 def force_snapshot(holder, pos, round32=True):
     pos = np.ascontiguousarray(pos, dtype=np.float64)
     f = np.empty_like(pos)

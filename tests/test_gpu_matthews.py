@@ -55,7 +55,8 @@ def plant(pos, vel, plasma, sim):
 def test_ion_potential_grid(gpu_lib):
     holder, plasma, sim, grains, pos, vel, tab = fork(4096, 4, table=False)
     grid_R, grid_H = sh.matthews_trap_grid(sim.R, sim.H, plasma.r_D_e)
-    ref = oracle.ion_potential_grid(holder, pos, grid_R, grid_H, round32=True)
+    # the device sums over the absolute float positions derived from its cell-relative state
+    ref = oracle.ion_potential_grid(holder, pos, grid_R, grid_H, round32=oracle.DEVICE_STATE)
     with _lib.Engine(holder) as eng:
         eng.set_state(pos, vel)
         got = eng.ion_potential_grid(grid_R, grid_H)
