@@ -60,6 +60,9 @@ def parse():
                              "serve"])
     ap.add_argument("--scale", type=int, default=8,
                     help="cutoff_scaling: k in N = k*2^15 ions, H = k*6 lambda")
+    ap.add_argument("--hard-cutoff", action="store_true",
+                    help="cutoff workloads: no switching polynomial (pairs at r_c decided in FP64 "
+                         "as the oracle decides them)")
     ap.add_argument("--sweep-sims", type=int, default=64)
     ap.add_argument("--sweep-exact", action="store_true")
     ap.add_argument("--pilot-steps", type=int, default=100)
@@ -152,16 +155,22 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def workload(name: str, n_total: int, scale: int = 8):
+def workload(name: str, n_total: int, scale: int = 8, hard: bool = False):
     from opendust_gb300 import workloads
 
     if name == "cutoff_scaling":
-        return workloads.cutoff_scaling(k=scale, n=n_total)
-    if name == "full_plain":
-        return workloads.full_plain(n=n_total)
-    if name == "field_chain":
-        return workloads.field_chain(n=n_total)
-    return workloads.small_plain(n=n_total)
+        w = workloads.cutoff_scaling(k=scale, n=n_total)
+    elif name == "full_plain":
+        w = workloads.full_plain(n=n_total)
+    elif name == "field_chain":
+        w = workloads.field_chain(n=n_total)
+    else:
+        w = workloads.small_plain(n=n_total)
+    if hard:
+        if name not in ("cutoff_scaling", "field_chain"):
+            raise SystemExit("--hard-cutoff applies to the cutoff workloads")
+        w[4]["switch_distance"] = 0.0
+    return w
 
 
 def describe(name, sim, ext):
@@ -179,8 +188,13 @@ def describe(name, sim, ext):
              f"R=3 lambda, H={6 * k} lambda, N={k}*2^15, cutoff 3.2 lambda with switching from "
              "3.0 lambda, one grain of given charge, d_t=3.5148e-9 s")
     cut = "cutoff_distance" in ext or ext.get("cutOff", False)
+    force = "all-pairs"
+    if cut:
+        force = "cutoff (Hilbert-sorted tile pairs), " + (
+            "hard: no switching, pairs within FP32 rounding of r_c decided in FP64"
+            if ext.get("switch_distance") == 0.0 else "OpenMM switching from 15/16 of r_c")
     return {"workload": f"{name}: {w}", "n_ions": int(sim.N), "grains": len(sim_grains(name)),
-            "force": "cutoff (Hilbert-sorted tile pairs)" if cut else "all-pairs",
+            "force": force,
             "collisions": ext.get("collisions", "none"),
             "l2": "flushed (512 MB write) before every timed step",
             "steps_in_workload": {"full_plain": 20000, "small_plain": 2000, "field_chain": 30000,
@@ -220,7 +234,7 @@ def run_reference(args, dist: Dist):
     from opendust_gb300 import build_simulation, setup_host
     from oracle import oracle
 
-    plasma, sim, grains, d, ext = workload(args.workload, 10, args.scale)
+    plasma, sim, grains, d, ext = workload(args.workload, 10, args.scale, args.hard_cutoff)
     holder, _ = build_simulation(plasma, sim, grains, d, seed=1, trap=np.zeros(15), **ext)
     pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],
                                         plasma.v_fl, plasma.v_T, d, 1)
@@ -278,7 +292,7 @@ def run_ours(args, dist: Dist):
     K, W = args.steps, args.warmup
     K_e2e = max(2, K)
     n_total = W + K + K_e2e + 5
-    plasma, sim, grains, d, ext = workload(args.workload, n_total, args.scale)
+    plasma, sim, grains, d, ext = workload(args.workload, n_total, args.scale, args.hard_cutoff)
     seed = 1000 + dist.rank
     holder, _ = build_simulation(plasma, sim, grains, d, seed=seed, device=device, **ext)
     pos, vel = setup_host.initial_state(sim.N, sim.R, sim.H, [(g.x, g.y, g.z, g.r) for g in grains],

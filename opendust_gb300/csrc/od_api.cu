@@ -1033,6 +1033,7 @@ static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   L->lo_z = (float)(-g.side * g.nb / 2.0);
   L->inv_s = (float)(G / g.side);
   L->T = T; L->ipt = ipt;
+  L->rc_d = h->cfg.cutoff / h->cfg.r_D_e;
   L->nT = (N + T - 1) / T;
   L->nslots = L->nT * T;
   L->nwords = (L->nT + 31) / 32;

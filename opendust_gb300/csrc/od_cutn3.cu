@@ -585,7 +585,7 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
   // group pairs whose farthest box distance is below the switching radius (hard cutoff: the
   // cutoff), with a relative margin of 1e-5 against rounding, skip the switching polynomial
   const float rin = (sw ? rs : rc) * (1.0f - 1e-5f);
-  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f, rin * rin};
+  const n3_cut cut{rho0, rc * rc, rs, sw ? 1.0f / (rc - rs) : 0.0f, rin * rin, L.rc_d};
   const int32_t* np = L.rowptr + L.nT;
 #define OD_CUTN3(MT, MS, BAL, SM)                                                             \
   do {                                                                                        \

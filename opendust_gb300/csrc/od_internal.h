@@ -120,6 +120,7 @@ struct od_cutn3 {
   int32_t* rowptr;                  // [nT + 1] pair counts, then their exclusive prefix
   int2* pairs;                      // [nT (nT + 1) / 2] listed pairs, row-major
   unsigned long long* acc;          // [3][nslots] fixed-point ion–ion sums per sorted slot
+  double rc_d;                      // cutoff / r_D_e in FP64 (the hard cutoff's exact test)
   int grid;                         // persistent blocks of the pair kernel
 };
 // cell grid of the tile-pair cutoff for N ions in a cylinder of radius R and height H (any

@@ -16,10 +16,13 @@ struct n3_consts {
   od_u64 eps, rho, nl2e, one, three, six, invw, nrsw, p30w;
   float rc2;
   float skip2;  // cutoff forms: a pack whose pairs all lie beyond sqrt(skip2) contributes 0
+  float band_lo, band_hi;  // hard cutoff: r^2 in FP32 within rounding of r_c^2
+  double rcd;              // hard cutoff: r_c in FP64, as the reference decides it
 };
 struct n3_cut {
   float rho0, rc2, rs, inv_w;
   float in2;  // cutoff tile pairs: group pairs closer than sqrt(in2) take the CUT = 0 term
+  double rcd;  // hard cutoff: r_c (lambda) in FP64
 };
 
 __device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
@@ -35,7 +38,22 @@ __device__ __forceinline__ n3_consts make_consts(const n3_cut& c) {
   // (1 + 2e-5) rc^2: beyond it the clamped switching variable is 1 in FP32, so S = 0 and the
   // switched term is exactly zero (the hard cutoff is exactly zero from rc^2 on)
   k.skip2 = c.rc2 * 1.00002f;
+  // the FP32 r^2 of a pair is within 4e-7 of its exact value on the same float positions
+  k.band_lo = c.rc2 * (1.f - 2e-6f);
+  k.band_hi = c.rc2 * (1.f + 2e-6f);
+  k.rcd = c.rcd;
   return k;
+}
+
+// Is the pair of float positions t, s inside the cutoff as the FP64 reference decides it:
+// sqrt((dx^2 + dy^2) + dz^2) < r_c with the differences taken exactly in FP64 and every
+// operation rounded once (the oracle's pair_factor).
+__device__ __noinline__ bool n3_inside_exact(float tx, float ty, float tz, float sx, float sy,
+                                             float sz, double rcd) {
+  const double dx = __dsub_rn((double)tx, (double)sx), dy = __dsub_rn((double)ty, (double)sy),
+               dz = __dsub_rn((double)tz, (double)sz);
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  return __dsqrt_rn(r2) < rcd;
 }
 
 // two pair terms (target X,Y,Z broadcast in both halves; sources packed in QX,QY,QZ); COUNT
@@ -76,9 +94,20 @@ __device__ __forceinline__ void n3_pair(const n3_consts& k, od_u64 X, od_u64 Y, 
     C = mul2(mul2(EX, RI), mul2(SI, U));
   } else {
     const float2 c = up2(mul2(mul2(EX, RI), fma2(SI, SI, SI)));
-    C = p2(r2.x < k.rc2 ? c.x : 0.f, r2.y < k.rc2 ? c.y : 0.f);
+    bool ix = r2.x < k.rc2, iy = r2.y < k.rc2;
+    // a pair within FP32 rounding of r_c is decided exactly as the FP64 reference decides it,
+    // so that both include the same pairs (rare: a warp-uniform branch)
+    const bool nx = r2.x > k.band_lo && r2.x < k.band_hi, ny = r2.y > k.band_lo && r2.y < k.band_hi;
+    if (__any_sync(0xffffffffu, nx || ny)) {
+      const float2 tx = up2(X), ty = up2(Y), tz = up2(Z), sx = up2(QX), sy = up2(QY), sz = up2(QZ);
+      if (nx) ix = n3_inside_exact(tx.x, ty.x, tz.x, sx.x, sy.x, sz.x, k.rcd);
+      if (ny) iy = n3_inside_exact(tx.y, ty.y, tz.y, sx.y, sy.y, sz.y, k.rcd);
+    }
+    C = p2(ix ? c.x : 0.f, iy ? c.y : 0.f);
+    if (COUNT)
+      cnt += (REACT ? 2u : 1u) * ((unsigned)(ix && r2.x > 1e-29f) + (unsigned)(iy && r2.y > 1e-29f));
   }
-  if (COUNT)
+  if (COUNT && CUT != 2)
     cnt += (REACT ? 2u : 1u) * ((unsigned)(r2.x < k.rc2 && r2.x > 1e-29f) +
                                 (unsigned)(r2.y < k.rc2 && r2.y > 1e-29f));
   AX = fma2(C, DX, AX); AY = fma2(C, DY, AY); AZ = fma2(C, DZ, AZ);
