@@ -1037,7 +1037,8 @@ static od_status alloc_cutn3(od_handle* h, int ipt, int T) {
   L->nT = (N + T - 1) / T;
   L->nslots = L->nT * T;
   L->nwords = (L->nT + 31) / 32;
-  L->grid = od_num_sms(h->device) * 3;
+  L->grid = od_num_sms(h->device) * od_cutn3_blocks_per_sm(ipt, T, false);
+  L->grid_hard = od_num_sms(h->device) * od_cutn3_blocks_per_sm(ipt, T, true);
   const size_t nT = L->nT, ns = L->nslots, nc = L->ncells;
   auto al = [&](auto** p, size_t n) {
     return cudaMalloc((void**)p, sizeof(**p) * std::max<size_t>(n, 1));

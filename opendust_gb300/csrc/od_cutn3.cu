@@ -216,33 +216,21 @@ __global__ void k_tile_list(int nT, int nwords, const uint32_t* __restrict__ adj
 // group pairs whose boxes come within the cutoff form a list in (target group, source group)
 // order, and warp w takes the contiguous slice [w·n/8, (w+1)·n/8) of it, so that the warps
 // evaluate the same number of group pairs (± 1) whatever the culling left and no barrier
-// separates them. A warp keeps one target group while consecutive items share it and sums its
-// targets into a segment slot of its own (a new segment at every change of target group and
-// at every slice start: at most NBT + 7); every item stores its FP32 reaction sums in a slot of
-// its own. The block then sums the slots of each ion in a fixed order — target segments in list
-// order, then reactions in target-group order — so the result does not depend on which warp
-// ran what, or when. A group pair whose farthest box distance is below the switching radius
-// (hard cutoff: the cutoff) is marked inner and takes the plain screened term: the switching
-// factor is exactly 1 for all its pairs.
+// separates them. Every listed group pair adds its FP32 target and reaction sums, converted to
+// 64-bit fixed point (od_fix), into per-ion words in shared memory with integer atomics, so
+// the block's sums do not depend on which warp ran what, or when; the block then adds each
+// ion's words to its global accumulators. A group pair whose farthest box distance is below the
+// switching radius (hard cutoff: the cutoff) is marked inner and takes the plain screened term:
+// the switching factor is exactly 1 for all its pairs.
 template <int MT, int MS>
 struct cut_traits {
   static constexpr int GT = 32 * MT, GS = 32 * MS;    // target and source group sizes
   static constexpr int T = 512;                       // ions per tile
   static constexpr int NBT = T / GT, NBS = T / GS;    // groups per tile
   static constexpr int NI = NBT * NBS;                // group pairs per tile pair (<= 64)
-  static constexpr int NSEG = NBT + kWarps;           // target segments
-  static constexpr bool HS = MT > 2;                  // target sums kept in the segment slot
-  static constexpr size_t RFL = (size_t)NI * 3 * GS;  // reaction slots (floats)
-  static constexpr size_t TFL = (size_t)NSEG * 6 * GT;  // two-float target segment slots
-  static constexpr size_t SMEM = sizeof(float) * (RFL + TFL) + 256;  // + list metadata
+  // [3][T] fixed-point words of tile a's ions and [3][T] of tile b's, then the list
+  static constexpr size_t SMEM = sizeof(unsigned long long) * 6 * T + 256;
 };
-
-// warp that owns list entry i of n
-__device__ __forceinline__ int cut_owner(int i, int n) {
-  int w = 0;
-  while (w < kWarps - 1 && (((w + 1) * n) >> 3) <= i) w++;
-  return w;
-}
 
 // group pair (ga, gb) of a diagonal tile: 2 each pair once, 1 directed (the sources lie in the
 // target group), 0 skipped (counted from the other side)
@@ -256,27 +244,24 @@ constexpr int kItem = 63, kInner = 128;  // list entry: group pair index | inner
 
 template <int MT, int MS, int CUT, bool COUNT>
 __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ sx,
-                                                      const float* __restrict__ sy,
-                                                      const float* __restrict__ sz,
-                                                      unsigned long long* __restrict__ acc,
-                                                      size_t stride,
-                                                      const n3_consts& k, int a, int b, float* sm,
-                                                      const float* __restrict__ gbox,
-                                                      float cull2, float k_in2) {
+                                                         const float* __restrict__ sy,
+                                                         const float* __restrict__ sz,
+                                                         unsigned long long* __restrict__ acc,
+                                                         size_t stride, const n3_consts& k, int a,
+                                                         int b, float* sm,
+                                                         const float* __restrict__ gbox,
+                                                         float cull2, float k_in2) {
   using CT = cut_traits<MT, MS>;
   constexpr int GT = CT::GT, GS = CT::GS, T = CT::T, NBT = CT::NBT, NBS = CT::NBS, NI = CT::NI;
   constexpr int MS2 = MS / 2;
-  constexpr bool HS = CT::HS;
-  static_assert(NI % 32 == 0 && NI <= 64 && NBT <= 8, "list of at most 64 group pairs");
-  float* const R = sm;              // [NI][3][GS] reaction sums of each listed group pair
-  float* const Tg = sm + CT::RFL;   // [NSEG][6][GT] two-float target sums of each segment
-  unsigned char* const items = reinterpret_cast<unsigned char*>(Tg + CT::TFL);  // ga·NBS + gb
-  unsigned char* const segid = items + 64;                                       // per entry
-  signed char* const item_of = reinterpret_cast<signed char*>(items + 128);      // by ga·NBS+gb
-  signed char* const gs0 = item_of + 64;  // first and last segment of each target group
-  signed char* const gs1 = gs0 + 8;
-  int* const s_n = reinterpret_cast<int*>(items + 208);
+  static_assert(NI % 32 == 0 && NI <= 64, "list of at most 64 group pairs");
+  // [3][T] fixed-point sums of tile a's ions, then [3][T] of tile b's (unused when a == b)
+  unsigned long long* const fa = reinterpret_cast<unsigned long long*>(sm);
+  unsigned long long* const fb = fa + 3 * T;
+  unsigned char* const items = reinterpret_cast<unsigned char*>(fb + 3 * T);  // ga·NBS + gb
+  int* const s_n = reinterpret_cast<int*>(items + 64);
   const bool diag = a == b;
+  unsigned long long* const fs = diag ? fa : fb;  // where the reactions go
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31, src = (lane + 1) & 31;
 
   // 1. the list (warp 0): group pairs within range; on a diagonal tile the source groups
@@ -291,7 +276,7 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
         float ta[6], tb[6];
         group_box(gbox, (a * NBT + ga) * (GT / 64), GT / 64, ta);
         group_box(gbox, (b * NBS + gb) * (GS / 64), GS / 64, tb);
-        float d2 = 0.f, f2 = 0.f;  // nearest and farthest box distances, squared
+        float d2 = 0.f, f2 = 0.f;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
           const float gap = fmaxf(fmaxf(tb[d] - ta[3 + d], ta[d] - tb[3 + d]), 0.f);
@@ -300,68 +285,31 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
           f2 = fmaf(far, far, f2);
         }
         if (mode == 2) keep = d2 < cull2;
-        // every pair of the two groups closer than the switching radius (hard cutoff: the
-        // cutoff): the switching factor is exactly 1 there, so the plain term applies
         inner = f2 < k_in2;
       }
       const unsigned int bal = __ballot_sync(0xffffffffu, keep);
       const int pos = n + __popc(bal & ((1u << lane) - 1u));
       if (keep) items[pos] = (unsigned char)(c | (inner ? kInner : 0));
-      item_of[c] = keep ? (signed char)pos : (signed char)-1;
       n += __popc(bal);
-    }
-    __syncwarp();
-    // a segment starts at every change of target group and at the start of every slice
-    int nseg = 0;
-    for (int r = 0; r < 2; r++) {
-      const int i = r * 32 + lane;
-      bool f = false;
-      if (i < n)
-        f = i == 0 || (items[i - 1] & kItem) / NBS != (items[i] & kItem) / NBS ||
-            cut_owner(i - 1, n) != cut_owner(i, n);
-      const unsigned int bal = __ballot_sync(0xffffffffu, f);
-      if (i < n) segid[i] = (unsigned char)(nseg + __popc(bal & ((2u << lane) - 1u)) - 1);
-      nseg += __popc(bal);
-    }
-    if (lane < 8) { gs0[lane] = 0; gs1[lane] = -1; }
-    __syncwarp();
-    for (int r = 0; r < 2; r++) {
-      const int i = r * 32 + lane;
-      if (i < n) {
-        const int ga = (items[i] & kItem) / NBS;
-        if (i == 0 || (items[i - 1] & kItem) / NBS != ga) gs0[ga] = (signed char)segid[i];
-        if (i == n - 1 || (items[i + 1] & kItem) / NBS != ga) gs1[ga] = (signed char)segid[i];
-      }
     }
     if (lane == 0) *s_n = n;
   }
   __syncthreads();
 
-  // 2. this warp's slice of the list
+  // 2. this warp's slice of the list; sums into the shared fixed-point words
   const int n = *s_n, i0 = (w * n) >> 3, i1 = ((w + 1) * n) >> 3;
   unsigned int cnt = 0;
   od_u64 X[MT], Y[MT], Z[MT];
-  float hreg[HS ? 1 : 6 * MT];
-  float* hs = Tg + lane;  // HS: this warp's current segment slot (lane-private words)
-#define CUT_H(c, kt) (HS ? hs[(c) * GT + 32 * (kt)] : hreg[(c) * MT + (kt)])
   int cur = -1;
   for (int i = i0; i < i1; i++) {
     const int c = items[i] & kItem, ga = c / NBS, gb = c % NBS;
     const bool inner = (items[i] & kInner) != 0;
     if (ga != cur) {
-      if (!HS && cur >= 0) {
-        float* t = Tg + (size_t)segid[i - 1] * 6 * GT + lane;
-#pragma unroll
-        for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
-      }
-      if (HS) hs = Tg + (size_t)segid[i] * 6 * GT + lane;
 #pragma unroll
       for (int kt = 0; kt < MT; kt++) {
         const int j = (a * NBT + ga) * GT + lane + 32 * kt;
         const float x = sx[j], y = sy[j], z = sz[j];
         X[kt] = p2(x, x); Y[kt] = p2(y, y); Z[kt] = p2(z, z);
-#pragma unroll
-        for (int q = 0; q < 6; q++) CUT_H(q, kt) = 0.f;
       }
       cur = ga;
     }
@@ -376,7 +324,8 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
     }
 #pragma unroll
     for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
-    if (diag && cut_diag_mode<GT, GS>(ga, gb) == 1) {
+    const bool react = !(diag && cut_diag_mode<GT, GS>(ga, gb) == 1);
+    if (!react) {
       if (inner)
         n3_group<MT, MS, 0, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
                                           cnt);
@@ -391,63 +340,43 @@ __device__ __forceinline__ unsigned int cut_tile_pair(const float* __restrict__ 
         n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
                                            cnt);
       // the force on the sources is minus the accumulated terms
-      float* r = R + (size_t)i * 3 * GS + lane;
 #pragma unroll
       for (int q = 0; q < MS2; q++) {
+        const int e = gb * GS + lane + 64 * q;
         const float2 rx = up2(RX[q]), ry = up2(RY[q]), rz = up2(RZ[q]);
-        r[64 * q] = -rx.x; r[64 * q + 32] = -rx.y;
-        r[GS + 64 * q] = -ry.x; r[GS + 64 * q + 32] = -ry.y;
-        r[2 * GS + 64 * q] = -rz.x; r[2 * GS + 64 * q + 32] = -rz.y;
+        atomicAdd(fs + e, od_fix(-rx.x, 0.f));
+        atomicAdd(fs + e + 32, od_fix(-rx.y, 0.f));
+        atomicAdd(fs + T + e, od_fix(-ry.x, 0.f));
+        atomicAdd(fs + T + e + 32, od_fix(-ry.y, 0.f));
+        atomicAdd(fs + 2 * T + e, od_fix(-rz.x, 0.f));
+        atomicAdd(fs + 2 * T + e + 32, od_fix(-rz.y, 0.f));
       }
     }
 #pragma unroll
     for (int kt = 0; kt < MT; kt++) {
-      od_acc2(CUT_H(0, kt), CUT_H(3, kt), sum2(AX[kt]));
-      od_acc2(CUT_H(1, kt), CUT_H(4, kt), sum2(AY[kt]));
-      od_acc2(CUT_H(2, kt), CUT_H(5, kt), sum2(AZ[kt]));
+      const int e = ga * GT + lane + 32 * kt;
+      atomicAdd(fa + e, od_fix(sum2(AX[kt]), 0.f));
+      atomicAdd(fa + T + e, od_fix(sum2(AY[kt]), 0.f));
+      atomicAdd(fa + 2 * T + e, od_fix(sum2(AZ[kt]), 0.f));
     }
   }
-  if (!HS && cur >= 0) {
-    float* t = Tg + (size_t)segid[i1 - 1] * 6 * GT + lane;
-#pragma unroll
-    for (int q = 0; q < 6 * MT; q++) t[(q / MT) * GT + 32 * (q % MT)] = hreg[q];
-  }
-#undef CUT_H
   __syncthreads();
 
-  // 3. fixed-order sums of the slots, added to the slots' fixed-point accumulators (tile a's
-  // target sums and tile b's reaction sums; one sum per slot on a diagonal tile)
+  // 3. the block's words into the ions' global accumulators, and cleared for the next tile pair
   for (int e = tid; e < T; e += kWarps * 32) {
-    const int g = e / GT, l = e % GT;
-    float hx = 0.f, hy = 0.f, hz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
-    for (int s = gs0[g]; s <= gs1[g]; s++) {
-      const float* t = Tg + (size_t)s * 6 * GT + l;
-      acc2x2(hx, lx, t[0], t[3 * GT]);
-      acc2x2(hy, ly, t[GT], t[4 * GT]);
-      acc2x2(hz, lz, t[2 * GT], t[5 * GT]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const unsigned long long va = fa[c * T + e];
+      if (va) atomicAdd(acc + c * stride + (size_t)a * T + e, va);
+      fa[c * T + e] = 0ull;
+      if (!diag) {
+        const unsigned long long vb = fb[c * T + e];
+        if (vb) atomicAdd(acc + c * stride + (size_t)b * T + e, vb);
+        fb[c * T + e] = 0ull;
+      }
     }
-    if (!diag) {
-      const size_t ia = (size_t)a * T + e;
-      od_fix_add(acc + ia, hx, lx);
-      od_fix_add(acc + stride + ia, hy, ly);
-      od_fix_add(acc + 2 * stride + ia, hz, lz);
-      hx = hy = hz = lx = ly = lz = 0.f;
-    }
-    const int gb = e / GS, l2 = e % GS;
-    for (int ga = 0; ga < NBT; ga++) {
-      const int it = item_of[ga * NBS + gb];
-      if (it < 0 || (diag && cut_diag_mode<GT, GS>(ga, gb) == 1)) continue;
-      const float* r = R + (size_t)it * 3 * GS + l2;
-      od_acc2(hx, lx, r[0]);
-      od_acc2(hy, ly, r[GS]);
-      od_acc2(hz, lz, r[2 * GS]);
-    }
-    const size_t ib = (size_t)b * T + e;
-    od_fix_add(acc + ib, hx, lx);
-    od_fix_add(acc + stride + ib, hy, ly);
-    od_fix_add(acc + 2 * stride + ib, hz, lz);
   }
-  __syncthreads();  // the next tile pair rewrites the list and the slots
+  __syncthreads();  // the next tile pair rewrites the list and the words
   return cnt;
 }
 
@@ -464,8 +393,19 @@ struct cutn3_tile<true, MT, MS, PA> {
 // every listed tile pair, each unordered ion pair once (static assignment: pair k to block
 // k mod grid), group pairs beyond the cutoff skipped. BAL: the balanced list routine above
 // (512-ion tiles); otherwise the staggered tile-pair routine.
+// blocks per SM the registers of the balanced tile pair are budgeted for. Measured on GB300 at
+// 2^19 ions (field_chain), ms per step: with switching 32.9 (4 blocks of at most 64 registers),
+// 34.2 (3 blocks), 35.8 with per-item slots in shared memory summed in a fixed order (74 KB per
+// block, 3 blocks); hard cutoff 30.6 (3 blocks), 31.6 (4 blocks: its exact-decision branch
+// spills at 64 registers), 31.9 with the slots.
+template <int CUT>
+struct cut_blocks {
+  static constexpr int value = CUT == 2 ? 3 : 4;
+};
+
 template <int MT, int MS, int PA, int CUT, bool COUNT, bool BAL>
-__global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCKS))
+__global__ void __launch_bounds__(kWarps * 32, (BAL ? cut_blocks<CUT>::value
+                                                                : n3_traits<MT, MS, PA>::MIN_BLOCKS))
     k_pairs_cutn3(const float* __restrict__ xs, const float* __restrict__ ys,
                   const float* __restrict__ zs, int nslots, int nT,
                   const int2* __restrict__ pairs, const int32_t* __restrict__ npairs,
@@ -478,10 +418,13 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   unsigned int cnt = 0;
   if constexpr (BAL) {
     const n3_consts kc = make_consts(cut);
+    unsigned long long* const f = reinterpret_cast<unsigned long long*>(sm);
+    for (int e = threadIdx.x; e < 6 * cut_traits<MT, MS>::T; e += kWarps * 32) f[e] = 0ull;
+    __syncthreads();
     for (int k = blockIdx.x; k < np; k += gridDim.x) {
       const int2 ab = pairs[k];
-      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, acc, (size_t)nslots, kc, ab.x, ab.y,
-                                               sm, gbox, cull2, cut.in2);
+      cnt += cut_tile_pair<MT, MS, CUT, COUNT>(xs, ys, zs, acc, (size_t)nslots, kc, ab.x,
+                                                  ab.y, sm, gbox, cull2, cut.in2);
     }
   } else {
     for (int k = blockIdx.x; k < np; k += gridDim.x) {
@@ -560,8 +503,28 @@ bool od_cutn3_supported(int ipt, int T) {
   return (ipt == 2 && T == 512) || (ipt == 4 && T == 1024);
 }
 
+// dynamic shared memory of the balanced tile pair
+constexpr size_t kCutBalSmem = cut_traits<2, 2>::SMEM;
+
+// resident blocks per SM of the production pair kernel (the persistent grid is this times the
+// SM count)
+int od_cutn3_blocks_per_sm(int ipt, int T, bool hard) {
+  int nb = 0;
+  cudaError_t e = cudaErrorInvalidValue;
+  if (ipt == 2 && T == 512)
+    e = hard ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &nb, k_pairs_cutn3<2, 2, 1, 2, false, true>, kWarps * 32, kCutBalSmem)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &nb, k_pairs_cutn3<2, 2, 1, 1, false, true>, kWarps * 32, kCutBalSmem);
+  else if (ipt == 4 && T == 1024)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_pairs_cutn3<4, 4, 1, 1, false, false>,
+                                                      kWarps * 32, n3_traits<4, 4, 1>::SMEM);
+  if (e != cudaSuccess) cudaGetLastError();
+  return e == cudaSuccess && nb > 0 ? nb : 3;
+}
+
 cudaError_t od_cutn3_prepare(int ipt, int T) {
-  if (ipt == 2 && T == 512) return prepare_cutn3<2, 2, true>((int)cut_traits<2, 2>::SMEM);
+  if (ipt == 2 && T == 512) return prepare_cutn3<2, 2, true>((int)kCutBalSmem);
   if (ipt == 4 && T == 1024)
     return prepare_cutn3<4, 4, false>((int)n3_traits<4, 4, 1>::SMEM);
   return cudaErrorInvalidValue;
@@ -598,9 +561,9 @@ cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, flo
     }                                                                                         \
   } while (0)
 #define OD_CUTN3L(MT, MS, CUT, CNT, BAL, SM)                                                  \
-  k_pairs_cutn3<MT, MS, 1, CUT, CNT, BAL><<<L.grid, kWarps * 32, SM, s>>>(                    \
+  k_pairs_cutn3<MT, MS, 1, CUT, CNT, BAL><<<sw ? L.grid : L.grid_hard, kWarps * 32, SM, s>>>( \
       L.xs, L.ys, L.zs, L.nslots, L.nT, L.pairs, np, L.acc, cut, L.gbox, rc2m, pair_count)
-  if (L.ipt == 2 && L.T == 512) OD_CUTN3(2, 2, true, (cut_traits<2, 2>::SMEM));
+  if (L.ipt == 2 && L.T == 512) OD_CUTN3(2, 2, true, kCutBalSmem);
   else if (L.ipt == 4 && L.T == 1024) OD_CUTN3(4, 4, false, (n3_traits<4, 4, 1>::SMEM));
   else return cudaErrorInvalidValue;
 #undef OD_CUTN3L

@@ -121,7 +121,7 @@ struct od_cutn3 {
   int2* pairs;                      // [nT (nT + 1) / 2] listed pairs, row-major
   unsigned long long* acc;          // [3][nslots] fixed-point ion–ion sums per sorted slot
   double rc_d;                      // cutoff / r_D_e in FP64 (the hard cutoff's exact test)
-  int grid;                         // persistent blocks of the pair kernel
+  int grid, grid_hard;              // persistent blocks of the pair kernel (switching, hard)
 };
 // cell grid of the tile-pair cutoff for N ions in a cylinder of radius R and height H (any
 // unit): nb cubes of side `side` (that unit) along z, G^3 cells each
@@ -130,6 +130,7 @@ od_cgrid od_cutn3_grid(int N, double R, double H);
 size_t od_cutn3_bytes(int N, int T, int ncells);
 bool od_cutn3_supported(int ipt, int T);
 cudaError_t od_cutn3_prepare(int ipt, int T);
+int od_cutn3_blocks_per_sm(int ipt, int T, bool hard);  // after od_cutn3_prepare
 cudaError_t od_launch_cutoff_n3(const od_cutn3& L, const float4* pos, int n, float4* part_hi,
                                 float4* part_lo, float rho0, float rc, float rs, uint32_t* err,
                                 unsigned long long* pair_count, cudaStream_t s);
