@@ -483,8 +483,9 @@ size_t od_cutn3_bytes(int N, int T, int ncells) {
 
 // cutoff tile-pair shapes: (ipt, T) = (2, 512) the balanced list with 2 x 2 targets x sources
 // per lane, (4, 1024) the staggered tile pair with 4 x 4. Measured on GB300 at 2^19 ions
-// (field_chain): 45.2 ms per step with (2, 512), 48.1 with the balanced list at 4 x 2 (128-ion
-// target groups: more arithmetic per shuffle, but coarser culling), 55.7 with (4, 1024).
+// (field_chain), ms per step: 32.9 with (2, 512); the balanced list at 4 x 2 (128-ion target
+// groups: more arithmetic per shuffle, but coarser culling) 33.2 with 3 blocks per SM and 34.3
+// with 4 (it spills at 64 registers); the staggered (4, 1024) 55.7 in an earlier form.
 template <int MT, int MS, bool BAL>
 cudaError_t prepare_cutn3(int smem) {
   void* fn[4] = {(void*)k_pairs_cutn3<MT, MS, 1, 1, false, BAL>,
