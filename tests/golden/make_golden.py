@@ -73,6 +73,30 @@ def main(ref):
             "N": 2**17, "n": 200000, "d_t": 1e-11, "avg_after": 150000, "grain_r": 1e-5,
             "grain_z_lambda": -1.0, "method": "consistent", "q0_e": 0.0, "q": qrow[1],
             "F_orbit_z": frow[1], "F_collect_z": frow[2]})
+    # two grains of given charge (Piel 2017, Figs. 6 and 7): per point the time averages of
+    # orbit + dust-dust force on each grain, (x, z), printed by the launch script as
+    # "<parameter>\t<F1x>\t<F1z>\t<F2x>\t<F2z>" after its run log
+    two = {"T_e": 29011.0, "T_i": 290.11, "n_inf": 1e14, "m_i": 6.6335209e-26, "R_lambda": 3.0,
+           "H_lambda": 6.0, "N": 2**17, "distribution": "Maxwellian", "method": "given"}
+    for fig, log, key in (("Figure6", "outputPiel2017Fig6", "M"), ("Figure7", "outputPiel2017Fig7", "d_x")):
+        script = open(os.path.join(ex, "Piel2017", fig, f"launchPiel2017{fig}.py")).read()
+        par = {
+            "n": int(re.search(r"\bn = (\d+)", script).group(1)),
+            "d_t": float(re.search(r"d_t = ([0-9.e+-]+)", script).group(1)),
+            "grain_r": float(re.search(r"\br = ([0-9.e+-]+)", script).group(1)),
+            "q0_e": float(re.search(r"q = ([0-9.e+-]+) \* plasmaParametersInSIUnits\.e", script).group(1)),
+            "avg_after": int(re.search(r"if i > (\d+):", script).group(1)),
+        }
+        for line in open(os.path.join(ex, "Piel2017", fig, log)):
+            m = re.match(r"^([0-9.]+)\t([-0-9.e+]+)\t([-0-9.e+]+)\t([-0-9.e+]+)\t([-0-9.e+]+)\s*$", line)
+            if not m:
+                continue
+            v, f1x, f1z, f2x, f2z = (float(x) for x in m.groups())
+            run = {**two, **par, "name": f"piel2017_{fig.lower().replace('figure', 'fig')}_{key}{v}",
+                   "source": f"examples/Piel2017/{fig}/{log}", "M": v if key == "M" else 1.0,
+                   "grains_lambda": [[0.0, 0.0, -0.5], [v if key == "d_x" else 0.5, 0.0, 0.5]],
+                   "F1": [f1x, f1z], "F2": [f2x, f2z]}
+            out["runs"].append(run)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_examples.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)
