@@ -206,7 +206,8 @@ const char* od_last_error(const od_handle* h);
  * Positions are held cell-relative: per axis a cell index c on a grid of side s (in Debye
  * lengths, the smallest power of two not below 1/256 of the domain's half extent) and the FP32 offset
  * x - c s, rounded once from the FP64 input; the force, flag and injection kernels read the
- * absolute FP32 position fmaf(c, s, offset) derived from it each step. */
+ * absolute FP32 position fmaf(c, s, offset) derived from it each step. A non-finite position or
+ * velocity is OD_ERR_INVALID (nothing is copied). */
 od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n);
 
 /* Samples the initial ion state on the device (replaces the host loops of opendust.py:373-451):

@@ -662,10 +662,18 @@ static void to_rel_state(const od_handle* h, const double* pos, int64_t n,
   }
 }
 
+static bool all_finite(const double* a, int64_t n) {
+  for (int64_t i = 0; i < n; i++)
+    if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
 extern "C" od_status od_set_state(od_handle* h, const double* pos, const double* vel, int64_t n) {
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!pos || !vel) return fail(h, OD_ERR_INVALID, "pos/vel is NULL");
   if (n != h->N) return fail(h, OD_ERR_INVALID, "n must equal the configured n_ions");
+  if (!all_finite(pos, 3 * n) || !all_finite(vel, 3 * n))
+    return fail(h, OD_ERR_INVALID, "a position or velocity is not finite");
   OD_CK(h, cudaSetDevice(h->device));
   std::vector<float4> xp, vp, rel;
   to_device_units(h, pos, vel, n, xp, &vp);
@@ -2003,6 +2011,8 @@ extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
   if (!h) return fail(nullptr, OD_ERR_INVALID, "handle is NULL");
   if (!h->shard) return fail(h, OD_ERR_STATE, "not a shard handle (od_shard_create)");
   if (!pos_all || !vel_own) return fail(h, OD_ERR_INVALID, "pos_all/vel_own is NULL");
+  if (!all_finite(pos_all, 3 * h->n_total) || !all_finite(vel_own, 3 * h->N))
+    return fail(h, OD_ERR_INVALID, "a position or velocity is not finite");
   OD_CK(h, cudaSetDevice(h->device));
   std::vector<float4> xa, vp, xo, ra, ro;
   to_rel_state(h, pos_all, h->n_total, ra, xa);  // every shard's sources, as their owners hold them

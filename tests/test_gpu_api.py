@@ -77,3 +77,26 @@ def test_bounded_wait_runs_out_and_context_survives(gpu_lib):
         eng.set_state(pos, vel)
         eng.step(2)
         assert np.isfinite(eng.series()["q"]).all()
+
+
+def test_set_state_rejects_non_finite(gpu_lib):
+    # a NaN or infinite position or velocity is refused before anything reaches the device, and
+    # the handle keeps stepping from its last valid state
+    from opendust_gb300 import _lib
+    from tests._util import case
+
+    holder, pos, vel, *_ = case(N=2048, n=2, seed=61)
+    with _lib.Engine(holder) as eng:
+        eng.set_state(pos, vel)
+        bad = pos.copy()
+        bad[17, 2] = np.nan
+        with pytest.raises(_lib.OpenDustError) as e:
+            eng.set_state(bad, vel)
+        assert _lib.STATUS[e.value.status] == "OD_ERR_INVALID" and "not finite" in str(e.value)
+        vbad = vel.copy()
+        vbad[3, 0] = np.inf
+        with pytest.raises(_lib.OpenDustError):
+            eng.set_state(pos, vbad)
+        eng.step(1)
+        p, v = eng.get_state()
+        assert np.isfinite(p).all() and np.isfinite(v).all()
