@@ -601,10 +601,12 @@ extern "C" od_status od_destroy(od_handle* h) {
 static void to_device_units(const od_handle* h, const double* pos, const double* vel, int64_t n,
                             std::vector<float4>& xp, std::vector<float4>* vp) {
   const double lam = h->hp.lam, vunit = h->hp.vunit;
-  xp.resize(n);
-  for (int64_t i = 0; i < n; i++)
-    xp[i] = make_float4((float)(pos[3 * i] / lam), (float)(pos[3 * i + 1] / lam),
-                        (float)(pos[3 * i + 2] / lam), 0.f);
+  if (pos) {  // NULL: velocities only (the state's positions come from to_rel_state)
+    xp.resize(n);
+    for (int64_t i = 0; i < n; i++)
+      xp[i] = make_float4((float)(pos[3 * i] / lam), (float)(pos[3 * i + 1] / lam),
+                          (float)(pos[3 * i + 2] / lam), 0.f);
+  }
   if (vp) {
     vp->resize(n);
     for (int64_t i = 0; i < n; i++)
@@ -676,7 +678,7 @@ extern "C" od_status od_set_state(od_handle* h, const double* pos, const double*
     return fail(h, OD_ERR_INVALID, "a position or velocity is not finite");
   OD_CK(h, cudaSetDevice(h->device));
   std::vector<float4> xp, vp, rel;
-  to_device_units(h, pos, vel, n, xp, &vp);
+  to_device_units(h, nullptr, vel, n, xp, &vp);
   to_rel_state(h, pos, n, rel, xp);
   OD_CK(h, cudaMemcpyAsync(h->b.rel, rel.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
   OD_CK(h, cudaMemcpyAsync(h->b.pos, xp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, h->stream));
@@ -2016,7 +2018,7 @@ extern "C" od_status od_shard_set_state(od_handle* h, const double* pos_all,
   OD_CK(h, cudaSetDevice(h->device));
   std::vector<float4> xa, vp, xo, ra, ro;
   to_rel_state(h, pos_all, h->n_total, ra, xa);  // every shard's sources, as their owners hold them
-  to_device_units(h, pos_all + 3 * h->ion0, vel_own, h->N, xo, &vp);
+  to_device_units(h, nullptr, vel_own, h->N, xo, &vp);
   to_rel_state(h, pos_all + 3 * h->ion0, h->N, ro, xo);
   std::vector<float> c(h->n_total);
   float* dst[3] = {h->ssx, h->ssy, h->ssz};
