@@ -1,8 +1,9 @@
 // od_cutn3.cu — ion–ion forces within a cutoff over tile pairs (cutoff variant 3): ions sorted
 // along a Hilbert curve of a cell grid, 512- or 1024-ion tiles of consecutive sorted ions, the tile
 // pairs whose bounding boxes come within the cutoff listed, each unordered pair inside the cutoff
-// evaluated once (od_n3_pair.cuh) with 64-ion group pairs beyond it skipped, and the tiles' rows of
-// partial sums added in a fixed order. Every result bit is independent of scheduling.
+// evaluated once (od_n3_pair.cuh) with 64-ion group pairs beyond it skipped, and the sums added
+// as 64-bit fixed point with integer atomics (per-ion words in shared memory, then per-slot
+// accumulators). Every result bit is independent of scheduling.
 #include "od_hilbert.h"
 #include "od_n3_pair.cuh"
 
