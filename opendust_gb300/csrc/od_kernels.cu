@@ -883,20 +883,29 @@ __device__ __forceinline__ void correct_orbit_body(
       for (int k = 0; k < kBlk / 32; k++) v += s_orb[k][tid];
       orbit_part[(size_t)blk * p.P * 3 + tid] = v;
     }
-    // move the ion–ion sums of unflagged ions to the re-injected positions
+    // move the ion–ion sums of unflagged ions to the re-injected positions (the entries are
+    // loaded kU at a time so that their loads overlap; the terms are added in list order)
     if (K > 0 && live && !((flags[i >> 5] >> (i & 31)) & 1u)) {
       float gx = 0.f, gy = 0.f, gz = 0.f;
       const bool cut = p.method == OD_FORCE_CUTOFF;
-      for (int k = 0; k < K; k++) {
-        const float4 qn = list_new[k], qo = list_old[k];
-        float dx = x.x - qn.x, dy = x.y - qn.y, dz = x.z - qn.z;
-        float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
-        float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
-        gx = fmaf(c, dx, gx); gy = fmaf(c, dy, gy); gz = fmaf(c, dz, gz);
-        dx = x.x - qo.x; dy = x.y - qo.y; dz = x.z - qo.z;
-        r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
-        c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
-        gx = fmaf(-c, dx, gx); gy = fmaf(-c, dy, gy); gz = fmaf(-c, dz, gz);
+      constexpr int kU = 4;
+      for (int k0 = 0; k0 < K; k0 += kU) {
+        float4 qn[kU], qo[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++)
+          if (k0 + u < K) { qn[u] = list_new[k0 + u]; qo[u] = list_old[k0 + u]; }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+          if (k0 + u >= K) break;
+          float dx = x.x - qn[u].x, dy = x.y - qn[u].y, dz = x.z - qn[u].z;
+          float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+          float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+          gx = fmaf(c, dx, gx); gy = fmaf(c, dy, gy); gz = fmaf(c, dz, gz);
+          dx = x.x - qo[u].x; dy = x.y - qo[u].y; dz = x.z - qo[u].z;
+          r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+          c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+          gx = fmaf(-c, dx, gx); gy = fmaf(-c, dy, gy); gz = fmaf(-c, dz, gz);
+        }
       }
       float4 h = fhi[i], l = flo[i];
       od_acc2(h.x, l.x, gx); od_acc2(h.y, l.y, gy); od_acc2(h.z, l.z, gz);
@@ -915,16 +924,28 @@ __device__ __forceinline__ void correct_orbit_body(
       float ax = 0.f, ay = 0.f, az = 0.f;
       int cnt = 0;
       const int nj = ssx ? nsrc : p.N;
-      for (int j = tid; j < nj; j += kBlk) {
-        const float4 q = ssx ? make_float4(ssx[j], ssy[j], ssz[j], 0.f) : pos[j];
-        const float dx = xi.x - q.x, dy = xi.y - q.y, dz = xi.z - q.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
-        const float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
-        ax = fmaf(c, dx, ax); ay = fmaf(c, dy, ay); az = fmaf(c, dz, az);
-        if (++cnt == 64) {
-          od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
-          ax = ay = az = 0.f;
-          cnt = 0;
+      // sources j = tid, tid + kBlk, ... in that order, loaded kU at a time so that their loads
+      // overlap (a load per iteration waited the full memory latency each time)
+      constexpr int kU = 8;
+      for (int j0 = tid; j0 < nj; j0 += kU * kBlk) {
+        float4 q[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+          const int j = j0 + u * kBlk;
+          if (j < nj) q[u] = ssx ? make_float4(ssx[j], ssy[j], ssz[j], 0.f) : pos[j];
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+          if (j0 + u * kBlk >= nj) break;
+          const float dx = xi.x - q[u].x, dy = xi.y - q[u].y, dz = xi.z - q[u].z;
+          const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, 1e-30f)));
+          const float c = cut ? od_pair_c_cut(r2, p) : od_pair_c(r2, p.rho0);
+          ax = fmaf(c, dx, ax); ay = fmaf(c, dy, ay); az = fmaf(c, dz, az);
+          if (++cnt == 64) {
+            od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
+            ax = ay = az = 0.f;
+            cnt = 0;
+          }
         }
       }
       od_acc2(hx, lx, ax); od_acc2(hy, ly, ay); od_acc2(hz, lz, az);
@@ -998,13 +1019,21 @@ __device__ __forceinline__ void tail_body(const od_dparams& p, od_dstate* __rest
   __shared__ double qn[OD_MAX_GRAINS];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int P = p.P, nc = P * 3;
-  for (int c = 0; c < nc; c++) {
-    double v = 0;
-    // L2 loads: the partials may come from other blocks of the same launch (fused tail)
-    for (int b = tid; b < nb; b += kBlk) v += __ldcg(orbit_part + (size_t)b * nc + c);
+  for (int g = 0; g < P; g++) {
+    double v[3] = {0, 0, 0};
+    // L2 loads: the partials may come from other blocks of the same launch (fused tail); the
+    // three components of a grain are loaded together so that their latencies overlap
+    for (int b = tid; b < nb; b += kBlk) {
+      const double* o = orbit_part + (size_t)b * nc + 3 * g;
+      const double a0 = __ldcg(o), a1 = __ldcg(o + 1), a2 = __ldcg(o + 2);
+      v[0] += a0; v[1] += a1; v[2] += a2;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_red[w][c] = v;
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
+      if (lane == 0) s_red[w][3 * g + d] = v[d];
+    }
   }
   const int64_t step = ds->step;
   if (tid < P)
