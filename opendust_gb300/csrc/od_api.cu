@@ -376,7 +376,7 @@ static constexpr size_t OD_N3_BUDGET = (size_t)32 << 30;
 // sort, boxes, tile-pair list and slot accumulators (0.3 GB at 2^20 ions); the budget bounds the
 // tile-pair list for very large N, beyond which 1024-ion tiles or the cell stencil take over.
 static constexpr size_t OD_CUTN3_BUDGET = (size_t)64 << 30;
-static bool uses_n3_default(int Npad) { return Npad >= 32768; }
+static bool uses_n3_default(int Npad) { return Npad >= 16384; }
 static od_status set_plan_n3(od_handle* h, int ions_per_lane, int tile);
 
 static od_pair_plan default_plan(int Npad, int sms) {

@@ -119,6 +119,7 @@ cudaError_t prepare_n3() {
 // (plan ipt, tile) -> instantiation: ipt 2 and 4 take as many sources as targets per lane,
 // ipt 8 takes 8 targets and 2 sources per lane.
 #define OD_N3_CASES(CALL)                                                  \
+  case 20512: return CALL(2, 2, 1);                                        \
   case 21024: return CALL(2, 2, 2); case 22048: return CALL(2, 2, 4);      \
   case 24096: return CALL(2, 2, 8); case 41024: return CALL(4, 4, 1);      \
   case 42048: return CALL(4, 4, 2); case 44096: return CALL(4, 4, 4);      \
@@ -148,12 +149,14 @@ cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int
 }
 
 int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
-  // 4 x 4 with 1024-ion tiles up to 2^16 ions (2.79e12 pair terms/s at 2^16 against 2.51e12
+  // 2 x 2 with 512-ion tiles at 2^14 ions (1.82e12 pair terms/s against 1.77e12 for the
+  // directed-pair kernel and 1.63e12 for 4 x 4 with 1024-ion tiles, which leave SMs idle: 136
+  // tile pairs), 4 x 4 with 1024-ion tiles up to 2^16 ions (2.79e12 at 2^16 against 2.51e12
   // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.91e12 at 2^17 against 2.87e12 for 4 x 4,
   // 2.99e12 at 2^18, 3.05e12 at 2^20), then 4 x 4 with 4096-ion tiles: the first whose
   // accumulators fit the budget (always: 24 bytes per ion)
-  const int cand[3][2] = {{4, 1024}, {8, 2048}, {4, 4096}};
-  for (int c = Npad <= (1 << 16) ? 0 : 1; c < 3; c++)
+  const int cand[4][2] = {{2, 512}, {4, 1024}, {8, 2048}, {4, 4096}};
+  for (int c = Npad <= (1 << 14) ? 0 : (Npad <= (1 << 16) ? 1 : 2); c < 4; c++)
     if (sizeof(float) * od_n3_floats(Npad, cand[c][1]) <= budget_bytes) {
       *ipt = cand[c][0];
       return cand[c][1];

@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 
 
 PLANS = [(256, 1, 0), (128, 2, 0), (256, 1, 1), (128, 2, 2), (256, 2, 2), (128, 2, 3), (256, 2, 3),
-         (256, 2, 4), (256, 1, 5), (128, 1, 6), (256, 1, 6), (256, 2, 7), (256, 4, 7), (256, 8, 7)]
+         (256, 2, 4), (256, 1, 5), (128, 1, 6), (256, 1, 6), (256, 2, 7), (256, 2, 7, 512),
+         (256, 4, 7), (256, 8, 7)]
 
 
 @pytest.mark.parametrize("plan", PLANS)
@@ -36,7 +37,7 @@ def test_force_snapshot_all_targets(gpu_lib, plan):
     assert err.max() <= 1e-5
 
 
-@pytest.mark.parametrize("N,plan", [(2**18, None), (2**20, None), (2**20, (256, 2, 3)),
+@pytest.mark.parametrize("N,plan", [(2**14, None), (2**18, None), (2**20, None), (2**20, (256, 2, 3)),
                                     (2**20, (256, 1, 5)), (2**18, (256, 2, 7)),
                                     (2**20, (256, 4, 7, 4096)), (2**18, (256, 4, 7, 2048))])
 def test_force_snapshot_large(gpu_lib, N, plan):
@@ -53,7 +54,7 @@ def test_force_snapshot_large(gpu_lib, N, plan):
     assert err.max() <= 1e-5
 
 
-@pytest.mark.parametrize("N,plan", [(5000, (256, 4, 7, 2048)), (5000, (256, 4, 7, 4096)),
+@pytest.mark.parametrize("N,plan", [(5000, (256, 2, 7, 512)), (5000, (256, 4, 7, 2048)), (5000, (256, 4, 7, 4096)),
                                     (5000, (256, 2, 7, 4096)), (9000, (256, 2, 7, 1024)),
                                     (5000, (256, 8, 7, 2048)), (9000, (256, 8, 7, 4096))])
 def test_each_pair_once_ragged_tiles(gpu_lib, N, plan):
