@@ -649,10 +649,17 @@ __device__ double block_sum_1024(double v) {
 }
 
 __device__ __forceinline__ float tab_eval(const od_dparams& p, int t, float u) {
+  // the first node i in [1, n - 1) with u <= txi[i], else n - 1 (txi is a CDF: non-decreasing),
+  // by bisection
   const int n = p.tn[t];
-  int i = 1;
   const double ud = u;
-  while (i < n - 1 && ud > p.txi[t][i]) i++;
+  int lo = 1, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ud > p.txi[t][mid]) lo = mid + 1;
+    else hi = mid;
+  }
+  const int i = lo;
   return p.tv[t][i - 1] + (u - (float)p.txi[t][i - 1]) * p.tsl[t][i];
 }
 
@@ -738,14 +745,16 @@ __device__ __forceinline__ void collect_inject_body(
     list_v[k] = v;
   }
   __syncthreads();
+  // warp 0 sums the grains' collected counts and momenta while warps 1.. re-inject
   list_sums(p, ds, K, list_bits, list_v);
+  if (tid < 32) return;
   const uint32_t step = (uint32_t)(ds->step + ds->rng_base);
   if (p.dist == OD_DIST_MATTHEWS) {
     // the fork (chains/matthews.py:653-682): ions past |z| = H/2 or inside a grain re-enter
     // through the top face; ions past the side wall keep their position and have the radial
     // velocity component reversed, with the normal taken before any re-injection
     const int grains = (1 << p.P) - 1;
-    for (int k = tid; k < K; k += kCT) {
+    for (int k = tid - 32; k < K; k += kCT - 32) {
       const int i = list[k];
       const int bits = list_bits[k];
       const float4 xo = list_old[k];
@@ -770,7 +779,7 @@ __device__ __forceinline__ void collect_inject_body(
     }
     return;
   }
-  for (int k = tid; k < K; k += kCT) {
+  for (int k = tid - 32; k < K; k += kCT - 32) {
     const int i = list[k];
     float4 x, v;
     inject_one(p, (uint32_t)(p.ion0 + i), step, x, v);
