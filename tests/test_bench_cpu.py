@@ -58,3 +58,18 @@ def test_cutoff_scaling_workload_matches_reference_benchmark():
     holder, _ = build_simulation(plasma, sim, grains, d, trap=[0.0] * 15, **ext)
     assert abs(holder.cfg.cutoff / lam - 3.2) < 1e-12 and abs(holder.cfg.switch_dist / lam - 3.0) < 1e-12
     assert set(bench.CUTOFF_SCRIPT_PUBLISHED_S) == {1, 2, 4, 8, 32}
+
+
+def test_reference_arm_cutoff_workloads():
+    # the reference arm on the cutoff workloads (the oracle's cell list), switching and hard
+    for extra in ([], ["--hard-cutoff"]):
+        out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                              "--workload", "cutoff_scaling", "--scale", "1", "--steps", "1",
+                              "--warmup", "1"] + extra,
+                             capture_output=True, text=True, timeout=600, cwd=ROOT)
+        assert out.returncode == 0, out.stderr[-2000:]
+        line = json.loads(out.stdout.strip().splitlines()[-1])
+        assert line["impl"] == "reference" and line["value"] > 0
+        assert line["config"]["n_ions"] == 2**15 and line["config"]["steps_in_workload"] == 3
+        assert ("hard" in line["config"]["force"]) == bool(extra)
+        assert "within the cutoff" in line["cpu_baseline"]["sample"]
