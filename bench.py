@@ -13,18 +13,25 @@ kick, flags, ordered compaction, re-injection, grain sums, FP64 tail).
              including the initial force evaluation), then per step od_step and od_get_series of
              that step (device->host), then od_get_state (device->host); wall clock.
   roofline   the all-pairs force evaluation: N(N-1) directed pair interactions x 25 FP32 flops
-             per launch over its CUDA-event duration, against the FP32 FMA peak measured on the
-             same GPU. The default kernel from 2^15 ions (variant 7) evaluates each unordered
-             pair once and applies it to both ions, so it does about half those flops: its
-             fraction can exceed what a directed-pair kernel could reach.
+             per launch over its CUDA-event duration, against the larger of the FP32 FMA probe
+             and the SMs' FP32 rate at the sampled clock. The default kernel from 2^14 ions
+             (variant 7) evaluates each unordered pair once and applies it to both ions, so it
+             does about half those flops (executed_frac). Cutoff workloads credit the pairs
+             inside r_c, counted by one more, untimed step.
+Other workloads (--workload): small_plain (C1, 16384 ions), field_chain (C3, 2^19 ions, 2 lambda
+cutoff; --hard-cutoff without the switching function), cutoff_scaling (the reference's cutoff
+benchmark, N = k*2^15 with --scale k, plus the wall time of its script through simulate()),
+sweep (C4: 64 simulations batched against the plain path back to back) and serve (C5: a Poisson
+request stream through the continuous-batching server against the plain path).
   cpu_baseline  the CPU oracle (FP64 C restatement of the reference step, OpenMP over all host
              cores) on a bounded sample: the reference's two ion–ion evaluations per step for T
              target ions against all N sources plus one linear pass over all N ions.
 
 --impl reference times that CPU restatement alone (the reference's own OpenMM/CuPy path
 cannot be installed or run on this machine) and prints the same metric.
-Multi-GPU (torchrun, N > 1): independent replicas, one per GPU (the plain path does not
-shard); value = ion-steps of all ranks / max over ranks of the timed duration.
+Multi-GPU (torchrun, N > 1): independent replicas, one per GPU (one simulation sharded over
+GPUs is opendust_gb300.shard, not this benchmark); value = ion-steps of all ranks / max over
+ranks of the timed duration.
 """
 from __future__ import annotations
 
