@@ -63,8 +63,11 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   const int4 w = items[blockIdx.x];
   const od_simdesc& d = sims[w.x];
   if (!od_evaluates(d.dp->force_every, d.ds->step)) return;  // force interval: no evaluation
-  n3_tile_pair<MT, MS, PA, 0, false>(d.b.sx, d.b.sy, d.b.sz, d.Npad, d.b.n3, (size_t)d.Npad,
-                                     n3_cut{d.rho0, 0.f, 0.f, 0.f}, w.y, w.z, sm);
+  // one lane step at a time (the batch's 4 x 4 spills with two: the other members' tile pairs
+  // already give every SM independent work)
+  n3_tile_pair<MT, MS, PA, 0, false, false, 1>(d.b.sx, d.b.sy, d.b.sz, d.Npad, d.b.n3,
+                                               (size_t)d.Npad, n3_cut{d.rho0, 0.f, 0.f, 0.f},
+                                               w.y, w.z, sm);
 }
 
 // Accumulators -> slab 0 of (ph, pl) as two-float sums, and cleared for the next evaluation.
@@ -149,14 +152,14 @@ cudaError_t od_launch_pairs_n3(const od_pair_plan& pl, const od_pair_io& io, int
 }
 
 int od_n3_default(int Npad, size_t budget_bytes, int* ipt) {
-  // 2 x 2 with 512-ion tiles at 2^14 ions (1.82e12 pair terms/s against 1.77e12 for the
-  // directed-pair kernel and 1.63e12 for 4 x 4 with 1024-ion tiles, which leave SMs idle: 136
-  // tile pairs), 4 x 4 with 1024-ion tiles up to 2^16 ions (2.79e12 at 2^16 against 2.51e12
-  // for 8 x 2), then 8 x 2 with 2048-ion tiles (2.91e12 at 2^17 against 2.87e12 for 4 x 4,
-  // 2.99e12 at 2^18, 3.05e12 at 2^20), then 4 x 4 with 4096-ion tiles: the first whose
-  // accumulators fit the budget (always: 24 bytes per ion)
+  // 2 x 2 with 512-ion tiles up to 2^15 ions (2.04e12 pair terms/s at 2^14 against 1.77e12 for
+  // the directed-pair kernel and 1.70e12 for 4 x 4 with 1024-ion tiles, which leave SMs idle:
+  // 136 tile pairs; 2.50e12 at 2^15 against 2.39e12), 4 x 4 with 1024-ion tiles up to 2^16
+  // (2.93e12 against 2.62e12 for 2 x 2 and 2.51e12 for 8 x 2), then 8 x 2 with 2048-ion tiles
+  // (2.91e12 at 2^17, 2.99e12 at 2^18, 3.05e12 at 2^20), then 4 x 4 with 4096-ion tiles: the
+  // first whose accumulators fit the budget (always: 24 bytes per ion)
   const int cand[4][2] = {{2, 512}, {4, 1024}, {8, 2048}, {4, 4096}};
-  for (int c = Npad <= (1 << 14) ? 0 : (Npad <= (1 << 16) ? 1 : 2); c < 4; c++)
+  for (int c = Npad <= (1 << 15) ? 0 : (Npad <= (1 << 16) ? 1 : 2); c < 4; c++)
     if (sizeof(float) * od_n3_floats(Npad, cand[c][1]) <= budget_bytes) {
       *ipt = cand[c][0];
       return cand[c][1];

@@ -120,8 +120,9 @@ __device__ __forceinline__ od_u64 shfl64(od_u64 v, int src) {
 
 // One group pair: 32 lane steps of MT x MS pair terms per lane with rotating sources. Each
 // source pack moves on as soon as its terms are done, so that its shuffles overlap the next
-// pack's arithmetic.
-template <int MT, int MS, int CUT, bool REACT, bool COUNT>
+// pack's arithmetic. UNR lane steps are interleaved (0: two for the cutoff forms, one for the
+// plain term).
+template <int MT, int MS, int CUT, bool REACT, bool COUNT, int UNR = 0>
 __device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[MT],
                                          const od_u64 (&Y)[MT], const od_u64 (&Z)[MT],
                                          od_u64 (&QX)[MS / 2], od_u64 (&QY)[MS / 2],
@@ -129,9 +130,9 @@ __device__ __forceinline__ void n3_group(const n3_consts& k, const od_u64 (&X)[M
                                          od_u64 (&AZ)[MT], od_u64 (&RX)[MS / 2],
                                          od_u64 (&RY)[MS / 2], od_u64 (&RZ)[MS / 2], int src,
                                          unsigned int& cnt) {
-  // cutoff forms: two lane steps interleaved (more independent work per warp; the 2 x 2 shape
-  // has only two packs per step)
-  constexpr int kUnroll = CUT != 0 ? 2 : 1;
+  // two lane steps interleaved give a 2 x 2 shape (two packs per step) more independent work
+  // per warp
+  constexpr int kUnroll = UNR != 0 ? UNR : (CUT != 0 ? 2 : 1);
 #pragma unroll kUnroll
   for (int st = 0; st < 32; st++) {
 #pragma unroll
@@ -211,6 +212,13 @@ struct n3_traits {
   static constexpr bool TP = MT == 8;
 };
 
+// lane steps interleaved by the tile pairs below (source-packed form): two for 2 x 2 and 4 x 4
+// (all pairs on GB300: 2 x 2 with 512-ion tiles 2.04e12 pair terms/s at 2^14 ions against 1.82e12
+// with one step; 4 x 4 with 1024-ion tiles 2.93e12 at 2^16 against 2.81e12), the n3_group
+// default otherwise
+template <int MT>
+constexpr int kN3Unroll = MT <= 4 ? 2 : 0;
+
 // (union) box of n consecutive 64-ion groups starting at group g0; 6 floats min xyz, max xyz
 __device__ __forceinline__ void group_box(const float* __restrict__ gbox, int g0, int n,
                                           float (&bx)[6]) {
@@ -230,7 +238,8 @@ __device__ __forceinline__ void group_box(const float* __restrict__ gbox, int g0
 // sm: dynamic shared memory of n3_traits::SMEM bytes. CULL skips group pairs whose 64-ion group
 // boxes (gbox) are farther apart than sqrt(cull2). Returns the directed pairs inside the cutoff
 // when COUNT.
-template <int MT, int MS, int PA, int CUT, bool COUNT, bool CULL = false>
+template <int MT, int MS, int PA, int CUT, bool COUNT, bool CULL = false,
+          int UNR = kN3Unroll<MT>>
 __device__ __forceinline__ unsigned int n3_tile_pair(const float* __restrict__ sx,
                                                      const float* __restrict__ sy,
                                                      const float* __restrict__ sz, int Npad,
@@ -353,11 +362,11 @@ __device__ __forceinline__ unsigned int n3_tile_pair(const float* __restrict__ s
   #pragma unroll
           for (int kt = 0; kt < MT; kt++) AX[kt] = AY[kt] = AZ[kt] = 0ull;
           if (mode == 2)
-            n3_group<MT, MS, CUT, true, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
-                                               cnt);
+            n3_group<MT, MS, CUT, true, COUNT, UNR>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY,
+                                                    RZ, src, cnt);
           else
-            n3_group<MT, MS, CUT, false, COUNT>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY, RZ, src,
-                                                cnt);
+            n3_group<MT, MS, CUT, false, COUNT, UNR>(k, X, Y, Z, QX, QY, QZ, AX, AY, AZ, RX, RY,
+                                                     RZ, src, cnt);
   #pragma unroll
           for (int kt = 0; kt < MT; kt++) {
             od_acc2(N3_H(0, kt), N3_H(3, kt), sum2(AX[kt]));
