@@ -284,3 +284,21 @@ def test_cutoff_cell_list_equals_double_loop():
         sub = pos[near]
         f_sub = oracle.force_targets(holder, sub, [int(np.flatnonzero(near == t)[0])], round32=False)[0]
         np.testing.assert_allclose(f_all, f_sub, rtol=1e-11, atol=1e-12 * np.linalg.norm(f_sub))
+
+
+def test_device_state_rounding():
+    # oracle.DEVICE_STATE starts a run from the device's cell-relative position state: per axis a
+    # cell of side s (the smallest power of two not below max(R, H/2) / 256, in lambda) and the
+    # offset rounded once to float, so every coordinate is within 2^-25 s of the input; plain
+    # float rounding (round32=True) is only within half an ulp of |x|
+    from tests._util import case
+
+    holder, pos, vel, plasma, sim, grains = case(N=512, n=2, seed=3, trap=np.zeros(15))
+    lam = plasma.r_D_e
+    s = 2.0 ** np.ceil(np.log2(max(sim.R, sim.H / 2) / lam / 256))
+    rel = oracle.run(holder, pos, vel, 0, 0, round32=oracle.DEVICE_STATE)["pos"]
+    f32 = oracle.run(holder, pos, vel, 0, 0, round32=True)["pos"]
+    d_rel = np.max(np.abs(rel - pos)) / lam
+    d_f32 = np.max(np.abs(f32 - pos)) / lam
+    assert d_rel <= s * 2.0**-25 * (1 + 1e-9)
+    assert d_f32 > 50 * d_rel
