@@ -63,11 +63,8 @@ __global__ void __launch_bounds__(kWarps * 32, (n3_traits<MT, MS, PA>::MIN_BLOCK
   const int4 w = items[blockIdx.x];
   const od_simdesc& d = sims[w.x];
   if (!od_evaluates(d.dp->force_every, d.ds->step)) return;  // force interval: no evaluation
-  // one lane step at a time (the batch's 4 x 4 spills with two: the other members' tile pairs
-  // already give every SM independent work)
-  n3_tile_pair<MT, MS, PA, 0, false, false, 1>(d.b.sx, d.b.sy, d.b.sz, d.Npad, d.b.n3,
-                                               (size_t)d.Npad, n3_cut{d.rho0, 0.f, 0.f, 0.f},
-                                               w.y, w.z, sm);
+  n3_tile_pair<MT, MS, PA, 0, false>(d.b.sx, d.b.sy, d.b.sz, d.Npad, d.b.n3, (size_t)d.Npad,
+                                     n3_cut{d.rho0, 0.f, 0.f, 0.f}, w.y, w.z, sm);
 }
 
 // Accumulators -> slab 0 of (ph, pl) as two-float sums, and cleared for the next evaluation.
