@@ -280,10 +280,10 @@ od_status od_set_graph(od_handle* h, int32_t enable);
  * 5: packed with one target per thread (targets_per_thread 1), 6: as 5 with every other source
  * pair on the Newton path of variant 4, 7: each unordered pair evaluated once and applied to
  * both ions (threads 256; targets_per_thread = target ions per lane: 2 or 4 with as many source
- * ions, 8 with two; jsplit = ions per tile, 1024, 2048 or 4096 (not 1024 with 8), <= 0 for the
- * default). Variants 2-7 add their sums into 64-bit fixed-point accumulators (24 bytes per ion)
- * with integer atomics, so results do not depend on the order of the GPU's blocks. From 2^15
- * ions od_create selects variant 7.
+ * ions, 8 with two; jsplit = ions per tile, 1024, 2048 or 4096 (not 1024 with 8; also 512 with
+ * 2), <= 0 for the default). Variants 2-7 add their sums into 64-bit fixed-point accumulators (24
+ * bytes per ion) with integer atomics, so results do not depend on the order of the GPU's
+ * blocks. From 2^14 ions od_create selects variant 7.
  * jsplit <= 0 picks the source split from the SM count. Takes effect at the next step.
  * Cutoff method (force_method OD_FORCE_CUTOFF): variant 0 or 2 walks a stencil of cells per
  * target cell (scalar or packed); variant 3 (the default) sorts
